@@ -1,0 +1,185 @@
+/*
+ * softmold_gb300 — C ABI of the GB300 implicit-solvent membrane MD step.
+ *
+ * The reference (SoftMold) has no FFI layer for this path: its `MD <name>`
+ * driver (MD.cpp:72-755) calls C++ templates in-process.  Each entry point
+ * below names the reference call it replaces.  All calls take and return plain
+ * host pointers and sizes; the library owns all device memory.  Status codes:
+ * 0 = OK, nonzero = error, with the message available from smd_last_error().
+ * Handles are not thread-safe; use one handle per host thread / stream.
+ *
+ * Layout conventions: per-bead vectors are AoS double x,y,z (n*3), bead order
+ * is the order of the .mpd file; constant tables are the reference's flat
+ * layouts (twoBodyFconst/Uconst: 6 doubles per ordered type pair, BEAD: 22).
+ */
+#ifndef SOFTMOLD_GB300_H
+#define SOFTMOLD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMD_ABI_VERSION 1
+
+/* Arithmetic of the pair and bonded forces. */
+enum smd_precision {
+  SMD_PLAIN_FP64 = 0, /* every force term in FP64, FP64 accumulation */
+  SMD_MIXED = 1       /* FP32 force arithmetic, int64 fixed-point accumulation,
+                         FP64 integrator, barostat and energy sums */
+};
+
+/* One membrane system (one replica).  Mirrors the Blob<double> fields the
+ * hot path reads (include/system.h:247-290). */
+typedef struct smd_system_desc {
+  int n;                        /* beads (nParticles) */
+  int n_types;                  /* nTypes */
+  const double* pos;            /* n*3, each coordinate in [0, box] */
+  const double* vel;            /* n*3 */
+  const int* type;              /* n */
+  double box[3];                /* size */
+  double cutoff;                /* rc */
+  const double* fconst;         /* 6*n_types^2 twoBodyFconst */
+  const double* uconst;         /* 6*n_types^2 twoBodyUconst */
+  int n_chain_blocks;           /* CHAIN residue blocks */
+  const int* chain_blocks;      /* n_chain_blocks*3: start, nChains, length */
+  const double* chain_consts;   /* n_chain_blocks*4: l0, kbond, abend, kbend */
+  int n_spheres;                /* beads of one BEAD residue (0 = none) */
+  const int* sphere_index;      /* n_spheres bead indices */
+  const double* sphere_consts;  /* 22*n_types^2 BEAD constants */
+  double dt;                    /* deltaT */
+  double gamma;                 /* Langevin friction */
+  double temperature;           /* kT (initialTemp) */
+  uint32_t seed;                /* .mpd seed: barostat trials and Langevin noise */
+  double tension;               /* constant-tension barostat target */
+  double delta_lxy;             /* MC box-move amplitude, 0 = barostat off */
+  int resize_rate;              /* MC move every resize_rate steps (MD.cpp:67: 8) */
+  int first_step;               /* loop index of the first step (initialTime/deltaT) */
+  double skin;                  /* Verlet-list skin in sigma (<=0: default 0.5) */
+} smd_system_desc;
+
+typedef struct smd_system smd_system;
+
+typedef struct smd_energy {
+  double pair;     /* CellOpt::computePotential */
+  double bonded;   /* sum of Blob::doChainPotential */
+  double sphere;   /* Blob::doBeadPotential */
+  double kinetic;  /* Kinetic::compute: sum v^2/2 */
+} smd_energy;
+
+typedef struct smd_mc_stats {
+  long trials;
+  long accepted;
+  double last_dU;  /* last trial's potential difference incl. tension term */
+} smd_mc_stats;
+
+/* Last error message of the calling thread; returns its length. */
+int smd_last_error(char* buf, size_t len);
+
+/* Number of visible CUDA devices (0 when none). */
+int smd_device_count(void);
+
+/* Builds the device state for one system (replaces the Verlet / Langevin /
+ * CellOpt constructors, MD.cpp:124-154).  precision: enum smd_precision. */
+int smd_create(const smd_system_desc* desc, int precision, smd_system** out);
+
+/* Builds n independent replicas that advance together in the same launches
+ * with per-replica offsets, boxes, seeds, tensions and barostat decisions. */
+int smd_create_batch(const smd_system_desc* descs, int n, int precision, smd_system** out);
+
+void smd_destroy(smd_system* h);
+
+/* Runs later work on this CUDA stream (cudaStream_t; NULL = library stream). */
+int smd_set_stream(smd_system* h, void* cuda_stream);
+
+/* Copies all beads' state, replicas concatenated (Blob::getPositions /
+ * getVelocities). */
+int smd_get_state(smd_system* h, double* pos, double* vel);
+int smd_set_state(smd_system* h, const double* pos, const double* vel);
+int smd_get_box(smd_system* h, int replica, double box[3]);
+
+/* Conservative forces at the current positions, no Langevin term:
+ * CellOpt::computeForce + Blob::doChainForce (+ doBeadForce)
+ * (include/algorithms/cellOpt.h:712-926, include/system.h:1782-1866,2043-2212). */
+int smd_compute_forces(smd_system* h, double* force_out);
+
+/* Non-bonded forces only (CellOpt::computeForce). */
+int smd_compute_pair_forces(smd_system* h, double* force_out);
+
+/* Energies at the current state, per replica (energies[n_replicas]):
+ * CellOpt::computePotential, Blob::doChainPotential, doBeadPotential and
+ * Kinetic::compute (cellOpt.h:928-1041, system.h:2487-2568, 2936-3074). */
+int smd_compute_energy(smd_system* h, smd_energy* energies);
+
+/* U(x) - U(s*x) summed over pairs within rc, CHAIN and BEAD terms, for an
+ * affine box scale s (CellOpt::computeDPotential + Blob::do*DPotential,
+ * cellOpt.h:1043-1180, system.h:3280-3384). One value per replica. */
+int smd_compute_dU(smd_system* h, const double scale[3], double* dU);
+
+/* CellOpt cell key of every bead for the reference grid nCells=int(L/rc)
+ * (cellOpt.h:532-555), computed on the GPU. */
+int smd_cell_keys(smd_system* h, int* keys);
+
+/* Unordered pairs (i<j, file order) with r < rc taken from the GPU Verlet
+ * list; writes at most cap pairs and stores the total count. */
+int smd_pair_list(smd_system* h, int* pairs, size_t cap, size_t* count);
+
+/* Start-up of MD.cpp:186-308: initial build, forces and thermostat, then the
+ * restart half-kick when initial_time != 0 (do_second), then the first
+ * half-kick and drift of the first loop step.  If energy_out is not NULL the
+ * energies at the initial positions and velocities are stored there before
+ * any update (the t = 0 measurement). */
+int smd_prepare(smd_system* h, int do_second, smd_energy* energy_out);
+
+/* Advances `steps` iterations of the MD.cpp:335-729 loop body: thermostat,
+ * pair and bonded forces, second half-kick, the MC box move on every
+ * resize_rate-th step, and the next step's first half-kick and drift.  With
+ * stop_at_measure != 0 the last iteration stops after its second half-kick so
+ * the caller can read the measured state; the next smd_advance call (steps may
+ * be 0) completes that iteration. */
+int smd_advance(smd_system* h, int steps, int stop_at_measure);
+
+/* Barostat statistics of a replica. */
+int smd_mc_stats_get(smd_system* h, int replica, smd_mc_stats* out);
+
+/* Box-move history of a replica: for trials [start, start+max) the x/y
+ * fluctuation drawn (MD.cpp:595) and whether it was accepted.  Returns the
+ * number of entries written, or a negative value on error. */
+long smd_mc_log(smd_system* h, int replica, long start, long max, double* fluct, int* accepted);
+
+/* Changes the thermostat temperature (the tempStepInterval ramp,
+ * MD.cpp:369-371).  update_sigma = 0 keeps the noise amplitude, as the
+ * reference does for per-type gammas (langevin.h:235-246). replica -1 = all. */
+int smd_set_temperature(smd_system* h, int replica, double kT, int update_sigma);
+
+/* Langevin noise from the caller for the next force evaluation: psi[n*3] in
+ * [-1,1), bead order, used once instead of the counter-based generator.
+ * Lets a test drive the device step with the reference's MT19937 stream. */
+int smd_set_noise_once(smd_system* h, const double* psi);
+
+/* Device time (ms) of the fused step kernel over the last smd_advance call,
+ * and the number of kernel launches it issued. */
+int smd_last_timing(smd_system* h, double* step_kernel_ms, long* launches);
+
+/* Number of Verlet-list rebuilds so far. */
+long smd_rebuild_count(smd_system* h);
+
+/* Runs the synthetic generators (restating generate/liposome.cpp,
+ * generate/bilayer.cpp and generate/continuumSphereAndLiposome.cpp) and
+ * writes <path>. */
+int smd_synth_vesicle(const char* path, int seed, int n_lipids, double areal_density, double box);
+int smd_synth_bilayer(const char* path, int seed, int n_lipids, double areal_density, double zsize,
+                      double delta_lxy, double tension);
+int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double areal_density,
+                             double box, double sphere_radius, double head_umin, double gap);
+
+/* Reads <name>.mpd and runs it exactly as `MD <name>` would, writing the
+ * same .mpd / .xyz / .dat files (MD.cpp:72-755).  precision: smd_precision. */
+int smd_md_main(const char* name, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOFTMOLD_GB300_H */

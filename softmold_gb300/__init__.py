@@ -1,0 +1,378 @@
+"""softmold_gb300: GB300 implicit-solvent membrane MD step behind a C ABI.
+
+This module is a thin ctypes mirror of include/softmold_gb300.h for tests,
+benchmarks and scripting.  The compute path is the CUDA library
+``_build/libsoftmold_gb300.so``; there is no CPU fallback: every call that
+needs the device raises when the library or the GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "_build", "libsoftmold_gb300.so")
+MD_EXE = os.path.join(PKG, "_build", "MD")
+HEADER = os.path.join(ROOT, "include", "softmold_gb300.h")
+
+PLAIN_FP64 = 0
+MIXED = 1
+
+
+class SmdError(RuntimeError):
+    pass
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("n_types", C.c_int),
+        ("pos", C.POINTER(C.c_double)), ("vel", C.POINTER(C.c_double)), ("type", C.POINTER(C.c_int)),
+        ("box", C.c_double * 3), ("cutoff", C.c_double),
+        ("fconst", C.POINTER(C.c_double)), ("uconst", C.POINTER(C.c_double)),
+        ("n_chain_blocks", C.c_int), ("chain_blocks", C.POINTER(C.c_int)),
+        ("chain_consts", C.POINTER(C.c_double)),
+        ("n_spheres", C.c_int), ("sphere_index", C.POINTER(C.c_int)),
+        ("sphere_consts", C.POINTER(C.c_double)),
+        ("dt", C.c_double), ("gamma", C.c_double), ("temperature", C.c_double),
+        ("seed", C.c_uint32), ("tension", C.c_double), ("delta_lxy", C.c_double),
+        ("resize_rate", C.c_int), ("first_step", C.c_int), ("skin", C.c_double),
+    ]
+
+
+class Energy(C.Structure):
+    _fields_ = [("pair", C.c_double), ("bonded", C.c_double), ("sphere", C.c_double), ("kinetic", C.c_double)]
+
+
+class McStats(C.Structure):
+    _fields_ = [("trials", C.c_long), ("accepted", C.c_long), ("last_dU", C.c_double)]
+
+
+_lib = None
+
+# name -> (restype, argtypes); every function declared in the header
+_SIGS = {
+    "smd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "smd_device_count": (C.c_int, []),
+    "smd_create": (C.c_int, [C.POINTER(SystemDesc), C.c_int, C.POINTER(C.c_void_p)]),
+    "smd_create_batch": (C.c_int, [C.POINTER(SystemDesc), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "smd_destroy": (None, [C.c_void_p]),
+    "smd_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smd_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_get_box": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "smd_compute_forces": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smd_compute_pair_forces": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smd_compute_energy": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smd_compute_dU": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_cell_keys": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smd_pair_list": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "smd_prepare": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "smd_advance": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "smd_mc_stats_get": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "smd_mc_log": (C.c_long, [C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_void_p, C.c_void_p]),
+    "smd_set_temperature": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int]),
+    "smd_set_noise_once": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "smd_last_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_rebuild_count": (C.c_long, [C.c_void_p]),
+    "smd_synth_vesicle": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double]),
+    "smd_synth_bilayer": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                    C.c_double]),
+    "smd_synth_vesicle_sphere": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                           C.c_double, C.c_double]),
+    "smd_md_main": (C.c_int, [C.c_char_p, C.c_int]),
+}
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/softmold_gb300.h."""
+    import re
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|long|void)\s+\*?\s*(smd_\w+)\s*\(", text, re.M)))
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SmdError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(2048)
+    lib().smd_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise SmdError(f"{what} failed ({rc}): {last_error()}")
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+@dataclass
+class Mpd:
+    """The hot-path fields of an .mpd file."""
+    n_types: int
+    pos: np.ndarray          # (n,3)
+    vel: np.ndarray          # (n,3)
+    type: np.ndarray         # (n,)
+    box: np.ndarray          # (3,)
+    cutoff: float
+    fconst: np.ndarray
+    uconst: np.ndarray
+    chain_blocks: np.ndarray  # (k,3)
+    chain_consts: np.ndarray  # (k,4)
+    dt: float
+    gamma: float
+    temperature: float
+    seed: int
+    tension: float
+    delta_lxy: float
+    initial_time: float
+    final_time: float
+    sphere_index: np.ndarray | None = None
+    sphere_consts: np.ndarray | None = None
+
+
+def read_mpd(path: str) -> Mpd:
+    """Parses the hot-path fields of an .mpd token stream (Blob::input,
+    include/system.h:589-1314)."""
+    toks = open(path).read().split()
+    i = 0
+    vals = {}
+    n_types = n_particles = n_mol = 0
+    pos = vel = typ = None
+    blocks, consts = [], []
+    sph_idx, sph_c = None, None
+    fc = uc = None
+
+    def take(k=1):
+        nonlocal i
+        out = toks[i:i + k]
+        i += k
+        return out
+
+    layouts = {6: (2, 2), 7: (3, 2), 8: (3, 4), 9: (1, None), 10: (1, 1), 11: (1, 4), 12: (2, 5), 13: (1, 4),
+               14: (1, 4), 15: (1, None), 16: (3, 4), 17: (2, 2), 18: (1, None), 19: (2, 2)}
+    while i < len(toks):
+        kw = take()[0]
+        if kw == "end":
+            break
+        if kw in ("gamma", "initialTemp", "finalTemp", "cutoff", "initialTime", "finalTime", "deltaT",
+                  "storeInterval", "measureInterval", "deltaLXY", "removeSolvent", "tempStepInterval", "tension"):
+            vals[kw] = float(take()[0])
+        elif kw in ("seed", "nTypes", "nMolecules", "nParticles"):
+            vals[kw] = int(take()[0])
+            n_types = vals.get("nTypes", n_types)
+            n_particles = vals.get("nParticles", n_particles)
+            n_mol = vals.get("nMolecules", n_mol)
+        elif kw == "periodic":
+            take()
+        elif kw == "size":
+            vals["size"] = [float(x) for x in take(3)]
+        elif kw == "twoBodyFconst":
+            fc = np.array(take(6 * n_types * n_types), dtype=np.float64)
+        elif kw == "twoBodyUconst":
+            uc = np.array(take(6 * n_types * n_types), dtype=np.float64)
+        elif kw == "positions":
+            a = np.array(take(4 * n_particles), dtype=np.float64).reshape(-1, 4)
+            typ = a[:, 0].astype(np.int32)
+            pos = np.ascontiguousarray(a[:, 1:])
+        elif kw == "velocities":
+            vel = np.array(take(3 * n_particles), dtype=np.float64).reshape(-1, 3)
+        elif kw == "molecule":
+            for _ in range(n_mol):
+                mt = int(take()[0])
+                if mt not in layouts:
+                    take(4)
+                    continue
+                nb = int(take()[0])
+                nidx, ncon = layouts[mt]
+                if ncon is None:
+                    ncon = {9: 22 * n_types * n_types, 15: 6 * n_types, 18: 22 * nb}[mt]
+                c = np.array(take(ncon), dtype=np.float64)
+                b = np.array(take(nidx * nb), dtype=np.int64).reshape(nb, nidx)
+                if mt == 8:
+                    for row in b:
+                        blocks.append(row[:3])
+                        consts.append(c[:4])
+                elif mt == 9:
+                    sph_idx = b[:, 0].astype(np.int32)
+                    sph_c = c
+        elif kw == "banana":
+            pass
+        elif kw == "solventGamma":
+            take(2)
+        elif kw == "gammaType":
+            vals["gammaType"] = [float(x) for x in take(n_types)]
+        else:
+            raise SmdError(f"unknown keyword {kw}")
+    gamma = vals.get("gamma", 0.0)
+    if not gamma > 0 and "gammaType" in vals:
+        gamma = vals["gammaType"][0]
+    return Mpd(n_types=n_types, pos=pos, vel=vel, type=typ, box=np.array(vals["size"]), cutoff=vals["cutoff"],
+               fconst=fc, uconst=uc,
+               chain_blocks=np.array(blocks, dtype=np.int32).reshape(-1, 3),
+               chain_consts=np.array(consts, dtype=np.float64).reshape(-1, 4),
+               dt=vals["deltaT"], gamma=gamma, temperature=vals["initialTemp"], seed=vals["seed"],
+               tension=vals.get("tension", 0.0), delta_lxy=vals.get("deltaLXY", 0.0),
+               initial_time=vals.get("initialTime", 0.0), final_time=vals.get("finalTime", 0.0),
+               sphere_index=sph_idx, sphere_consts=sph_c)
+
+
+class System:
+    """One handle of the C ABI: one system or a batch of replicas."""
+
+    def __init__(self, systems: Mpd | list[Mpd], precision: int = MIXED, skin: float = 0.5):
+        systems = systems if isinstance(systems, list) else [systems]
+        self._keep = []
+        descs = (SystemDesc * len(systems))()
+        for k, m in enumerate(systems):
+            arrs = dict(pos=np.ascontiguousarray(m.pos, np.float64), vel=np.ascontiguousarray(m.vel, np.float64),
+                        type=np.ascontiguousarray(m.type, np.int32), fc=np.ascontiguousarray(m.fconst, np.float64),
+                        uc=np.ascontiguousarray(m.uconst, np.float64),
+                        cb=np.ascontiguousarray(m.chain_blocks, np.int32),
+                        cc=np.ascontiguousarray(m.chain_consts, np.float64))
+            self._keep.append(arrs)
+            d = descs[k]
+            d.n = len(m.type)
+            d.n_types = m.n_types
+            d.pos, d.vel, d.type = _dp(arrs["pos"]), _dp(arrs["vel"]), _ip(arrs["type"])
+            for a in range(3):
+                d.box[a] = float(m.box[a])
+            d.cutoff = m.cutoff
+            d.fconst, d.uconst = _dp(arrs["fc"]), _dp(arrs["uc"])
+            d.n_chain_blocks = len(arrs["cb"])
+            d.chain_blocks, d.chain_consts = _ip(arrs["cb"]), _dp(arrs["cc"])
+            d.n_spheres = 0
+            d.dt, d.gamma, d.temperature = m.dt, m.gamma, m.temperature
+            d.seed = m.seed & 0xffffffff
+            d.tension, d.delta_lxy = m.tension, m.delta_lxy
+            d.resize_rate = 8
+            d.first_step = int(m.initial_time / m.dt + 1e-7)
+            d.skin = skin
+        h = C.c_void_p()
+        _check(lib().smd_create_batch(descs, len(systems), precision, C.byref(h)), "smd_create_batch")
+        self.h = h
+        self.n = sum(len(m.type) for m in systems)
+        self.n_rep = len(systems)
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().smd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def state(self):
+        p = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        _check(lib().smd_get_state(self.h, p.ctypes.data, v.ctypes.data), "smd_get_state")
+        return p, v
+
+    def set_state(self, pos=None, vel=None):
+        pp = None if pos is None else np.ascontiguousarray(pos, np.float64)
+        vv = None if vel is None else np.ascontiguousarray(vel, np.float64)
+        _check(lib().smd_set_state(self.h, None if pp is None else pp.ctypes.data,
+                                   None if vv is None else vv.ctypes.data), "smd_set_state")
+
+    def box(self, replica=0):
+        b = np.zeros(3)
+        _check(lib().smd_get_box(self.h, replica, b.ctypes.data), "smd_get_box")
+        return b
+
+    def forces(self, pair_only=False):
+        f = np.zeros((self.n, 3))
+        fn = lib().smd_compute_pair_forces if pair_only else lib().smd_compute_forces
+        _check(fn(self.h, f.ctypes.data), "smd_compute_forces")
+        return f
+
+    def energy(self):
+        e = (Energy * self.n_rep)()
+        _check(lib().smd_compute_energy(self.h, e), "smd_compute_energy")
+        return [dict(pair=x.pair, bonded=x.bonded, sphere=x.sphere, kinetic=x.kinetic) for x in e]
+
+    def dU(self, scale):
+        s = np.ascontiguousarray(scale, np.float64)
+        out = np.zeros(self.n_rep)
+        _check(lib().smd_compute_dU(self.h, s.ctypes.data, out.ctypes.data), "smd_compute_dU")
+        return out
+
+    def cell_keys(self):
+        k = np.zeros(self.n, np.int32)
+        _check(lib().smd_cell_keys(self.h, k.ctypes.data), "smd_cell_keys")
+        return k
+
+    def pair_list(self):
+        cnt = C.c_size_t(0)
+        _check(lib().smd_pair_list(self.h, None, 0, C.byref(cnt)), "smd_pair_list")
+        out = np.zeros((max(cnt.value, 1), 2), np.int32)
+        _check(lib().smd_pair_list(self.h, out.ctypes.data, cnt.value, C.byref(cnt)), "smd_pair_list")
+        return out[:cnt.value]
+
+    def prepare(self, do_second=False, energy=False):
+        e = Energy()
+        _check(lib().smd_prepare(self.h, 1 if do_second else 0, C.byref(e) if energy else None), "smd_prepare")
+        return dict(pair=e.pair, bonded=e.bonded, sphere=e.sphere, kinetic=e.kinetic) if energy else None
+
+    def advance(self, steps, stop_at_measure=False):
+        _check(lib().smd_advance(self.h, int(steps), 1 if stop_at_measure else 0), "smd_advance")
+
+    def set_noise_once(self, psi):
+        p = np.ascontiguousarray(psi, np.float64)
+        _check(lib().smd_set_noise_once(self.h, p.ctypes.data), "smd_set_noise_once")
+
+    def set_stream(self, stream_handle: int | None):
+        _check(lib().smd_set_stream(self.h, C.c_void_p(stream_handle) if stream_handle else None),
+               "smd_set_stream")
+
+    def mc_stats(self, replica=0):
+        s = McStats()
+        _check(lib().smd_mc_stats_get(self.h, replica, C.byref(s)), "smd_mc_stats_get")
+        return dict(trials=s.trials, accepted=s.accepted, last_dU=s.last_dU)
+
+    def launches(self):
+        ms = C.c_double(0)
+        n = C.c_long(0)
+        _check(lib().smd_last_timing(self.h, C.byref(ms), C.byref(n)), "smd_last_timing")
+        return n.value
+
+    def rebuilds(self):
+        return lib().smd_rebuild_count(self.h)
+
+
+def synth_vesicle(path, seed, n_lipids, density=3.45, box=400.0):
+    _check(lib().smd_synth_vesicle(path.encode(), seed, n_lipids, density, box), "smd_synth_vesicle")
+
+
+def synth_bilayer(path, seed, n_lipids, density=3.45, zsize=40.0, delta_lxy=0.01, tension=0.0):
+    _check(lib().smd_synth_bilayer(path.encode(), seed, n_lipids, density, zsize, delta_lxy, tension),
+           "smd_synth_bilayer")
+
+
+def synth_vesicle_sphere(path, seed, n_lipids, density, box, radius=5.0, head_umin=-10.0, gap=2.0):
+    _check(lib().smd_synth_vesicle_sphere(path.encode(), seed, n_lipids, density, box, radius, head_umin, gap),
+           "smd_synth_vesicle_sphere")

@@ -1,0 +1,37 @@
+// Host-only C ABI entries: the synthetic input generators.
+#include <cmath>
+#include <string>
+
+#include "../../include/softmold_gb300.h"
+#include "mpd_io.h"
+#include "synth.h"
+
+extern "C" {
+
+int smd_synth_vesicle(const char* path, int seed, int n_lipids, double density, double box) {
+  if (!path || n_lipids <= 0 || !(density > 0) || !(box > 0)) return 1;
+  std::string err;
+  return smd::mpd_write_file(path, smd::synth_vesicle(seed, n_lipids, density, box), err);
+}
+
+int smd_synth_bilayer(const char* path, int seed, int n_lipids, double density, double zsize, double delta_lxy,
+                      double tension) {
+  if (!path || n_lipids <= 0 || !(density > 0) || !(zsize > 0)) return 1;
+  std::string err;
+  return smd::mpd_write_file(path, smd::synth_bilayer(seed, n_lipids, density, zsize, delta_lxy, tension), err);
+}
+
+int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double density, double box,
+                             double sphere_radius, double head_umin, double gap) {
+  if (!path || n_lipids <= 0 || !(density > 0) || !(box > 0) || !(sphere_radius > 1)) return 1;
+  smd::MpdSystem s = smd::synth_vesicle(seed, n_lipids, density, box);
+  // sphere centred on the +z axis, its surface `gap` outside the outer heads
+  // (outer head shell: radius + 5 bond lengths, models/lipidModels.h:1428-1431)
+  const double R = std::sqrt(((double)n_lipids / density) / (4.0 * M_PI));
+  const double c[3] = {box / 2.0, box / 2.0, box / 2.0 + R + 0.7 * 5 + gap + sphere_radius};
+  smd::add_continuum_sphere(s, c, sphere_radius, head_umin, 10.0, 4);
+  std::string err;
+  return smd::mpd_write_file(path, s, err);
+}
+
+}  // extern "C"

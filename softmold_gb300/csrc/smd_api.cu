@@ -1,0 +1,829 @@
+// Host orchestration and C ABI of the GB300 membrane MD step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/softmold_gb300.h"
+#include "mt19937.h"
+#include "smd_kernels.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define SMD_CUDA(call)                                                                       \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail(100 + (int)e_, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+  } while (0)
+
+constexpr int kTrialChunk = 1024;  // barostat trials staged per upload
+
+}  // namespace
+
+using namespace smd;
+
+struct smd_system {
+  bool mixed = true;
+  int n = 0, n_rep = 0, npad = 0, kmax = 0, n_cells = 0, n_tiles = 0;
+  int cur = 0;
+  long long it = 0;         // current loop step
+  bool at_measure = false;  // stopped after the second half-kick of step `it`
+  bool pending_trial = false;
+  int pending_trial_slot = 0;
+  bool ext_noise_pending = false;
+  double skin = 0.5, dt = 0, half_skin = 0;
+  bool barostat = false;
+  int resize_rate = 8;
+  std::vector<RepParams> rp;
+  std::vector<Mt19937> baro;  // one MTRand(seed) stream per replica (MD.cpp:149)
+  std::vector<int> first_step;
+  Tables tab{};
+  DevPtrs P{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<void*> allocs;
+  long launches = 0;
+  bool profile = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double step_ms = 0;
+  std::vector<double> trial_host;
+  int trials_staged = 0, trials_used = 0;
+  std::vector<std::vector<double>> mc_fluct;  // per replica, every trial so far
+  std::vector<std::vector<int>> mc_accept;
+  std::vector<int> log_host;
+
+  template <typename T>
+  int alloc(T** p, size_t count) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(100 + (int)e, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    e = cudaMemset(q, 0, bytes);
+    if (e != cudaSuccess) return fail(100 + (int)e, std::string("cudaMemset: ") + cudaGetErrorString(e));
+    allocs.push_back(q);
+    *p = (T*)q;
+    return 0;
+  }
+  ~smd_system() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* q : allocs) cudaFree(q);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+  }
+  int grid() const { return (n + kBlock - 1) / kBlock; }
+};
+
+namespace {
+
+int check_launch(smd_system* h) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(200 + (int)e, std::string("kernel launch: ") + cudaGetErrorString(e));
+  h->launches++;
+  return 0;
+}
+
+#define SMD_LAUNCH(h, ...)               \
+  do {                                   \
+    __VA_ARGS__;                         \
+    int rc_ = check_launch(h);           \
+    if (rc_) return rc_;                 \
+  } while (0)
+
+__global__ void k_set_rebuild(Global* g, int v) { g->rebuild = v; }
+
+// The list kernels run only when the device flag asks for a rebuild.  API
+// calls outside the loop clear the flag afterwards; in the loop the step's
+// last block recomputes it from the displacement bound.
+int rebuild_if_needed(smd_system* h, bool clear_after = false) {
+  auto& P = h->P;
+  const int g = h->grid();
+  SMD_LAUNCH(h, k_bin<<<g, kBlock, 0, h->stream>>>(P));
+  SMD_LAUNCH(h, k_scan_tiles<<<h->n_tiles, kBlock, 0, h->stream>>>(P));
+  SMD_LAUNCH(h, k_scan_sums<<<1, kBlock, 0, h->stream>>>(P, h->n_tiles));
+  SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, h->stream>>>(P));
+  if (h->mixed) {
+    SMD_LAUNCH(h, k_reorder<true><<<g, kBlock, 0, h->stream>>>(P, h->cur));
+    SMD_LAUNCH(h, k_nbr<true><<<g, kBlock, 0, h->stream>>>(P, h->cur));
+  } else {
+    SMD_LAUNCH(h, k_reorder<false><<<g, kBlock, 0, h->stream>>>(P, h->cur));
+    SMD_LAUNCH(h, k_nbr<false><<<g, kBlock, 0, h->stream>>>(P, h->cur));
+  }
+  if (clear_after) SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 0));
+  return 0;
+}
+
+int force_rebuild(smd_system* h) {
+  SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(h->P.g, 1));
+  return rebuild_if_needed(h, true);
+}
+
+template <int FL>
+int launch_step(smd_system* h) {
+  auto& P = h->P;
+  const int g = h->grid();
+  if (h->mixed)
+    SMD_LAUNCH(h, k_step<true, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, h->it));
+  else
+    SMD_LAUNCH(h, k_step<false, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, h->it));
+  return 0;
+}
+
+int launch_finish(smd_system* h, int do_second, int apply_mc) {
+  auto& P = h->P;
+  const int g = h->grid();
+  if (h->mixed)
+    SMD_LAUNCH(h, k_finish<true><<<g, kBlock, 0, h->stream>>>(P, h->cur, do_second, apply_mc));
+  else
+    SMD_LAUNCH(h, k_finish<false><<<g, kBlock, 0, h->stream>>>(P, h->cur, do_second, apply_mc));
+  h->cur ^= 1;
+  return 0;
+}
+
+bool is_trial_step(const smd_system* h, long long it) {
+  return h->barostat && (it % h->resize_rate) == 0 && it != 0;
+}
+
+// Counts the barostat trials among the next `steps` iterations, draws their
+// two uniforms per replica from the MT19937 streams, and stages them.
+// Appends the decisions of the trials run from the staged buffer to the host
+// log (called once the stream has drained).
+int flush_mc_log(smd_system* h) {
+  if (h->trials_used == 0) return 0;
+  const size_t n = (size_t)h->trials_used * h->n_rep;
+  h->log_host.resize(n);
+  SMD_CUDA(cudaMemcpyAsync(h->log_host.data(), h->P.accept_log, n * sizeof(int), cudaMemcpyDeviceToHost,
+                           h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  for (int t = 0; t < h->trials_used; ++t)
+    for (int r = 0; r < h->n_rep; ++r) {
+      if (h->rp[r].dlxy == 0) continue;
+      const double u1 = h->trial_host[((size_t)t * h->n_rep + r) * 2];
+      h->mc_fluct[r].push_back(h->rp[r].dlxy * (2.0 * u1 - 1.0));
+      h->mc_accept[r].push_back(h->log_host[(size_t)t * h->n_rep + r]);
+    }
+  h->trials_used = 0;
+  h->trials_staged = 0;
+  return 0;
+}
+
+int stage_trials(smd_system* h, long long from, int steps) {
+  int count = 0;
+  for (long long k = from; k < from + steps; ++k)
+    if (is_trial_step(h, k)) ++count;
+  if (count == 0) return 0;
+  if (count > kTrialChunk) return fail(3, "internal: too many barostat trials staged at once");
+  if (int rc = flush_mc_log(h)) return rc;
+  h->trial_host.assign((size_t)count * h->n_rep * 2, 0.0);
+  for (int t = 0; t < count; ++t)
+    for (int r = 0; r < h->n_rep; ++r) {
+      h->trial_host[((size_t)t * h->n_rep + r) * 2] = h->baro[r].rand53();
+      h->trial_host[((size_t)t * h->n_rep + r) * 2 + 1] = h->baro[r].rand53();
+    }
+  // pageable source: the copy is staged before cudaMemcpyAsync returns
+  SMD_CUDA(cudaMemcpyAsync(h->P.trial_u, h->trial_host.data(), h->trial_host.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, h->stream));
+  h->trials_staged = count;
+  h->trials_used = 0;
+  return 0;
+}
+
+int complete_pending(smd_system* h) {
+  if (!h->at_measure) return 0;
+  const int apply = h->pending_trial ? 1 : 0;
+  if (h->pending_trial) {
+    SMD_LAUNCH(h, k_mc<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P, h->pending_trial_slot));
+  }
+  int rc = launch_finish(h, 0, apply);
+  if (rc) return rc;
+  h->at_measure = false;
+  h->pending_trial = false;
+  h->it++;
+  return 0;
+}
+
+int read_error(smd_system* h) {
+  Global g;
+  SMD_CUDA(cudaMemcpyAsync(&g, h->P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (g.error & 1) {
+    char buf[256];
+    std::snprintf(buf, sizeof buf,
+                  "Verlet list overflow: a bead has %d neighbours within rc+skin, capacity %d "
+                  "(system density grew far beyond the start configuration)",
+                  g.need_nbr, h->kmax);
+    return fail(7, buf);
+  }
+  return 0;
+}
+
+int validate(const smd_system_desc& d, std::string& why) {
+  if (d.n <= 0) return why = "n must be positive", 1;
+  if (d.n_types <= 0 || d.n_types > kMaxTypes) return why = "n_types must be in 1..8", 1;
+  if (!d.pos || !d.vel || !d.type || !d.fconst || !d.uconst) return why = "null array in descriptor", 1;
+  if (!(d.cutoff > 0)) return why = "cutoff must be positive", 1;
+  for (int k = 0; k < 3; ++k) {
+    if (!(d.box[k] > 0)) return why = "box must be positive", 1;
+    if (int(d.box[k] / d.cutoff) < 3)
+      return why = "box edge shorter than 3 cutoffs: the reference cell traversal double-counts there", 1;
+  }
+  for (int i = 0; i < d.n; ++i) {
+    if (d.type[i] < 0 || d.type[i] >= d.n_types) return why = "bead type out of range", 1;
+    for (int k = 0; k < 3; ++k) {
+      const double x = d.pos[3 * i + k];
+      if (!(x >= 0 && x <= d.box[k])) return why = "position out of the box", 1;
+    }
+  }
+  for (int b = 0; b < d.n_chain_blocks; ++b) {
+    const int s = d.chain_blocks[3 * b], c = d.chain_blocks[3 * b + 1], l = d.chain_blocks[3 * b + 2];
+    if (l < 3 || l > 4095) return why = "CHAIN length must be in 3..4095", 1;
+    if (s < 0 || (long long)s + (long long)c * l > d.n) return why = "CHAIN block out of range", 1;
+  }
+  if (d.n_spheres > 0) return why = "BEAD residues are not supported by this build of the device step", 1;
+  if (!(d.dt > 0)) return why = "dt must be positive", 1;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int smd_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    std::strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)g_last_error.size();
+}
+
+int smd_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+int smd_create(const smd_system_desc* desc, int precision, smd_system** out) {
+  return smd_create_batch(desc, 1, precision, out);
+}
+
+int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd_system** out) {
+  if (!descs || n_rep <= 0 || !out) return fail(1, "smd_create_batch: bad arguments");
+  if (precision != SMD_PLAIN_FP64 && precision != SMD_MIXED) return fail(1, "unknown precision");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(2, "no CUDA device: the GB300 step has no CPU fallback");
+  std::string why;
+  for (int r = 0; r < n_rep; ++r)
+    if (validate(descs[r], why)) return fail(1, "replica " + std::to_string(r) + ": " + why);
+  const smd_system_desc& d0 = descs[0];
+  for (int r = 1; r < n_rep; ++r) {
+    const smd_system_desc& d = descs[r];
+    if (d.n_types != d0.n_types || d.cutoff != d0.cutoff || d.dt != d0.dt)
+      return fail(1, "replicas of a batch must share n_types, cutoff and dt");
+    for (int k = 0; k < 6 * d0.n_types * d0.n_types; ++k)
+      if (d.fconst[k] != d0.fconst[k] || d.uconst[k] != d0.uconst[k])
+        return fail(1, "replicas of a batch must share the pair tables");
+  }
+  std::unique_ptr<smd_system> h(new smd_system());
+  h->mixed = (precision == SMD_MIXED);
+  h->n_rep = n_rep;
+  h->dt = d0.dt;
+  h->skin = d0.skin > 0 ? d0.skin : 0.5;
+  h->half_skin = 0.5 * h->skin;
+  h->resize_rate = d0.resize_rate > 0 ? d0.resize_rate : 8;
+  int total = 0;
+  for (int r = 0; r < n_rep; ++r) total += descs[r].n;
+  h->n = total;
+  h->npad = (total + 31) / 32 * 32;
+  // ---- tables
+  Tables& T = h->tab;
+  T.nT = d0.n_types;
+  T.rc = d0.cutoff;
+  T.rc2 = d0.cutoff * d0.cutoff;
+  T.rcf = (float)d0.cutoff;
+  T.rc2f = (float)(d0.cutoff * d0.cutoff);
+  T.list_cut = d0.cutoff + h->skin;
+  T.list_cut2 = T.list_cut * T.list_cut;
+  double maxF = 1.0;
+  for (int k = 0; k < d0.n_types * d0.n_types; ++k) {
+    const double* c = d0.fconst + 6 * k;
+    T.dF[6 * k + 0] = c[0];
+    for (int q = 0; q < 6; ++q) {
+      T.dF[6 * k + q] = c[q];
+      T.fF[6 * k + q] = (float)c[q];
+      T.dU[6 * k + q] = d0.uconst[6 * k + q];
+      T.fU[6 * k + q] = (float)d0.uconst[6 * k + q];
+    }
+    // |F| = |mag| r: inner segment at most C1*rm, outer sampled on [rm, rc]
+    maxF = std::max(maxF, std::fabs(c[1] * c[0]));
+    for (int s = 0; s <= 64; ++s) {
+      const double r = c[0] + (d0.cutoff - c[0]) * s / 64.0;
+      const double m = c[3] - r;
+      maxF = std::max(maxF, std::fabs((c[4] - c[5] * m) * m) * 1.05);
+    }
+  }
+  // one pair force must fit in int32 after scaling
+  T.fscale = (float)std::ldexp(1.0, (int)std::floor(std::log2(1073741824.0 / maxF)));
+  T.inv_fscale = 1.0 / (double)T.fscale;
+  // chain constant sets
+  std::vector<std::array<double, 4>> sets;
+  std::vector<int> cinfo(total, 0);
+  std::vector<int> type(total, 0);
+  h->rp.resize(n_rep);
+  h->first_step.resize(n_rep);
+  int bead = 0, cells = 0;
+  for (int r = 0; r < n_rep; ++r) {
+    const smd_system_desc& d = descs[r];
+    RepParams& p = h->rp[r];
+    p.dt = d.dt;
+    p.gamma = d.gamma;
+    p.kT = d.temperature;
+    p.sigma = std::sqrt((6.0 * d.temperature * d.gamma) / d.dt);
+    p.tension = d.tension;
+    p.dlxy = d.delta_lxy;
+    p.seed = d.seed;
+    p.resize_rate = h->resize_rate;
+    p.bead_begin = bead;
+    p.bead_end = bead + d.n;
+    if (d.delta_lxy != 0) h->barostat = true;
+    int cap = 1;
+    for (int k = 0; k < 3; ++k) cap *= (int)(1.3 * d.box[k] / T.list_cut) + 2;
+    p.cell_begin = cells;
+    p.cell_cap = cap;
+    cells += cap;
+    h->baro.emplace_back((uint32_t)d.seed);
+    h->first_step[r] = d.first_step;
+    for (int i = 0; i < d.n; ++i) type[bead + i] = d.type[i];
+    for (int b = 0; b < d.n_chain_blocks; ++b) {
+      std::array<double, 4> c = {d.chain_consts[4 * b], d.chain_consts[4 * b + 1], d.chain_consts[4 * b + 2],
+                                 d.chain_consts[4 * b + 3]};
+      int set = -1;
+      for (size_t q = 0; q < sets.size(); ++q)
+        if (sets[q] == c) set = (int)q;
+      if (set < 0) {
+        if ((int)sets.size() >= kMaxChainSets) return fail(1, "too many distinct CHAIN constant sets");
+        sets.push_back(c);
+        set = (int)sets.size() - 1;
+      }
+      const int s = d.chain_blocks[3 * b], nc = d.chain_blocks[3 * b + 1], l = d.chain_blocks[3 * b + 2];
+      for (int c2 = 0; c2 < nc; ++c2)
+        for (int q = 0; q < l; ++q) cinfo[bead + s + c2 * l + q] = cinfo_pack(q, l, set);
+    }
+    bead += d.n;
+  }
+  for (int r = 1; r < n_rep; ++r)
+    if (h->first_step[r] != h->first_step[0]) return fail(1, "replicas of a batch must start at the same step");
+  h->it = h->first_step[0];
+  T.n_sets = (int)sets.size();
+  for (size_t q = 0; q < sets.size(); ++q)
+    for (int k = 0; k < 4; ++k) {
+      T.chainD[q][k] = sets[q][k];
+      T.chainF[q][k] = (float)sets[q][k];
+    }
+  h->n_cells = cells;
+  h->n_tiles = (cells + kScanTile - 1) / kScanTile;
+  // ---- device memory
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(2, "cudaStreamCreate failed");
+  h->own_stream = true;
+  DevPtrs& P = h->P;
+  P.n = total;
+  P.npad = h->npad;
+  P.n_rep = n_rep;
+  P.n_cells_total = cells;
+  P.half_skin = h->half_skin;
+  int rc = 0;
+  double** dbl[] = {&P.x, &P.y, &P.z, &P.vx, &P.vy, &P.vz, &P.ax, &P.ay, &P.az,
+                    &P.tx, &P.ty, &P.tz, &P.tvx, &P.tvy, &P.tvz, &P.tax, &P.tay, &P.taz};
+  for (double** q : dbl)
+    if ((rc = h->alloc(q, total))) return rc;
+  if (h->mixed) {
+    if ((rc = h->alloc(&P.m4[0], total)) || (rc = h->alloc(&P.m4[1], total)) || (rc = h->alloc(&P.mt, total)))
+      return rc;
+  } else {
+    if ((rc = h->alloc(&P.d4[0], total)) || (rc = h->alloc(&P.d4[1], total)) || (rc = h->alloc(&P.dt4, total)))
+      return rc;
+  }
+  int** ints[] = {&P.orig, &P.inv, &P.cinfo, &P.torig, &P.tcinfo, &P.key, &P.slot, &P.nnbr, &P.key_out};
+  for (int** q : ints)
+    if ((rc = h->alloc(q, total))) return rc;
+  if ((rc = h->alloc(&P.cell_count, cells)) || (rc = h->alloc(&P.cell_start, cells + 1)) ||
+      (rc = h->alloc(&P.block_sums, h->n_tiles)))
+    return rc;
+  if ((rc = h->alloc(&P.rp, n_rep)) || (rc = h->alloc(&P.rs, n_rep)) || (rc = h->alloc(&P.g, 1))) return rc;
+  Tables* tdev = nullptr;
+  if ((rc = h->alloc(&tdev, 1))) return rc;
+  P.tab = tdev;
+  if ((rc = h->alloc(&P.accept_log, (size_t)kTrialChunk * n_rep))) return rc;
+  h->mc_fluct.resize(n_rep);
+  h->mc_accept.resize(n_rep);
+  if ((rc = h->alloc(&P.trial_u, (size_t)kTrialChunk * n_rep * 2)) || (rc = h->alloc(&P.ext_noise, 3 * total)) ||
+      (rc = h->alloc(&P.force_out, 3 * total)))
+    return rc;
+  // ---- upload state (sorted order = file order until the first build)
+  {
+    std::vector<double> hx(total), hy(total), hz(total), hvx(total), hvy(total), hvz(total);
+    std::vector<int> orig(total);
+    std::vector<uint4> m4(h->mixed ? total : 0);
+    std::vector<double4> d4(h->mixed ? 0 : total);
+    std::vector<RepState> rs(n_rep);
+    int b = 0;
+    for (int r = 0; r < n_rep; ++r) {
+      const smd_system_desc& d = descs[r];
+      std::memset(&rs[r], 0, sizeof(RepState));
+      for (int k = 0; k < 3; ++k) {
+        rs[r].box[k] = d.box[k];
+        rs[r].scale[k] = 1.0;
+      }
+      for (int i = 0; i < d.n; ++i, ++b) {
+        hx[b] = d.pos[3 * i];
+        hy[b] = d.pos[3 * i + 1];
+        hz[b] = d.pos[3 * i + 2];
+        hvx[b] = d.vel[3 * i];
+        hvy[b] = d.vel[3 * i + 1];
+        hvz[b] = d.vel[3 * i + 2];
+        orig[b] = b;
+        const unsigned w = (unsigned)type[b] | ((unsigned)r << 8);
+        if (h->mixed) {
+          auto fr = [](double x, double L) { return (unsigned int)(long long)(x * (1.0 / L) * 4294967296.0); };
+          m4[b] = make_uint4(fr(hx[b], d.box[0]), fr(hy[b], d.box[1]), fr(hz[b], d.box[2]), w);
+        } else {
+          long long wb = (long long)w;
+          double wd;
+          std::memcpy(&wd, &wb, sizeof wd);
+          d4[b] = make_double4(hx[b], hy[b], hz[b], wd);
+        }
+      }
+    }
+    SMD_CUDA(cudaMemcpy(P.x, hx.data(), total * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.y, hy.data(), total * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.z, hz.data(), total * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.vx, hvx.data(), total * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.vy, hvy.data(), total * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.vz, hvz.data(), total * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.orig, orig.data(), total * sizeof(int), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.inv, orig.data(), total * sizeof(int), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.cinfo, cinfo.data(), total * sizeof(int), cudaMemcpyHostToDevice));
+    if (h->mixed)
+      SMD_CUDA(cudaMemcpy(P.m4[0], m4.data(), total * sizeof(uint4), cudaMemcpyHostToDevice));
+    else
+      SMD_CUDA(cudaMemcpy(P.d4[0], d4.data(), total * sizeof(double4), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.rp, h->rp.data(), n_rep * sizeof(RepParams), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.rs, rs.data(), n_rep * sizeof(RepState), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(tdev, &T, sizeof(Tables), cudaMemcpyHostToDevice));
+  }
+  // ---- size the Verlet list: count pass with zero capacity, then the build
+  P.kmax = 0;
+  if ((rc = force_rebuild(h.get()))) return rc;
+  Global g;
+  SMD_CUDA(cudaMemcpyAsync(&g, P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  const int need = std::max(g.need_nbr, 1);
+  h->kmax = ((int)(need * 1.5) + 32 + 7) / 8 * 8;
+  P.kmax = h->kmax;
+  if ((rc = h->alloc(&P.nbr, (size_t)h->kmax * h->npad))) return rc;
+  g.error = 0;
+  g.need_nbr = 0;
+  g.rebuild = 1;
+  g.n_rebuilds = 0;
+  SMD_CUDA(cudaMemcpy(P.g, &g, sizeof(Global), cudaMemcpyHostToDevice));
+  if ((rc = rebuild_if_needed(h.get()))) return rc;
+  if ((rc = read_error(h.get()))) return rc;
+  SMD_CUDA(cudaEventCreate(&h->ev0));
+  SMD_CUDA(cudaEventCreate(&h->ev1));
+  *out = h.release();
+  return 0;
+}
+
+void smd_destroy(smd_system* h) { delete h; }
+
+int smd_set_stream(smd_system* h, void* s) {
+  if (!h) return fail(1, "null handle");
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  h->own_stream = (s == nullptr);
+  if (s == nullptr) {
+    SMD_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  } else {
+    h->stream = (cudaStream_t)s;
+  }
+  return 0;
+}
+
+int smd_get_state(smd_system* h, double* pos, double* vel) {
+  if (!h) return fail(1, "null handle");
+  const int n = h->n;
+  std::vector<double> a(n), b(n), c(n), va(n), vb(n), vc(n);
+  std::vector<int> orig(n);
+  auto& P = h->P;
+  SMD_CUDA(cudaMemcpyAsync(a.data(), P.x, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaMemcpyAsync(b.data(), P.y, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaMemcpyAsync(c.data(), P.z, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaMemcpyAsync(va.data(), P.vx, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaMemcpyAsync(vb.data(), P.vy, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaMemcpyAsync(vc.data(), P.vz, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaMemcpyAsync(orig.data(), P.orig, n * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < n; ++i) {
+    const int o = orig[i];
+    if (pos) {
+      pos[3 * o] = a[i];
+      pos[3 * o + 1] = b[i];
+      pos[3 * o + 2] = c[i];
+    }
+    if (vel) {
+      vel[3 * o] = va[i];
+      vel[3 * o + 1] = vb[i];
+      vel[3 * o + 2] = vc[i];
+    }
+  }
+  return 0;
+}
+
+int smd_set_state(smd_system* h, const double* pos, const double* vel) {
+  if (!h) return fail(1, "null handle");
+  const int n = h->n;
+  auto& P = h->P;
+  std::vector<int> orig(n);
+  SMD_CUDA(cudaMemcpyAsync(orig.data(), P.orig, n * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  std::vector<double> a(n), b(n), c(n), va(n), vb(n), vc(n);
+  for (int i = 0; i < n; ++i) {
+    const int o = orig[i];
+    if (pos) {
+      a[i] = pos[3 * o];
+      b[i] = pos[3 * o + 1];
+      c[i] = pos[3 * o + 2];
+    }
+    if (vel) {
+      va[i] = vel[3 * o];
+      vb[i] = vel[3 * o + 1];
+      vc[i] = vel[3 * o + 2];
+    }
+  }
+  if (pos) {
+    SMD_CUDA(cudaMemcpy(P.x, a.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.y, b.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.z, c.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    if (h->mixed)
+      SMD_LAUNCH(h, k_mirror<true><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur));
+    else
+      SMD_LAUNCH(h, k_mirror<false><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur));
+    SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 1));
+  }
+  if (vel) {
+    SMD_CUDA(cudaMemcpy(P.vx, va.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.vy, vb.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(P.vz, vc.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int smd_get_box(smd_system* h, int replica, double box[3]) {
+  if (!h || replica < 0 || replica >= h->n_rep) return fail(1, "bad replica");
+  RepState rs;
+  SMD_CUDA(cudaMemcpyAsync(&rs, h->P.rs + replica, sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < 3; ++k) box[k] = rs.box[k];
+  return 0;
+}
+
+static int compute_forces_impl(smd_system* h, double* out, bool pair_only) {
+  if (!h || !out) return fail(1, "bad arguments");
+  int rc = rebuild_if_needed(h, true);
+  if (rc) return rc;
+  rc = pair_only ? launch_step<F_FORCES | F_PAIRONLY>(h) : launch_step<F_FORCES>(h);
+  if (rc) return rc;
+  SMD_CUDA(cudaMemcpyAsync(out, h->P.force_out, 3 * h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  return read_error(h);
+}
+
+int smd_compute_forces(smd_system* h, double* out) { return compute_forces_impl(h, out, false); }
+int smd_compute_pair_forces(smd_system* h, double* out) { return compute_forces_impl(h, out, true); }
+
+int smd_compute_energy(smd_system* h, smd_energy* e) {
+  if (!h || !e) return fail(1, "bad arguments");
+  int rc = rebuild_if_needed(h, true);
+  if (rc) return rc;
+  std::vector<RepState> rs(h->n_rep);
+  SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  for (auto& s : rs) s.e_pair = s.e_bond = s.e_kin = 0;
+  SMD_CUDA(cudaMemcpyAsync(h->P.rs, rs.data(), h->n_rep * sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
+  if ((rc = launch_step<F_ENERGY>(h))) return rc;
+  SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  for (int r = 0; r < h->n_rep; ++r) {
+    e[r].pair = rs[r].e_pair;
+    e[r].bonded = rs[r].e_bond;
+    e[r].sphere = 0;
+    e[r].kinetic = rs[r].e_kin;
+  }
+  return read_error(h);
+}
+
+int smd_compute_dU(smd_system* h, const double scale[3], double* dU) {
+  if (!h || !scale || !dU) return fail(1, "bad arguments");
+  int rc = rebuild_if_needed(h, true);
+  if (rc) return rc;
+  std::vector<RepState> rs(h->n_rep);
+  SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  std::vector<RepState> saved = rs;
+  for (auto& s : rs) {
+    s.dU_pair = s.dU_bond = 0;
+    for (int k = 0; k < 3; ++k) s.scale[k] = scale[k];
+  }
+  SMD_CUDA(cudaMemcpyAsync(h->P.rs, rs.data(), h->n_rep * sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
+  if ((rc = launch_step<F_DU | F_ENERGY>(h))) return rc;
+  SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  for (int r = 0; r < h->n_rep; ++r) dU[r] = rs[r].dU_pair + rs[r].dU_bond;
+  SMD_CUDA(cudaMemcpyAsync(h->P.rs, saved.data(), h->n_rep * sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  return read_error(h);
+}
+
+int smd_cell_keys(smd_system* h, int* keys) {
+  if (!h || !keys) return fail(1, "bad arguments");
+  SMD_LAUNCH(h, k_ref_keys<<<h->grid(), kBlock, 0, h->stream>>>(h->P));
+  SMD_CUDA(cudaMemcpyAsync(keys, h->P.key_out, h->n * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int smd_pair_list(smd_system* h, int* pairs, size_t cap, size_t* count) {
+  if (!h || !count) return fail(1, "bad arguments");
+  int rc = rebuild_if_needed(h, true);
+  if (rc) return rc;
+  int* dpairs = nullptr;
+  unsigned long long* dcount = nullptr;
+  SMD_CUDA(cudaMallocAsync((void**)&dpairs, std::max<size_t>(cap, 1) * 2 * sizeof(int), h->stream));
+  SMD_CUDA(cudaMallocAsync((void**)&dcount, sizeof(unsigned long long), h->stream));
+  SMD_CUDA(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), h->stream));
+  SMD_LAUNCH(h, k_pairs<<<h->grid(), kBlock, 0, h->stream>>>(h->P, dpairs, (long long)cap, dcount));
+  unsigned long long c = 0;
+  SMD_CUDA(cudaMemcpyAsync(&c, dcount, sizeof c, cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (pairs && cap)
+    SMD_CUDA(cudaMemcpy(pairs, dpairs, std::min<size_t>(cap, c) * 2 * sizeof(int), cudaMemcpyDeviceToHost));
+  SMD_CUDA(cudaFreeAsync(dpairs, h->stream));
+  SMD_CUDA(cudaFreeAsync(dcount, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  *count = (size_t)c;
+  return 0;
+}
+
+int smd_set_noise_once(smd_system* h, const double* psi) {
+  if (!h || !psi) return fail(1, "bad arguments");
+  SMD_CUDA(cudaMemcpy(h->P.ext_noise, psi, 3 * h->n * sizeof(double), cudaMemcpyHostToDevice));
+  h->ext_noise_pending = true;
+  return 0;
+}
+
+int smd_prepare(smd_system* h, int do_second, smd_energy* energy_out) {
+  if (!h) return fail(1, "null handle");
+  int rc = force_rebuild(h);
+  if (rc) return rc;
+  if (h->ext_noise_pending) {
+    rc = launch_step<F_INIT | F_EXTNOISE>(h);
+    h->ext_noise_pending = false;
+  } else {
+    rc = launch_step<F_INIT>(h);
+  }
+  if (rc) return rc;
+  if (energy_out && (rc = smd_compute_energy(h, energy_out))) return rc;
+  if ((rc = launch_finish(h, do_second ? 1 : 0, 0))) return rc;
+  h->at_measure = false;
+  h->it = h->first_step[0];
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  return read_error(h);
+}
+
+int smd_advance(smd_system* h, int steps, int stop_at_measure) {
+  if (!h || steps < 0) return fail(1, "bad arguments");
+  int rc = complete_pending(h);
+  if (rc) return rc;
+  if (h->profile) {
+    SMD_CUDA(cudaEventRecord(h->ev0, h->stream));
+  }
+  int done = 0;
+  while (done < steps) {
+    const int chunk = std::min(steps - done, kTrialChunk * std::max(1, h->resize_rate) / 2);
+    if ((rc = stage_trials(h, h->it, chunk))) return rc;
+    for (int s = 0; s < chunk; ++s) {
+      if ((rc = rebuild_if_needed(h))) return rc;
+      const bool trial = is_trial_step(h, h->it);
+      const bool stop = stop_at_measure && (done + s == steps - 1);
+      const bool ext = h->ext_noise_pending;
+      h->ext_noise_pending = false;
+      if (!trial && !stop) {
+        rc = ext ? launch_step<F_EXTNOISE>(h) : launch_step<0>(h);
+        if (rc) return rc;
+        h->cur ^= 1;
+        h->it++;
+        continue;
+      }
+      int slot = 0;
+      if (trial) {
+        slot = h->trials_used++;
+        SMD_LAUNCH(h, k_trial<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P, slot));
+        rc = ext ? launch_step<F_STOP | F_DU | F_EXTNOISE>(h) : launch_step<F_STOP | F_DU>(h);
+      } else {
+        rc = ext ? launch_step<F_STOP | F_EXTNOISE>(h) : launch_step<F_STOP>(h);
+      }
+      if (rc) return rc;
+      h->at_measure = true;
+      h->pending_trial = trial;
+      h->pending_trial_slot = slot;
+      if (stop) break;
+      if ((rc = complete_pending(h))) return rc;
+    }
+    done += chunk;
+  }
+  if (h->profile) {
+    SMD_CUDA(cudaEventRecord(h->ev1, h->stream));
+    SMD_CUDA(cudaEventSynchronize(h->ev1));
+    float ms = 0;
+    SMD_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->step_ms = ms;
+  }
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (!h->at_measure || !h->pending_trial) {
+    if (int e = flush_mc_log(h)) return e;
+  }
+  return read_error(h);
+}
+
+int smd_mc_stats_get(smd_system* h, int replica, smd_mc_stats* out) {
+  if (!h || !out || replica < 0 || replica >= h->n_rep) return fail(1, "bad arguments");
+  RepState rs;
+  SMD_CUDA(cudaMemcpyAsync(&rs, h->P.rs + replica, sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  out->trials = (long)rs.n_trial;
+  out->accepted = (long)rs.n_accept;
+  out->last_dU = rs.last_dU;
+  return 0;
+}
+
+long smd_mc_log(smd_system* h, int replica, long start, long max, double* fluct, int* accepted) {
+  if (!h || replica < 0 || replica >= h->n_rep || start < 0 || max < 0) return -fail(1, "bad arguments");
+  if (!h->at_measure || !h->pending_trial) {
+    if (flush_mc_log(h)) return -1;
+  }
+  const auto& f = h->mc_fluct[replica];
+  const auto& a = h->mc_accept[replica];
+  long n = 0;
+  for (long k = start; k < (long)f.size() && n < max; ++k, ++n) {
+    if (fluct) fluct[n] = f[k];
+    if (accepted) accepted[n] = a[k];
+  }
+  return n;
+}
+
+int smd_set_temperature(smd_system* h, int replica, double kT, int update_sigma) {
+  if (!h || replica < -1 || replica >= h->n_rep) return fail(1, "bad arguments");
+  for (int r = 0; r < h->n_rep; ++r) {
+    if (replica >= 0 && r != replica) continue;
+    h->rp[r].kT = kT;
+    if (update_sigma) h->rp[r].sigma = std::sqrt((6.0 * kT * h->rp[r].gamma) / h->rp[r].dt);
+  }
+  SMD_CUDA(cudaMemcpyAsync(h->P.rp, h->rp.data(), h->n_rep * sizeof(RepParams), cudaMemcpyHostToDevice,
+                           h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int smd_last_timing(smd_system* h, double* ms, long* launches) {
+  if (!h) return fail(1, "null handle");
+  if (ms) *ms = h->step_ms;
+  if (launches) *launches = h->launches;
+  return 0;
+}
+
+long smd_rebuild_count(smd_system* h) {
+  if (!h) return -1;
+  Global g;
+  if (cudaMemcpyAsync(&g, h->P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return -1;
+  return (long)g.n_rebuilds;
+}
+
+}  // extern "C"

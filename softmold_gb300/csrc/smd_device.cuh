@@ -1,0 +1,250 @@
+// Device data layout and kernels of the GB300 membrane MD step.
+//
+// Per-bead state lives in HBM in cell-sorted order (beads of one replica are
+// contiguous; within a replica they are ordered by Verlet-list cell), FP64 SoA:
+//   x,y,z  vx,vy,vz  ax,ay,az        master state (8 B each)
+//   mirror[2]                        double-buffered 16 B position mirror read
+//                                    by the pair loop: MIXED = uint4 of 32-bit
+//                                    fractional coordinates + (type | replica<<8),
+//                                    PLAIN = double4 (x,y,z,type bits)
+//   orig / inv                       sorted -> file order and back
+//   cinfo                            CHAIN role of the bead (position, length, set)
+// The Verlet list is column-major: nbr[k * npad + i] is neighbour k of bead i.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+namespace smd {
+
+constexpr int kMaxTypes = 8;
+constexpr int kMaxChainSets = 32;
+constexpr int kBlock = 256;
+constexpr int kScanTile = 2048;  // cells per scan block (256 threads x 8)
+
+// cinfo word: bit 31 chain member, bits 0..11 position in chain, bits 12..23
+// chain length, bits 24..28 chain-constant set; bit 30 marks a BEAD sphere.
+__host__ __device__ inline int cinfo_pack(int p, int len, int set) {
+  return (int)(0x80000000u | (unsigned)(p & 0xfff) | ((unsigned)(len & 0xfff) << 12) |
+               ((unsigned)(set & 0x1f) << 24));
+}
+
+struct RepParams {  // per replica, fixed
+  double dt, gamma, kT, sigma, tension, dlxy;
+  uint32_t seed;
+  int resize_rate;
+  int bead_begin, bead_end;
+  int cell_begin, cell_cap;
+};
+
+struct RepState {  // per replica, updated on the device
+  double box[3];
+  double trial_box[3];
+  double scale[3];   // scale of the last accepted / current trial
+  double dU_pair, dU_bond;
+  double e_pair, e_bond, e_kin;
+  double last_dU;
+  long long n_trial, n_accept;
+  int accept;
+  int ncell[3];
+  int pad;
+};
+
+struct Global {  // single instance
+  double disp;                 // displacement bound since the last list build
+  unsigned long long mc_shift; // largest bead shift of accepted box moves (double bits)
+  long long n_rebuilds;
+  unsigned int vmax_bits;      // max |v| of the current step (float bits)
+  unsigned int blocks_done;    // last-block counter
+  int rebuild;                 // 1: rebuild the Verlet list before the next force pass
+  int error;                   // bit 0: list overflow, bit 1: cell overflow (>kMaxCell)
+  int need_nbr;                // largest neighbour count seen on overflow
+  int pad;
+};
+
+struct Tables {  // force/potential tables (float and double) in constant-like memory
+  int nT;
+  int n_sets;
+  float rc2f, rcf;
+  double rc2, rc;
+  double list_cut2;  // (rc+skin)^2
+  double list_cut;
+  float fscale;      // fixed-point scale of one pair force (2^k)
+  double inv_fscale;
+  float fF[6 * kMaxTypes * kMaxTypes];
+  float fU[6 * kMaxTypes * kMaxTypes];
+  double dF[6 * kMaxTypes * kMaxTypes];
+  double dU[6 * kMaxTypes * kMaxTypes];
+  float chainF[kMaxChainSets][4];
+  double chainD[kMaxChainSets][4];
+};
+
+// All device pointers of one handle.
+struct DevPtrs {
+  int n, npad, n_rep, kmax, n_cells_total;
+  double half_skin;
+  double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az;
+  uint4* m4[2];
+  double4* d4[2];
+  int *orig, *inv, *cinfo;
+  // rebuild scratch
+  uint4* mt;
+  double4* dt4;
+  double *tx, *ty, *tz, *tvx, *tvy, *tvz, *tax, *tay, *taz;
+  int *torig, *tcinfo;
+  int *key, *slot;
+  int *cell_count, *cell_start, *block_sums;
+  int *nbr, *nnbr;
+  RepParams* rp;
+  RepState* rs;
+  Global* g;
+  const Tables* tab;
+  double* trial_u;   // 2 draws per barostat trial, per replica: [trial][rep][2]
+  int* accept_log;   // decision of each staged trial: [trial][rep]
+  double* ext_noise; // n*3 noise in sorted order (test hook)
+  double* force_out; // n*3 scratch for host reads (file order)
+  int* key_out;
+};
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ int rep_of(const DevPtrs& P, int i) {
+  // replicas are contiguous ranges; linear scan is fine for the few replicas
+  // of a batch, binary search for many.
+  int lo = 0, hi = P.n_rep - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (P.rp[mid].bead_begin <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// CellOpt cell coordinate: int(p/cellSize) with the x>=n -> n-1 correction
+// (include/algorithms/cellOpt.h:532-539).  IEEE FP64 division, no fast-math.
+__device__ __forceinline__ int cell_coord(double p, double cs, int n) {
+  int c = int(p / cs);
+  c = (c >= n) ? c - 1 : c;
+  return c;
+}
+
+__device__ __forceinline__ unsigned int to_frac(double x, double invL) {
+  // 32-bit fractional coordinate; x == L wraps to 0 like any periodic image.
+  return (unsigned int)(long long)(x * invL * 4294967296.0);
+}
+
+__device__ __forceinline__ float frac_delta(unsigned int a, unsigned int b, float scale) {
+  return (float)(int)(a - b) * scale;  // two's-complement wrap = minimum image
+}
+
+__device__ __forceinline__ double frac_delta_d(unsigned int a, unsigned int b, double scale) {
+  return (double)(int)(a - b) * scale;
+}
+
+// Philox4x32-10 counter-based generator (J. K. Salmon, M. A. Moraes,
+// R. O. Dror, D. E. Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11), restated from the publication.
+__device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned int hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const unsigned int hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Uniform noise psi in (-1,1) for bead `orig` of replica `rep` at loop step
+// `it`; phase 1 is the start-up thermostat call before the loop.
+__device__ __forceinline__ void langevin_noise(uint32_t seed, int rep, int orig, long long it, int phase,
+                                               double psi[3]) {
+  const uint4 c = make_uint4((unsigned)orig, (unsigned)(it & 0xffffffff),
+                             (unsigned)((unsigned long long)it >> 32) ^ ((unsigned)phase << 31), (unsigned)rep);
+  const uint4 r = philox4x32(c, make_uint2(seed, 0x5A17u));
+  const double s = 1.0 / 4294967296.0;
+  psi[0] = 2.0 * (((double)r.x + 0.5) * s) - 1.0;
+  psi[1] = 2.0 * (((double)r.y + 0.5) * s) - 1.0;
+  psi[2] = 2.0 * (((double)r.z + 0.5) * s) - 1.0;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide sum of a per-thread double into *dst (one atomic per block).
+__device__ __forceinline__ void block_sum_atomic(double v, double* dst, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0 && t != 0.0) atomicAdd(dst, t);
+  }
+  __syncthreads();
+}
+
+// Box of replica r after the MC trial drawn from u1 (MD.cpp:593-611).
+__device__ __forceinline__ void trial_box(const double box[3], double dlxy, double u1, double nb[3],
+                                          double s[3]) {
+  const double fx = dlxy * (2.0 * u1 - 1.0), fy = fx;
+  const double fz = (box[0] * box[1]) / ((box[0] + fx) * (box[1] + fy));
+  nb[0] = box[0] + fx;
+  nb[1] = box[1] + fy;
+  nb[2] = box[2] * fz;
+  s[0] = nb[0] / box[0];
+  s[1] = nb[1] / box[1];
+  s[2] = nb[2] / box[2];
+}
+
+// ------------------------------------------------------------------ potentials
+// Pair force magnitude with the reference's table index trick
+// (include/MD.h:811-825): force on i = mag * d.
+template <typename R>
+__device__ __forceinline__ R pair_mag(const R* c, R r) {
+  int ci = int(r / c[0]) * 3;
+  ci = ci > 3 ? 3 : ci;  // rows hold two segments; the tables use rc = 2 rm
+  R m = c[ci] - r;
+  return ((c[ci + 1] - c[ci + 2] * m) * m) / r;
+}
+// Pair potential (include/MD.h:913-926).
+template <typename R>
+__device__ __forceinline__ R pair_pot(const R* c, R r) {
+  if (r <= c[0]) {
+    const R m = c[0] - r;
+    return c[1] * m * m + c[2];
+  }
+  const R m = c[3] - r;
+  return m * m * (c[4] - m * c[5]);
+}
+// U(r) - U(r') with r' = r + dr, written so that a small dr does not cancel:
+// each branch's polynomial difference is factored through dr.  rc2 bounds the
+// interaction range of both arguments.
+__device__ __forceinline__ float pair_dpot_f(const float* c, float r, float rn, float dr, float rc) {
+  const bool in0 = r < rc, in1 = rn < rc;
+  if (!in0 && !in1) return 0.f;
+  if (in0 && in1 && ((r <= c[0]) == (rn <= c[0]))) {
+    if (r <= c[0]) {
+      // C1[(rm-r)^2-(rm-r')^2] = C1 dr (2 rm - r - r')
+      return c[1] * dr * (2.f * c[0] - r - rn);
+    }
+    const float m = c[3] - r, mn = c[3] - rn;  // mn = m - dr
+    // m^2(C4 - C5 m) - mn^2(C4 - C5 mn) = dr[C4 (m+mn) - C5 (m^2 + m mn + mn^2)]
+    return dr * (c[4] * (m + mn) - c[5] * (m * m + m * mn + mn * mn));
+  }
+  const float u0 = in0 ? pair_pot<float>(c, r) : 0.f;
+  const float u1 = in1 ? pair_pot<float>(c, rn) : 0.f;
+  return u0 - u1;
+}
+
+}  // namespace smd
