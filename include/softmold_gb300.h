@@ -173,7 +173,8 @@ int smd_synth_vesicle(const char* path, int seed, int n_lipids, double areal_den
 int smd_synth_bilayer(const char* path, int seed, int n_lipids, double areal_density, double zsize,
                       double delta_lxy, double tension);
 int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double areal_density,
-                             double box, double sphere_radius, double head_umin, double gap);
+                             double box, double sphere_radius, double head_umin, double head_umax,
+                             double gap);
 
 /* Reads <name>.mpd and runs it exactly as `MD <name>` would, writing the
  * same .mpd / .xyz / .dat files (MD.cpp:72-755).  precision: smd_precision. */

@@ -531,6 +531,14 @@ double beadbead_potential_fn(V3 d, const double* C, double cut2) {
 // ================================================================ C API
 extern "C" {
 
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n < 1 ? 1 : n);
+#else
+  (void)n;
+#endif
+}
+
 void orc_mt_seed(orc_mt* g, uint32_t seed) {
   g->state[0] = seed;
   for (int i = 1; i < 624; ++i)

@@ -18,6 +18,10 @@
 extern "C" {
 #endif
 
+// OpenMP threads used by the pair and chain passes (1 = the reference's
+// serial order, which makes results bit-identical).
+void orc_set_threads(int n);
+
 // MT19937 (Matsumoto & Nishimura 1998) with the 53-bit real draw used by the
 // reference's MTRand::rand53 (include/algorithms/MersenneTwister.h:337-341).
 typedef struct {

@@ -82,7 +82,7 @@ _SIGS = {
     "smd_synth_bilayer": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                     C.c_double]),
     "smd_synth_vesicle_sphere": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
-                                           C.c_double, C.c_double]),
+                                           C.c_double, C.c_double, C.c_double]),
     "smd_md_main": (C.c_int, [C.c_char_p, C.c_int]),
 }
 
@@ -373,6 +373,7 @@ def synth_bilayer(path, seed, n_lipids, density=3.45, zsize=40.0, delta_lxy=0.01
            "smd_synth_bilayer")
 
 
-def synth_vesicle_sphere(path, seed, n_lipids, density, box, radius=5.0, head_umin=-10.0, gap=2.0):
-    _check(lib().smd_synth_vesicle_sphere(path.encode(), seed, n_lipids, density, box, radius, head_umin, gap),
-           "smd_synth_vesicle_sphere")
+def synth_vesicle_sphere(path, seed, n_lipids, density, box, radius=5.0, head_umin=-10.0, head_umax=10.0,
+                         gap=2.0):
+    _check(lib().smd_synth_vesicle_sphere(path.encode(), seed, n_lipids, density, box, radius, head_umin,
+                                          head_umax, gap), "smd_synth_vesicle_sphere")

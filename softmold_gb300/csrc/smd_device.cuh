@@ -128,6 +128,13 @@ __device__ __forceinline__ int cell_coord(double p, double cs, int n) {
   return c;
 }
 
+// Cell coordinate on the Verlet-list grid, clamped into [0, n) so that a bead
+// outside the box (a blown-up run) can never index outside the cell arrays.
+__device__ __forceinline__ int list_cell_coord(double p, double cs, int n) {
+  int c = cell_coord(p, cs, n);
+  return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
 __device__ __forceinline__ unsigned int to_frac(double x, double invL) {
   // 32-bit fractional coordinate; x == L wraps to 0 like any periodic image.
   return (unsigned int)(long long)(x * invL * 4294967296.0);

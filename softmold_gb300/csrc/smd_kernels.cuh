@@ -73,9 +73,9 @@ __global__ void __launch_bounds__(kBlock) k_bin(DevPtrs P) {
   int n[3];
   double cs[3];
   list_grid(P, r, n, cs);
-  const int cx = cell_coord(P.x[i], cs[0], n[0]);
-  const int cy = cell_coord(P.y[i], cs[1], n[1]);
-  const int cz = cell_coord(P.z[i], cs[2], n[2]);
+  const int cx = list_cell_coord(P.x[i], cs[0], n[0]);
+  const int cy = list_cell_coord(P.y[i], cs[1], n[1]);
+  const int cz = list_cell_coord(P.z[i], cs[2], n[2]);
   const int key = P.rp[r].cell_begin + cx + n[0] * (cy + n[1] * cz);
   P.key[i] = key;
   P.slot[i] = atomicAdd(&P.cell_count[key], 1);
@@ -226,7 +226,8 @@ __global__ void __launch_bounds__(kBlock) k_nbr(DevPtrs P, int cur) {
   const int cb = P.rp[r].cell_begin;
   double cs[3] = {rs.box[0] / n0, rs.box[1] / n1, rs.box[2] / n2};
   const double xi = P.tx[i], yi = P.ty[i], zi = P.tz[i];
-  const int cx = cell_coord(xi, cs[0], n0), cy = cell_coord(yi, cs[1], n1), cz = cell_coord(zi, cs[2], n2);
+  const int cx = list_cell_coord(xi, cs[0], n0), cy = list_cell_coord(yi, cs[1], n1),
+            cz = list_cell_coord(zi, cs[2], n2);
   const double lc2 = P.tab->list_cut2;
   int cnt = 0;
   const int kmax = P.kmax;

@@ -1,0 +1,142 @@
+"""Generates the golden fixtures in this directory from the reference's own code.
+
+Run where the reference sources are present (it needs oracle/_ref, built by
+oracle/build_ref.sh):  python tests/golden/make_golden.py
+
+Fixtures
+  <case>.npz       state of a system relaxed by the reference MD, plus what the
+                   reference's CellOpt / Blob code computes on it (ref_dump):
+                   cell keys, visited pair list, pair and total forces, pair /
+                   bonded / BEAD energies and their size-change differences for
+                   the scales in `scales`, and 4096 MTRand(seed).rand53() draws.
+  traj_bil/        a 48-step reference MD run on a 200-lipid bilayer with the
+                   barostat on: input .mpd, sha256 of every file the run writes
+                   (digests.json) and the small ones verbatim (out/).
+  generators.json  sha256 of the reference generators' .mpd for a few seeds.
+Inputs are seeded synthetic membranes built in the reference generators' terms
+(softmold_gb300 synth_*, byte-identical to generate/liposome and bilayer).
+"""
+from __future__ import annotations
+
+import glob
+import hashlib
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+import softmold_gb300 as smd  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+SCALES = np.array([[1.0001, 1.0001, 0.9998000099990001], [0.9995, 0.9995, 1.0010007505629221],
+                   [1.01, 0.99, 1.0]])
+
+
+def set_run(path, final, store, measure):
+    t = open(path).read()
+    t = re.sub(r"finalTime \S+", f"finalTime {final}", t)
+    t = re.sub(r"storeInterval \S+", f"storeInterval {store}", t)
+    t = re.sub(r"measureInterval \S+", f"measureInterval {measure}", t)
+    open(path, "w").write(t)
+
+
+def run_ref_md(workdir, name):
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.run([os.path.join(REF, "MD"), name], cwd=workdir, env=env, check=True,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+
+
+def dump_case(workdir, name, out_name):
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    dump = os.path.join(workdir, "dump")
+    os.makedirs(dump, exist_ok=True)
+    args = [os.path.join(REF, "ref_dump"), name, dump] + [f"{x:.17g}" for x in SCALES.ravel()]
+    subprocess.run(args, cwd=workdir, env=env, check=True, stdout=subprocess.DEVNULL)
+    m = smd.read_mpd(os.path.join(workdir, name + ".mpd"))
+    n = len(m.type)
+    rd = lambda f, dt: np.fromfile(os.path.join(dump, f), dtype=dt)  # noqa: E731
+    np.savez_compressed(
+        os.path.join(HERE, out_name + ".npz"),
+        pos=m.pos, vel=m.vel, type=m.type, box=m.box, cutoff=m.cutoff, n_types=m.n_types,
+        fconst=m.fconst, uconst=m.uconst, chain_blocks=m.chain_blocks, chain_consts=m.chain_consts,
+        dt=m.dt, gamma=m.gamma, temperature=m.temperature, seed=m.seed, tension=m.tension,
+        delta_lxy=m.delta_lxy,
+        sphere_index=m.sphere_index if m.sphere_index is not None else np.zeros(0, np.int32),
+        sphere_consts=m.sphere_consts if m.sphere_consts is not None else np.zeros(0),
+        keys=rd("keys.i32", np.int32), pairs=rd("pairs.i32", np.int32).reshape(-1, 2),
+        pair_force=rd("pair_force.f64", np.float64).reshape(n, 3),
+        force=rd("force.f64", np.float64).reshape(n, 3),
+        energy=rd("energy.f64", np.float64), scales=SCALES,
+        rand53=rd("rand53.f64", np.float64))
+
+
+def main():
+    if not os.path.exists(os.path.join(REF, "ref_dump")):
+        sys.exit("oracle/_ref is missing: run oracle/build_ref.sh first")
+    tmp = tempfile.mkdtemp(prefix="smd_golden_")
+    try:
+        # relaxed vesicle, 300 lipids in a 30^3 box
+        smd.synth_vesicle(os.path.join(tmp, "ves.mpd"), 1234, 300, 3.45, 30.0)
+        set_run(os.path.join(tmp, "ves.mpd"), 4, 4, 4)
+        run_ref_md(tmp, "ves")
+        dump_case(tmp, "ves", "ves300")
+        # relaxed bilayer, 400 lipids, barostat on
+        smd.synth_bilayer(os.path.join(tmp, "bil.mpd"), 77, 400, 3.45, 20.0, 0.01, 0.0)
+        set_run(os.path.join(tmp, "bil.mpd"), 4, 4, 4)
+        run_ref_md(tmp, "bil")
+        dump_case(tmp, "bil", "bil400")
+        # vesicle with a continuum sphere (BEAD residue, radius 5) whose surface
+        # is 0.8 sigma outside the outer heads, inside its attractive well; the
+        # reference's Umax=10 core is not repulsive enough for a stable run, so
+        # the forces are dumped on the start configuration
+        smd.synth_vesicle_sphere(os.path.join(tmp, "sph.mpd"), 99, 300, 3.45, 40.0, 5.0, -10.0, 10.0, 0.8)
+        dump_case(tmp, "sph", "sphere300")
+        # trajectory: every output file of a short reference run
+        tdir = os.path.join(HERE, "traj_bil")
+        shutil.rmtree(tdir, ignore_errors=True)
+        os.makedirs(os.path.join(tdir, "out"))
+        smd.synth_bilayer(os.path.join(tdir, "bil.mpd"), 5, 200, 3.45, 16.0, 0.01, 0.0)
+        set_run(os.path.join(tdir, "bil.mpd"), 0.96, 0.48, 0.16)
+        run_dir = os.path.join(tmp, "traj")
+        os.makedirs(run_dir)
+        shutil.copy(os.path.join(tdir, "bil.mpd"), run_dir)
+        run_ref_md(run_dir, "bil")
+        digests = {}
+        for f in sorted(glob.glob(os.path.join(run_dir, "*"))):
+            data = open(f, "rb").read()
+            digests[os.path.basename(f)] = hashlib.sha256(data).hexdigest()
+            if len(data) < 100_000:  # large histograms are kept as digests only
+                shutil.copy(f, os.path.join(tdir, "out"))
+        json.dump(digests, open(os.path.join(tdir, "digests.json"), "w"), indent=1)
+        # generator digests
+        gens = []
+        for seed, n in [(1234, 300), (7, 1000)]:
+            d = os.path.join(tmp, f"g{seed}")
+            os.makedirs(d)
+            subprocess.run([os.path.join(REF, "liposome"), "g", str(seed), str(n), "3.45"], cwd=d, check=True,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            gens.append(dict(kind="liposome", seed=seed, n=n, density=3.45,
+                             sha256=hashlib.sha256(open(os.path.join(d, "g.mpd"), "rb").read()).hexdigest()))
+        for seed, n in [(77, 400), (3, 2000)]:
+            d = os.path.join(tmp, f"b{seed}")
+            os.makedirs(d)
+            subprocess.run([os.path.join(REF, "bilayer"), "g", str(seed), str(n), "3.45", "0", "0", "0", "0"],
+                           cwd=d, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            gens.append(dict(kind="bilayer", seed=seed, n=n, density=3.45,
+                             sha256=hashlib.sha256(open(os.path.join(d, "g.mpd"), "rb").read()).hexdigest()))
+        json.dump(gens, open(os.path.join(HERE, "generators.json"), "w"), indent=1)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,65 @@
+"""Host side of the boundary: the C-ABI library, the synthetic generators and
+the .mpd reader.  No GPU is touched here."""
+import ctypes
+import hashlib
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+from conftest import GOLDEN
+
+import softmold_gb300 as smd
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = ctypes.CDLL(smd.LIB_PATH)
+    declared = smd.declared_symbols()
+    assert len(declared) >= 25
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+    # the Python mirror binds every declared function
+    assert sorted(set(declared) - set(smd._SIGS)) == []
+
+
+def test_oracle_is_a_separate_library(built):
+    """The product library carries no oracle code."""
+    out = subprocess.run(["nm", "-D", "--defined-only", smd.LIB_PATH], capture_output=True, text=True).stdout
+    assert "orc_" not in out
+
+
+@pytest.mark.parametrize("entry", json.load(open(os.path.join(GOLDEN, "generators.json"))))
+def test_generators_byte_identical_to_reference(built, tmp_path, entry):
+    p = str(tmp_path / "g.mpd")
+    if entry["kind"] == "liposome":
+        smd.synth_vesicle(p, entry["seed"], entry["n"], entry["density"], 400.0)
+    else:
+        smd.synth_bilayer(p, entry["seed"], entry["n"], entry["density"], 40.0, 0.01, 0.0)
+    assert hashlib.sha256(open(p, "rb").read()).hexdigest() == entry["sha256"]
+
+
+def test_mpd_reader_roundtrip(built, tmp_path):
+    p = str(tmp_path / "b.mpd")
+    smd.synth_bilayer(p, 3, 200, 3.45, 16.0, 0.01, 0.25)
+    m = smd.read_mpd(p)
+    assert len(m.type) == 600 and m.pos.shape == (600, 3)
+    assert m.chain_blocks.tolist() == [[0, 200, 3]]
+    assert np.allclose(m.chain_consts, [[0.7, 100, 1, 100]])
+    assert m.delta_lxy == 0.01 and m.tension == 0.25
+    assert (m.pos >= 0).all() and (m.pos <= m.box).all()
+
+
+def test_create_without_device_fails_loudly(built):
+    """No CPU fallback: without a GPU the library refuses to build a system."""
+    if smd.lib().smd_device_count() > 0:
+        pytest.skip("a GPU is present")
+    g = np.load(os.path.join(GOLDEN, "bil400.npz"))
+    from conftest import mpd_from_golden
+    with pytest.raises(smd.SmdError, match="no CUDA device"):
+        smd.System(mpd_from_golden({k: g[k] for k in g.files}))
+
+
+def test_md_executable_usage(built):
+    r = subprocess.run([smd.MD_EXE], capture_output=True, text=True)
+    assert r.returncode == 0 and "usage" in r.stderr

@@ -1,0 +1,34 @@
+"""The oracle's MD driver reproduces the reference `MD` run byte for byte.
+
+tests/golden/traj_bil holds a 48-step reference run of a 200-lipid bilayer
+with the barostat on, stores every 24 steps and measurements every 8 steps:
+the input and the sha256 of every file the run wrote.  The digests were made
+on x86-64 (glibc prints the 0/0 bond-length average as "-nan" there).
+"""
+import hashlib
+import json
+import os
+import platform
+import shutil
+import subprocess
+
+import pytest
+from conftest import GOLDEN
+
+TRAJ = os.path.join(GOLDEN, "traj_bil")
+
+
+@pytest.mark.skipif(platform.machine() != "x86_64", reason="digests are of x86-64 glibc number formatting")
+def test_md_oracle_matches_reference_outputs(oracle, tmp_path):
+    from oracle_binding import MD
+    shutil.copy(os.path.join(TRAJ, "bil.mpd"), tmp_path)
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([MD, "bil", "1"], cwd=tmp_path, env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    want = json.load(open(os.path.join(TRAJ, "digests.json")))
+    got = {f: hashlib.sha256(open(os.path.join(tmp_path, f), "rb").read()).hexdigest()
+           for f in os.listdir(tmp_path)}
+    assert sorted(got) == sorted(want)
+    for f in want:
+        assert got[f] == want[f], f
+    assert "Resize acceptance ratio" in r.stderr
