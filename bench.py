@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 membrane MD step: bead-steps/s on one GB300.
+
+Workload (default): the flat tensionless bilayer of 20,000 three-bead lipids
+(60,000 beads) at 3.45 lipids/sigma^2, z box 15 sigma, constant-tension MC
+barostat on (deltaLXY 0.01, tension 0), Langevin gamma 1, kT 3, dt 0.02,
+mixed precision.  Seeded synthetic input built in the reference generator's
+geometry, equilibrated for 1,000 untimed steps.
+
+One bench step = one MD loop iteration (MD.cpp:335-729) on the device-resident
+state; L2 is flushed (256 MiB write) between timed steps and every step is
+bracketed by CUDA events on the library's stream.  `e2e` runs the same metric
+through the C ABI with host buffers: per e2e step the state is uploaded, one
+measure interval (50 iterations) is advanced, the energies are measured and the
+state is read back.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG_BYTES_PER_BEAD_STEP = 176  # x,v FP64 r/w 96 + position mirror w/r 32 + force accumulator w/r 48
+METRIC = "bead-steps/s on 1 GB300 (mixed precision)"
+UNIT = "bead-steps/s"
+E2E_INTERVAL = 50
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(args, rank, tmpdir):
+    import softmold_gb300 as smd
+    path = os.path.join(tmpdir, f"bench{rank}.mpd")
+    if args.workload == "bilayer20k":
+        smd.synth_bilayer(path, 1000 + rank, 20000, 3.45, 15.0, 0.01, 0.0)
+        cfg = {"workload": "flat tensionless bilayer, 20,000 3-bead lipids (60,000 beads), 3.45/sigma^2, "
+                           "z 15 sigma, MC barostat deltaLXY 0.01 tension 0, kT 3, gamma 1, dt 0.02"}
+    elif args.workload == "vesicle5k":
+        smd.synth_vesicle(path, 1000 + rank, 5000, 3.45, 60.0)
+        cfg = {"workload": "vesicle, 5,000 3-bead lipids (15,000 beads), 60^3 box, kT 3, gamma 1, dt 0.02"}
+    else:
+        raise SystemExit(f"unknown workload {args.workload}")
+    return path, smd.read_mpd(path), cfg
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(path, threads, target_s=12.0):
+    """The oracle's restatement of the reference MD loop on the host cores."""
+    import ctypes as C
+    lib = C.CDLL(os.path.join(ROOT, "oracle", "_build", "libsmd_oracle.so"))
+    lib.orc_md_time.argtypes = [C.c_char_p, C.c_int, C.c_int]
+    lib.orc_md_time.restype = C.c_double
+    name = path[:-4].encode()
+    t = lib.orc_md_time(name, threads, 4)
+    steps = max(4, int(4 * target_s / max(t, 1e-3)))
+    t = lib.orc_md_time(name, threads, steps)
+    return steps, t
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU algorithm (the oracle port of
+    MD.cpp, built here) on all host threads, same workload and metric."""
+    if rank != 0:
+        return
+    import softmold_gb300 as smd
+    from softmold_gb300 import build
+    build.build_oracle()
+    with tempfile.TemporaryDirectory() as tmp:
+        path, m, cfg = workload(args, 0, tmp)
+        n = len(m.type)
+        threads = os.cpu_count() or 1
+        per_step = 10
+        import ctypes as C
+        lib = C.CDLL(os.path.join(ROOT, "oracle", "_build", "libsmd_oracle.so"))
+        lib.orc_md_time.argtypes = [C.c_char_p, C.c_int, C.c_int]
+        lib.orc_md_time.restype = C.c_double
+        name = path[:-4].encode()
+        for _ in range(args.warmup):
+            lib.orc_md_time(name, threads, 2)
+        times = [lib.orc_md_time(name, threads, per_step) for _ in range(args.steps)]
+        total = sum(times)
+        value = n * per_step * args.steps / total
+        sample = f"{args.steps} samples of {per_step} MD steps of the {n}-bead workload"
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / (args.steps * per_step),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="bilayer20k")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--skin", type=float, default=0.5)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import softmold_gb300 as smd
+    from softmold_gb300 import build
+    build.build_library()
+
+    tmp = tempfile.mkdtemp(prefix="smd_bench_")
+    path, m, cfg = workload(args, rank, tmp)
+    n = len(m.type)
+    stream = torch.cuda.Stream()
+    s = smd.System(m, precision=smd.MIXED, skin=args.skin)
+    s.set_stream(stream.cuda_stream)
+    s.prepare()
+    s.advance(1000)  # equilibration from the lattice start (untimed)
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    K, W = args.steps, args.warmup
+
+    def timed_loop(sys_, steps, profile=False):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        if profile:
+            sys_.profile(True)
+        l0 = sys_.timing()[2]
+        with torch.cuda.stream(stream):
+            for k in range(steps):
+                flush.zero_()
+                starts[k].record(stream)
+                sys_.advance(1, asynchronous=True)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+        sys_.sync()
+        launches = sys_.timing()[2] - l0
+        ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+        return sum(ms), launches
+
+    timed_loop(s, W)
+    rebuilds0 = s.rebuilds()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_wait = time.time()
+    while not sampler.lines and time.time() - t_wait < 5:  # NVML start-up outside the timed region
+        time.sleep(0.05)
+    torch.cuda.nvtx.range_push("timed")
+    total_ms, launches = timed_loop(s, K, profile=True)
+    torch.cuda.nvtx.range_pop()
+    clocks = sampler.stop()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    kernel_ms, kernel_launches, _ = s.timing()
+    s.profile(False)
+    rebuilds = s.rebuilds() - rebuilds0
+    last_disp, slack = s.list_state()
+
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = n * world * K / (max_ms / 1e3)
+
+    # FP64 plain form on the same state, and the mixed form's force error
+    pos, vel = s.state()
+    p = smd.System(m, precision=smd.PLAIN_FP64, skin=args.skin)
+    p.set_stream(stream.cuda_stream)
+    p.set_box(s.box())
+    p.set_state(pos, vel)
+    f_plain = p.forces()
+    f_mixed = s.forces()
+    p.prepare()
+    fscale = np.abs(f_plain).max()
+    force_err = {"max": float(np.abs(f_mixed - f_plain).max() / fscale),
+                 "rms": float(np.sqrt(np.mean((f_mixed - f_plain) ** 2)) / fscale),
+                 "reference": "plain FP64 GPU form (matches the CPU oracle to 1e-12)"}
+    kp = min(K, 40)
+    timed_loop(p, 3)
+    plain_ms, _ = timed_loop(p, kp)
+    plain_value = n * kp / (plain_ms / 1e3)
+    p.close()
+
+    # end to end through the C ABI with host buffers
+    hp = torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy()
+    hv = torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy()
+    hp[:], hv[:] = s.state()
+    e2e_t = []
+    for k in range(args.e2e_steps + 2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.set_state(hp, hv)
+        s.advance(E2E_INTERVAL)
+        e = s.energy()
+        pp, vv = s.state()
+        hp[:], hv[:] = pp, vv
+        t1 = time.perf_counter()
+        if k >= 2:
+            e2e_t.append(t1 - t0)
+    e2e_value = n * E2E_INTERVAL / statistics.mean(e2e_t)
+    e2e = {"value": e2e_value * world, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes + hv.nbytes),
+           "d2h_bytes_per_step": int(hp.nbytes + hv.nbytes + 32),
+           "md_steps_per_e2e_step": E2E_INTERVAL, "potential_last": e[0]["pair"] + e[0]["bonded"]}
+
+    peak, peak_kind = load_peaks()
+    achieved = None
+    if kernel_launches:
+        avg_s = kernel_ms / kernel_launches / 1e3
+        achieved = ALG_BYTES_PER_BEAD_STEP * n / avg_s / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    if os.path.exists(tf):
+        d = json.load(open(tf))
+        traffic = d.get("dram_bytes_per_bead") and d["dram_bytes_per_bead"] * n
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "kernel": "k_step<mixed> (fused forces + Langevin + Verlet)",
+                "kernel_avg_us": 1e3 * kernel_ms / kernel_launches if kernel_launches else None,
+                "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_bead_step": ALG_BYTES_PER_BEAD_STEP}
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        ck = os.path.join(tmp, "cpu.mpd")
+        smd.mpd_update_state(path, ck, pos, vel, s.box(), 0.0)
+        threads = os.cpu_count() or 1
+        steps, secs = cpu_baseline(ck, threads)
+        base = {"value": n * steps / secs, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"{steps} MD steps of the same {n}-bead bilayer (equilibrated state), oracle port "
+                          f"of MD.cpp with OpenMP"}
+    s.close()
+    if rank == 0:
+        cfg.update({"beads_per_gpu": n, "l2": "flushed (256 MiB write) between timed steps",
+                    "skin": args.skin, "parallelism": f"replicas x{world}",
+                    "list_rebuilds_per_step": rebuilds / K, "last_max_displacement": last_disp})
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": max_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+i64 fixed-point forces, f64 integrate", "data": "synthetic", "config": cfg,
+            "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": launches,
+            "plain_fp64": {"value": plain_value * world, "ms_per_step": plain_ms / kp,
+                           "mixed_speedup": value / (plain_value * world)},
+            "force_err": force_err,
+        }), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -99,6 +99,9 @@ int smd_set_stream(smd_system* h, void* cuda_stream);
 int smd_get_state(smd_system* h, double* pos, double* vel);
 int smd_set_state(smd_system* h, const double* pos, const double* vel);
 int smd_get_box(smd_system* h, int replica, double box[3]);
+/* Sets a replica's box without moving the beads (Blob::setSize,
+ * include/system.h:4436-4444); positions must lie inside the new box. */
+int smd_set_box(smd_system* h, int replica, const double box[3]);
 
 /* Conservative forces at the current positions, no Langevin term:
  * CellOpt::computeForce + Blob::doChainForce (+ doBeadForce)
@@ -135,11 +138,18 @@ int smd_prepare(smd_system* h, int do_second, smd_energy* energy_out);
 
 /* Advances `steps` iterations of the MD.cpp:335-729 loop body: thermostat,
  * pair and bonded forces, second half-kick, the MC box move on every
- * resize_rate-th step, and the next step's first half-kick and drift.  With
- * stop_at_measure != 0 the last iteration stops after its second half-kick so
- * the caller can read the measured state; the next smd_advance call (steps may
- * be 0) completes that iteration. */
-int smd_advance(smd_system* h, int steps, int stop_at_measure);
+ * resize_rate-th step, and the next step's first half-kick and drift.
+ * flags: SMD_STOP_AT_MEASURE stops the last iteration after its second
+ * half-kick so the caller can read the measured state (the next smd_advance
+ * call, steps may be 0, completes that iteration); SMD_ASYNC returns without
+ * waiting for the device (errors surface at the next synchronising call or
+ * smd_sync). */
+#define SMD_STOP_AT_MEASURE 1
+#define SMD_ASYNC 2
+int smd_advance(smd_system* h, int steps, int flags);
+
+/* Waits for the handle's stream and reports any device-side error. */
+int smd_sync(smd_system* h);
 
 /* Barostat statistics of a replica. */
 int smd_mc_stats_get(smd_system* h, int replica, smd_mc_stats* out);
@@ -159,12 +169,22 @@ int smd_set_temperature(smd_system* h, int replica, double kT, int update_sigma)
  * Lets a test drive the device step with the reference's MT19937 stream. */
 int smd_set_noise_once(smd_system* h, const double* psi);
 
-/* Device time (ms) of the fused step kernel over the last smd_advance call,
- * and the number of kernel launches it issued. */
-int smd_last_timing(smd_system* h, double* step_kernel_ms, long* launches);
+/* Per-launch CUDA-event timing of the fused step kernel (on = 1).  While on,
+ * every step-kernel launch is bracketed by events on the handle's stream. */
+int smd_profile(smd_system* h, int on);
+
+/* Accumulated device time (ms) and launch count of the fused step kernel
+ * since profiling was switched on, and the total number of kernel launches
+ * the handle has issued. */
+int smd_last_timing(smd_system* h, double* step_kernel_ms, long* step_kernel_launches, long* total_launches);
 
 /* Number of Verlet-list rebuilds so far. */
 long smd_rebuild_count(smd_system* h);
+
+/* Largest bead displacement from its list-build position seen by the last
+ * step, and the list-distance slack used by accepted box moves since the
+ * build (both in sigma; the list is rebuilt when their sum exceeds skin/2). */
+int smd_list_state(smd_system* h, double* max_disp, double* slack);
 
 /* Runs the synthetic generators (restating generate/liposome.cpp,
  * generate/bilayer.cpp and generate/continuumSphereAndLiposome.cpp) and
@@ -175,6 +195,11 @@ int smd_synth_bilayer(const char* path, int seed, int n_lipids, double areal_den
 int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double areal_density,
                              double box, double sphere_radius, double head_umin, double head_umax,
                              double gap);
+
+/* Rewrites the .mpd at in_path with new positions, velocities, box and
+ * initialTime into out_path (the store of MD.cpp:373-377). */
+int smd_mpd_update_state(const char* in_path, const char* out_path, const double* pos, const double* vel,
+                         const double box[3], double time);
 
 /* Reads <name>.mpd and runs it exactly as `MD <name>` would, writing the
  * same .mpd / .xyz / .dat files (MD.cpp:72-755).  precision: smd_precision. */

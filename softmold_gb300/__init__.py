@@ -64,6 +64,7 @@ _SIGS = {
     "smd_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "smd_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "smd_get_box": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "smd_set_box": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "smd_compute_forces": (C.c_int, [C.c_void_p, C.c_void_p]),
     "smd_compute_pair_forces": (C.c_int, [C.c_void_p, C.c_void_p]),
     "smd_compute_energy": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -76,8 +77,12 @@ _SIGS = {
     "smd_mc_log": (C.c_long, [C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_void_p, C.c_void_p]),
     "smd_set_temperature": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int]),
     "smd_set_noise_once": (C.c_int, [C.c_void_p, C.c_void_p]),
-    "smd_last_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_last_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "smd_sync": (C.c_int, [C.c_void_p]),
+    "smd_mpd_update_state": (C.c_int, [C.c_char_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
     "smd_rebuild_count": (C.c_long, [C.c_void_p]),
+    "smd_list_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "smd_synth_vesicle": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double]),
     "smd_synth_bilayer": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                     C.c_double]),
@@ -304,6 +309,10 @@ class System:
         _check(lib().smd_get_box(self.h, replica, b.ctypes.data), "smd_get_box")
         return b
 
+    def set_box(self, box, replica=0):
+        b = np.ascontiguousarray(box, np.float64)
+        _check(lib().smd_set_box(self.h, replica, b.ctypes.data), "smd_set_box")
+
     def forces(self, pair_only=False):
         f = np.zeros((self.n, 3))
         fn = lib().smd_compute_pair_forces if pair_only else lib().smd_compute_forces
@@ -338,8 +347,23 @@ class System:
         _check(lib().smd_prepare(self.h, 1 if do_second else 0, C.byref(e) if energy else None), "smd_prepare")
         return dict(pair=e.pair, bonded=e.bonded, sphere=e.sphere, kinetic=e.kinetic) if energy else None
 
-    def advance(self, steps, stop_at_measure=False):
-        _check(lib().smd_advance(self.h, int(steps), 1 if stop_at_measure else 0), "smd_advance")
+    def advance(self, steps, stop_at_measure=False, asynchronous=False):
+        flags = (1 if stop_at_measure else 0) | (2 if asynchronous else 0)
+        _check(lib().smd_advance(self.h, int(steps), flags), "smd_advance")
+
+    def sync(self):
+        _check(lib().smd_sync(self.h), "smd_sync")
+
+    def profile(self, on=True):
+        _check(lib().smd_profile(self.h, 1 if on else 0), "smd_profile")
+
+    def timing(self):
+        """(step-kernel ms, step-kernel launches, total launches)."""
+        ms = C.c_double(0)
+        k = C.c_long(0)
+        n = C.c_long(0)
+        _check(lib().smd_last_timing(self.h, C.byref(ms), C.byref(k), C.byref(n)), "smd_last_timing")
+        return ms.value, k.value, n.value
 
     def set_noise_once(self, psi):
         p = np.ascontiguousarray(psi, np.float64)
@@ -355,13 +379,24 @@ class System:
         return dict(trials=s.trials, accepted=s.accepted, last_dU=s.last_dU)
 
     def launches(self):
-        ms = C.c_double(0)
-        n = C.c_long(0)
-        _check(lib().smd_last_timing(self.h, C.byref(ms), C.byref(n)), "smd_last_timing")
-        return n.value
+        return self.timing()[2]
 
     def rebuilds(self):
         return lib().smd_rebuild_count(self.h)
+
+    def list_state(self):
+        d = C.c_double(0)
+        sl = C.c_double(0)
+        _check(lib().smd_list_state(self.h, C.byref(d), C.byref(sl)), "smd_list_state")
+        return d.value, sl.value
+
+
+def mpd_update_state(in_path, out_path, pos, vel, box, time):
+    p = np.ascontiguousarray(pos, np.float64)
+    v = np.ascontiguousarray(vel, np.float64)
+    b = np.ascontiguousarray(box, np.float64)
+    _check(lib().smd_mpd_update_state(in_path.encode(), out_path.encode(), p.ctypes.data, v.ctypes.data,
+                                      b.ctypes.data, float(time)), "smd_mpd_update_state")
 
 
 def synth_vesicle(path, seed, n_lipids, density=3.45, box=400.0):

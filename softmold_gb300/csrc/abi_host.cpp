@@ -34,4 +34,19 @@ int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double de
   return smd::mpd_write_file(path, s, err);
 }
 
+int smd_mpd_update_state(const char* in_path, const char* out_path, const double* pos, const double* vel,
+                         const double box[3], double time) {
+  if (!in_path || !out_path) return 1;
+  smd::MpdSystem s;
+  std::string err;
+  if (int rc = smd::mpd_read_file(in_path, s, err)) return rc;
+  const size_t n = 3 * (size_t)s.nParticles;
+  if (pos) s.pos.assign(pos, pos + n);
+  if (vel) s.vel.assign(vel, vel + n);
+  if (box)
+    for (int k = 0; k < 3; ++k) s.size[k] = box[k];
+  s.initialTime = time;
+  return smd::mpd_write_file(out_path, s, err);
+}
+
 }  // extern "C"

@@ -150,7 +150,7 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
     long long m = it;
     while (m < next && !is_measure(m)) ++m;
     if (m < next && m <= endInt) {
-      if (smd_advance(h, (int)(m - it + 1), 1)) return die("smd_advance");
+      if (smd_advance(h, (int)(m - it + 1), SMD_STOP_AT_MEASURE)) return die("smd_advance");
       S.initialTime = (double)m * S.deltaT;
       const time_t last = current;
       current = time(NULL);

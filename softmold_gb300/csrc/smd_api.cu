@@ -58,8 +58,10 @@ struct smd_system {
   std::vector<void*> allocs;
   long launches = 0;
   bool profile = false;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double step_ms = 0;
+  long step_launches = 0;
+  std::vector<cudaEvent_t> prof_events;  // pairs around step-kernel launches
+  size_t prof_used = 0;
   std::vector<double> trial_host;
   int trials_staged = 0, trials_used = 0;
   std::vector<std::vector<double>> mc_fluct;  // per replica, every trial so far
@@ -80,12 +82,16 @@ struct smd_system {
   }
   ~smd_system() {
     if (stream) cudaStreamSynchronize(stream);
+    for (cudaEvent_t e : prof_events) cudaEventDestroy(e);
     for (void* q : allocs) cudaFree(q);
     if (own_stream && stream) cudaStreamDestroy(stream);
-    if (ev0) cudaEventDestroy(ev0);
-    if (ev1) cudaEventDestroy(ev1);
   }
   int grid() const { return (n + kBlock - 1) / kBlock; }
+  int grid_lanes() const { return (int)(((long long)n * kLanes + kBlock - 1) / kBlock); }
+  int sms = 152;
+  // list build: one CTA per cell; the hardware scheduler balances the very
+  // uneven cell occupancy of a membrane better than a fixed stride does
+  int nbr_grid() const { return n_cells; }
 };
 
 namespace {
@@ -112,16 +118,16 @@ __global__ void k_set_rebuild(Global* g, int v) { g->rebuild = v; }
 int rebuild_if_needed(smd_system* h, bool clear_after = false) {
   auto& P = h->P;
   const int g = h->grid();
-  SMD_LAUNCH(h, k_bin<<<g, kBlock, 0, h->stream>>>(P));
+  SMD_LAUNCH(h, k_bin<<<g, kBlock, 0, h->stream>>>(P, h->cur, h->mixed ? 1 : 0));
   SMD_LAUNCH(h, k_scan_tiles<<<h->n_tiles, kBlock, 0, h->stream>>>(P));
   SMD_LAUNCH(h, k_scan_sums<<<1, kBlock, 0, h->stream>>>(P, h->n_tiles));
   SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, h->stream>>>(P));
   if (h->mixed) {
     SMD_LAUNCH(h, k_reorder<true><<<g, kBlock, 0, h->stream>>>(P, h->cur));
-    SMD_LAUNCH(h, k_nbr<true><<<g, kBlock, 0, h->stream>>>(P, h->cur));
+    SMD_LAUNCH(h, (k_nbr_cells<true><<<h->nbr_grid(), kNbrThreads, 0, h->stream>>>(P, h->cur)));
   } else {
     SMD_LAUNCH(h, k_reorder<false><<<g, kBlock, 0, h->stream>>>(P, h->cur));
-    SMD_LAUNCH(h, k_nbr<false><<<g, kBlock, 0, h->stream>>>(P, h->cur));
+    SMD_LAUNCH(h, (k_nbr_cells<false><<<h->nbr_grid(), kNbrThreads, 0, h->stream>>>(P, h->cur)));
   }
   if (clear_after) SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 0));
   return 0;
@@ -132,14 +138,52 @@ int force_rebuild(smd_system* h) {
   return rebuild_if_needed(h, true);
 }
 
+// Sums the elapsed time of the recorded event pairs (after a stream sync).
+int collect_profile(smd_system* h) {
+  for (size_t k = 0; k + 1 < h->prof_used; k += 2) {
+    float ms = 0;
+    SMD_CUDA(cudaEventElapsedTime(&ms, h->prof_events[k], h->prof_events[k + 1]));
+    h->step_ms += ms;
+    h->step_launches++;
+  }
+  h->prof_used = 0;
+  return 0;
+}
+
+int prof_mark(smd_system* h) {
+  if (h->prof_used == h->prof_events.size()) {
+    if (h->prof_used >= 8192) {  // bound the pool: drain what was recorded
+      SMD_CUDA(cudaStreamSynchronize(h->stream));
+      if (int rc = collect_profile(h)) return rc;
+    } else {
+      cudaEvent_t e;
+      SMD_CUDA(cudaEventCreate(&e));
+      h->prof_events.push_back(e);
+    }
+  }
+  SMD_CUDA(cudaEventRecord(h->prof_events[h->prof_used++], h->stream));
+  return 0;
+}
+
 template <int FL>
 int launch_step(smd_system* h) {
   auto& P = h->P;
   const int g = h->grid();
-  if (h->mixed)
-    SMD_LAUNCH(h, k_step<true, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, h->it));
-  else
-    SMD_LAUNCH(h, k_step<false, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, h->it));
+  constexpr bool kLoopStep = (FL & (F_FORCES | F_ENERGY | F_INIT)) == 0;
+  if (kLoopStep && h->profile) {
+    if (int rc = prof_mark(h)) return rc;
+  }
+  const int gl = h->grid_lanes();
+  if (h->mixed) {
+    SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
+    SMD_LAUNCH(h, (k_integ<true, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, h->it)));
+  } else {
+    SMD_LAUNCH(h, (k_force<false, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
+    SMD_LAUNCH(h, (k_integ<false, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, h->it)));
+  }
+  if (kLoopStep && h->profile) {
+    if (int rc = prof_mark(h)) return rc;
+  }
   return 0;
 }
 
@@ -220,6 +264,7 @@ int read_error(smd_system* h) {
   Global g;
   SMD_CUDA(cudaMemcpyAsync(&g, h->P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (g.error & 2) return fail(8, "a Verlet-list cell holds more than 1024 beads (collapsed system)");
   if (g.error & 1) {
     char buf[256];
     std::snprintf(buf, sizeof buf,
@@ -354,6 +399,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     p.gamma = d.gamma;
     p.kT = d.temperature;
     p.sigma = std::sqrt((6.0 * d.temperature * d.gamma) / d.dt);
+    p.sig31 = p.sigma * (1.0 / 2147483648.0);
     p.tension = d.tension;
     p.dlxy = d.delta_lxy;
     p.seed = d.seed;
@@ -361,8 +407,9 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     p.bead_begin = bead;
     p.bead_end = bead + d.n;
     if (d.delta_lxy != 0) h->barostat = true;
+    // one extra cell per axis: a growing box coarsens the grid in derive_box
     int cap = 1;
-    for (int k = 0; k < 3; ++k) cap *= (int)(1.3 * d.box[k] / T.list_cut) + 2;
+    for (int k = 0; k < 3; ++k) cap *= std::max(1, (int)(d.box[k] / T.list_cut)) + 1;
     p.cell_begin = cells;
     p.cell_cap = cap;
     cells += cap;
@@ -398,6 +445,12 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   h->n_cells = cells;
   h->n_tiles = (cells + kScanTile - 1) / kScanTile;
   // ---- device memory
+  {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+      h->sms = sms;
+  }
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(2, "cudaStreamCreate failed");
   h->own_stream = true;
@@ -419,9 +472,15 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     if ((rc = h->alloc(&P.d4[0], total)) || (rc = h->alloc(&P.d4[1], total)) || (rc = h->alloc(&P.dt4, total)))
       return rc;
   }
-  int** ints[] = {&P.orig, &P.inv, &P.cinfo, &P.torig, &P.tcinfo, &P.key, &P.slot, &P.nnbr, &P.key_out};
+  if ((rc = h->alloc(&P.ref, total))) return rc;
+  int** ints[] = {&P.orig, &P.inv, &P.cinfo, &P.torig, &P.tcinfo, &P.key, &P.slot, &P.tkey, &P.nnbr, &P.key_out};
   for (int** q : ints)
     if ((rc = h->alloc(q, total))) return rc;
+  if (h->mixed) {
+    if ((rc = h->alloc(&P.fq, 3 * (size_t)total))) return rc;
+  } else {
+    if ((rc = h->alloc(&P.fp, 3 * (size_t)total))) return rc;
+  }
   if ((rc = h->alloc(&P.cell_count, cells)) || (rc = h->alloc(&P.cell_start, cells + 1)) ||
       (rc = h->alloc(&P.block_sums, h->n_tiles)))
     return rc;
@@ -450,6 +509,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
         rs[r].box[k] = d.box[k];
         rs[r].scale[k] = 1.0;
       }
+      derive_box(rs[r], h->rp[r].cell_cap, T.list_cut);
       for (int i = 0; i < d.n; ++i, ++b) {
         hx[b] = d.pos[3 * i];
         hy[b] = d.pos[3 * i + 1];
@@ -496,7 +556,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   const int need = std::max(g.need_nbr, 1);
   h->kmax = ((int)(need * 1.5) + 32 + 7) / 8 * 8;
   P.kmax = h->kmax;
-  if ((rc = h->alloc(&P.nbr, (size_t)h->kmax * h->npad))) return rc;
+  if ((rc = h->alloc(&P.nbr, (size_t)h->kmax * total))) return rc;
   g.error = 0;
   g.need_nbr = 0;
   g.rebuild = 1;
@@ -504,8 +564,6 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   SMD_CUDA(cudaMemcpy(P.g, &g, sizeof(Global), cudaMemcpyHostToDevice));
   if ((rc = rebuild_if_needed(h.get()))) return rc;
   if ((rc = read_error(h.get()))) return rc;
-  SMD_CUDA(cudaEventCreate(&h->ev0));
-  SMD_CUDA(cudaEventCreate(&h->ev1));
   *out = h.release();
   return 0;
 }
@@ -601,6 +659,25 @@ int smd_get_box(smd_system* h, int replica, double box[3]) {
   SMD_CUDA(cudaMemcpyAsync(&rs, h->P.rs + replica, sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
   for (int k = 0; k < 3; ++k) box[k] = rs.box[k];
+  return 0;
+}
+
+int smd_set_box(smd_system* h, int replica, const double box[3]) {
+  if (!h || !box || replica < 0 || replica >= h->n_rep) return fail(1, "bad arguments");
+  for (int k = 0; k < 3; ++k)
+    if (!(box[k] > 0) || int(box[k] / h->tab.rc) < 3) return fail(1, "box edge shorter than 3 cutoffs");
+  RepState rs;
+  SMD_CUDA(cudaMemcpyAsync(&rs, h->P.rs + replica, sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < 3; ++k) rs.box[k] = box[k];
+  derive_box(rs, h->rp[replica].cell_cap, h->tab.list_cut);
+  SMD_CUDA(cudaMemcpyAsync(h->P.rs + replica, &rs, sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
+  if (h->mixed)
+    SMD_LAUNCH(h, k_mirror<true><<<h->grid(), kBlock, 0, h->stream>>>(h->P, h->cur));
+  else
+    SMD_LAUNCH(h, k_mirror<false><<<h->grid(), kBlock, 0, h->stream>>>(h->P, h->cur));
+  SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(h->P.g, 1));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
   return 0;
 }
 
@@ -717,13 +794,12 @@ int smd_prepare(smd_system* h, int do_second, smd_energy* energy_out) {
   return read_error(h);
 }
 
-int smd_advance(smd_system* h, int steps, int stop_at_measure) {
+int smd_advance(smd_system* h, int steps, int flags) {
   if (!h || steps < 0) return fail(1, "bad arguments");
+  const bool stop_at_measure = (flags & SMD_STOP_AT_MEASURE) != 0;
+  const bool async = (flags & SMD_ASYNC) != 0;
   int rc = complete_pending(h);
   if (rc) return rc;
-  if (h->profile) {
-    SMD_CUDA(cudaEventRecord(h->ev0, h->stream));
-  }
   int done = 0;
   while (done < steps) {
     const int chunk = std::min(steps - done, kTrialChunk * std::max(1, h->resize_rate) / 2);
@@ -758,18 +834,28 @@ int smd_advance(smd_system* h, int steps, int stop_at_measure) {
     }
     done += chunk;
   }
-  if (h->profile) {
-    SMD_CUDA(cudaEventRecord(h->ev1, h->stream));
-    SMD_CUDA(cudaEventSynchronize(h->ev1));
-    float ms = 0;
-    SMD_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-    h->step_ms = ms;
-  }
+  if (async) return 0;
+  return smd_sync(h);
+}
+
+int smd_sync(smd_system* h) {
+  if (!h) return fail(1, "null handle");
   SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (int rc = collect_profile(h)) return rc;
   if (!h->at_measure || !h->pending_trial) {
     if (int e = flush_mc_log(h)) return e;
   }
   return read_error(h);
+}
+
+int smd_profile(smd_system* h, int on) {
+  if (!h) return fail(1, "null handle");
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (int rc = collect_profile(h)) return rc;
+  h->profile = on != 0;
+  h->step_ms = 0;
+  h->step_launches = 0;
+  return 0;
 }
 
 int smd_mc_stats_get(smd_system* h, int replica, smd_mc_stats* out) {
@@ -803,7 +889,10 @@ int smd_set_temperature(smd_system* h, int replica, double kT, int update_sigma)
   for (int r = 0; r < h->n_rep; ++r) {
     if (replica >= 0 && r != replica) continue;
     h->rp[r].kT = kT;
-    if (update_sigma) h->rp[r].sigma = std::sqrt((6.0 * kT * h->rp[r].gamma) / h->rp[r].dt);
+    if (update_sigma) {
+      h->rp[r].sigma = std::sqrt((6.0 * kT * h->rp[r].gamma) / h->rp[r].dt);
+      h->rp[r].sig31 = h->rp[r].sigma * (1.0 / 2147483648.0);
+    }
   }
   SMD_CUDA(cudaMemcpyAsync(h->P.rp, h->rp.data(), h->n_rep * sizeof(RepParams), cudaMemcpyHostToDevice,
                            h->stream));
@@ -811,10 +900,21 @@ int smd_set_temperature(smd_system* h, int replica, double kT, int update_sigma)
   return 0;
 }
 
-int smd_last_timing(smd_system* h, double* ms, long* launches) {
+int smd_last_timing(smd_system* h, double* ms, long* step_launches, long* launches) {
   if (!h) return fail(1, "null handle");
   if (ms) *ms = h->step_ms;
+  if (step_launches) *step_launches = h->step_launches;
   if (launches) *launches = h->launches;
+  return 0;
+}
+
+int smd_list_state(smd_system* h, double* max_disp, double* slack) {
+  if (!h) return fail(1, "null handle");
+  Global g;
+  SMD_CUDA(cudaMemcpyAsync(&g, h->P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (max_disp) *max_disp = g.last_disp;
+  if (slack) *slack = g.slack;
   return 0;
 }
 

@@ -9,7 +9,9 @@
 //                                    PLAIN = double4 (x,y,z,type bits)
 //   orig / inv                       sorted -> file order and back
 //   cinfo                            CHAIN role of the bead (position, length, set)
-// The Verlet list is column-major: nbr[k * npad + i] is neighbour k of bead i.
+// The Verlet list is bead-major: nbr[i * kmax + k] is neighbour k of bead i.
+// Between the two passes of a step the non-bonded force of each bead is held
+// as int64 fixed point (MIXED, fq) or FP64 (PLAIN, fp), SoA x | y | z.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -23,6 +25,7 @@ constexpr int kMaxTypes = 8;
 constexpr int kMaxChainSets = 32;
 constexpr int kBlock = 256;
 constexpr int kScanTile = 2048;  // cells per scan block (256 threads x 8)
+constexpr int kLanes = 8;        // lanes per bead in the list build and the pair pass
 
 // cinfo word: bit 31 chain member, bits 0..11 position in chain, bits 12..23
 // chain length, bits 24..28 chain-constant set; bit 30 marks a BEAD sphere.
@@ -33,6 +36,7 @@ __host__ __device__ inline int cinfo_pack(int p, int len, int set) {
 
 struct RepParams {  // per replica, fixed
   double dt, gamma, kT, sigma, tension, dlxy;
+  double sig31;      // sigma * 2^-31: noise amplitude per unit of a signed 32-bit draw
   uint32_t seed;
   int resize_rate;
   int bead_begin, bead_end;
@@ -41,6 +45,9 @@ struct RepParams {  // per replica, fixed
 
 struct RepState {  // per replica, updated on the device
   double box[3];
+  double frac_per_len[3];  // 2^32 / box: real -> 32-bit fractional coordinate
+  float len_per_frac[3];   // box / 2^32
+  float pad_f;
   double trial_box[3];
   double scale[3];   // scale of the last accepted / current trial
   double dU_pair, dU_bond;
@@ -53,10 +60,11 @@ struct RepState {  // per replica, updated on the device
 };
 
 struct Global {  // single instance
-  double disp;                 // displacement bound since the last list build
-  unsigned long long mc_shift; // largest bead shift of accepted box moves (double bits)
+  double slack;                // list-distance slack used up by accepted box moves since the build
+  unsigned long long mc_shift; // slack of this step's accepted box moves (double bits, max over replicas)
   long long n_rebuilds;
-  unsigned int vmax_bits;      // max |v| of the current step (float bits)
+  unsigned int dmax_bits;      // largest bead displacement from its build position (float bits)
+  float last_disp;
   unsigned int blocks_done;    // last-block counter
   int rebuild;                 // 1: rebuild the Verlet list before the next force pass
   int error;                   // bit 0: list overflow, bit 1: cell overflow (>kMaxCell)
@@ -88,15 +96,18 @@ struct DevPtrs {
   double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az;
   uint4* m4[2];
   double4* d4[2];
+  uint4* ref;        // fractional position of each bead at the last list build
   int *orig, *inv, *cinfo;
   // rebuild scratch
   uint4* mt;
   double4* dt4;
   double *tx, *ty, *tz, *tvx, *tvy, *tvz, *tax, *tay, *taz;
   int *torig, *tcinfo;
-  int *key, *slot;
+  int *key, *slot, *tkey;
   int *cell_count, *cell_start, *block_sums;
   int *nbr, *nnbr;
+  long long* fq;     // MIXED pair force, fixed point, 3*n (x | y | z)
+  double* fp;        // PLAIN pair force, 3*n
   RepParams* rp;
   RepState* rs;
   Global* g;
@@ -135,9 +146,28 @@ __device__ __forceinline__ int list_cell_coord(double p, double cs, int n) {
   return c < 0 ? 0 : (c >= n ? n - 1 : c);
 }
 
-__device__ __forceinline__ unsigned int to_frac(double x, double invL) {
+__device__ __forceinline__ unsigned int to_frac(double x, double frac_per_len) {
   // 32-bit fractional coordinate; x == L wraps to 0 like any periodic image.
-  return (unsigned int)(long long)(x * invL * 4294967296.0);
+  return (unsigned int)(long long)(x * frac_per_len);
+}
+
+// Derived box quantities of a replica: fractional scales and the Verlet-list
+// grid (cells of at least list_cut, at most cap cells).  Computed on the host
+// at creation and on the device when a box move is accepted; the same IEEE
+// arithmetic gives the same grid on both.
+__host__ __device__ inline void derive_box(RepState& rs, int cap, double list_cut) {
+  for (int d = 0; d < 3; ++d) {
+    rs.frac_per_len[d] = 4294967296.0 / rs.box[d];
+    rs.len_per_frac[d] = (float)(rs.box[d] * (1.0 / 4294967296.0));
+    int n = int(rs.box[d] / list_cut);
+    rs.ncell[d] = n < 1 ? 1 : n;
+  }
+  while ((long long)rs.ncell[0] * rs.ncell[1] * rs.ncell[2] > cap) {
+    int m = 0;
+    if (rs.ncell[1] > rs.ncell[m]) m = 1;
+    if (rs.ncell[2] > rs.ncell[m]) m = 2;
+    rs.ncell[m]--;
+  }
 }
 
 __device__ __forceinline__ float frac_delta(unsigned int a, unsigned int b, float scale) {
@@ -163,17 +193,20 @@ __device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
   return c;
 }
 
-// Uniform noise psi in (-1,1) for bead `orig` of replica `rep` at loop step
-// `it`; phase 1 is the start-up thermostat call before the loop.
+// Langevin noise sigma*psi with psi uniform in (-1,1) (the reference draws
+// 2u-1, include/algorithms/langevin.h:309-314) for bead `orig` of replica
+// `rep` at loop step `it`; phase 1 is the start-up thermostat call.  A draw r
+// gives psi = (signed(r - 2^31) + 1/2) 2^-31, so sigma*psi is one FMA with
+// sig31 = sigma 2^-31.
 __device__ __forceinline__ void langevin_noise(uint32_t seed, int rep, int orig, long long it, int phase,
-                                               double psi[3]) {
+                                               double sig31, double out[3]) {
   const uint4 c = make_uint4((unsigned)orig, (unsigned)(it & 0xffffffff),
                              (unsigned)((unsigned long long)it >> 32) ^ ((unsigned)phase << 31), (unsigned)rep);
   const uint4 r = philox4x32(c, make_uint2(seed, 0x5A17u));
-  const double s = 1.0 / 4294967296.0;
-  psi[0] = 2.0 * (((double)r.x + 0.5) * s) - 1.0;
-  psi[1] = 2.0 * (((double)r.y + 0.5) * s) - 1.0;
-  psi[2] = 2.0 * (((double)r.z + 0.5) * s) - 1.0;
+  const double half = 0.5 * sig31;
+  out[0] = fma((double)(int)(r.x ^ 0x80000000u), sig31, half);
+  out[1] = fma((double)(int)(r.y ^ 0x80000000u), sig31, half);
+  out[2] = fma((double)(int)(r.z ^ 0x80000000u), sig31, half);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -224,6 +257,16 @@ __device__ __forceinline__ R pair_mag(const R* c, R r) {
   R m = c[ci] - r;
   return ((c[ci + 1] - c[ci + 2] * m) * m) / r;
 }
+// The same force magnitude from r^2 without divisions: r and 1/r from one
+// reciprocal square root, and the table row chosen by r >= rm, which equals
+// int(r/rm) >= 1 for the positive values involved.
+__device__ __forceinline__ float pair_mag_rsqrt(const float* c, float r2) {
+  const float rinv = rsqrtf(r2), r = r2 * rinv;
+  const int ci = (r >= c[0]) ? 3 : 0;
+  const float m = c[ci] - r;
+  return ((c[ci + 1] - c[ci + 2] * m) * m) * rinv;
+}
+
 // Pair potential (include/MD.h:913-926).
 template <typename R>
 __device__ __forceinline__ R pair_pot(const R* c, R r) {

@@ -2,9 +2,10 @@
 //
 // One MD loop iteration (MD.cpp:335-729) in the steady state is
 //   [k_bin, k_scan_*, k_reorder, k_nbr]   only when the Verlet list is stale
-//   k_step<MIXED>                          forces + Langevin + both half-kicks + drift
+//   k_force<MIXED>                         non-bonded forces, G lanes per bead
+//   k_integ<MIXED>                         CHAIN + Langevin + both half-kicks + drift
 // and on barostat steps
-//   k_trial, k_step<STOP|DU>, k_mc, k_finish.
+//   k_trial, k_force<DU>, k_integ<STOP|DU>, k_mc, k_finish.
 #pragma once
 
 #include "smd_device.cuh"
@@ -22,14 +23,15 @@ enum StepFlags {
 };
 
 // ------------------------------------------------------------ last block
-// Runs once per launch after every block has passed its atomics: folds this
-// step's largest speed into the displacement bound and decides whether the
-// Verlet list must be rebuilt before the next force pass.
-__device__ __forceinline__ void finalize_step(const DevPtrs& P, float vmax_block, double dt, double half_skin,
-                                              double mc_shift) {
+// Runs once per launch after every block has passed its atomics.  The list
+// stays valid while every bead is within half the skin of its build position
+// (a pair now inside rc was then inside rc + skin); accepted box moves use up
+// (rc + skin)|s - 1| of that margin each.  Decides whether the Verlet list
+// must be rebuilt before the next force pass.
+__device__ __forceinline__ void finalize_step(const DevPtrs& P, float dmax_block) {
   __shared__ bool last;
   if (threadIdx.x == 0) {
-    if (vmax_block > 0.f) atomicMax(&P.g->vmax_bits, __float_as_uint(vmax_block));
+    if (dmax_block > 0.f) atomicMax(&P.g->dmax_bits, __float_as_uint(dmax_block));
     __threadfence();
     const unsigned int prev = atomicAdd(&P.g->blocks_done, 1u);
     last = (prev == gridDim.x - 1);
@@ -37,53 +39,51 @@ __device__ __forceinline__ void finalize_step(const DevPtrs& P, float vmax_block
   __syncthreads();
   if (last && threadIdx.x == 0) {
     __threadfence();
-    const float vmax = __uint_as_float(atomicExch(&P.g->vmax_bits, 0u));
+    const float dmax = __uint_as_float(atomicExch(&P.g->dmax_bits, 0u));
     const unsigned long long sb = atomicExch(&P.g->mc_shift, 0ull);
-    const double d = P.g->disp + (double)vmax * dt + __longlong_as_double((long long)sb);
-    P.g->disp = d;
-    P.g->rebuild = (d > half_skin) ? 1 : 0;
+    const double slack = P.g->slack + __longlong_as_double((long long)sb);
+    P.g->slack = slack;
+    P.g->last_disp = dmax;
+    P.g->rebuild = ((double)dmax + slack > P.half_skin) ? 1 : 0;
     P.g->blocks_done = 0u;
   }
-  (void)mc_shift;
+}
+
+// Displacement of bead i from its build position, from 32-bit fractional
+// coordinates (unchanged by box rescaling), in units of the current box.
+__device__ __forceinline__ float displacement(uint4 ref, unsigned int fx, unsigned int fy, unsigned int fz,
+                                              const RepState& rs) {
+  const float dx = frac_delta(fx, ref.x, rs.len_per_frac[0]);
+  const float dy = frac_delta(fy, ref.y, rs.len_per_frac[1]);
+  const float dz = frac_delta(fz, ref.z, rs.len_per_frac[2]);
+  return sqrtf(dx * dx + dy * dy + dz * dz);
 }
 
 // ------------------------------------------------------------ list build
-__device__ __forceinline__ void list_grid(const DevPtrs& P, int r, int n[3], double cs[3]) {
-  const RepState& rs = P.rs[r];
-  const double lc = P.tab->list_cut;
-  for (int d = 0; d < 3; ++d) {
-    n[d] = int(rs.box[d] / lc);
-    n[d] = n[d] < 1 ? 1 : n[d];
-  }
-  const int cap = P.rp[r].cell_cap;
-  while ((long long)n[0] * n[1] * n[2] > cap) {
-    int m = 0;
-    if (n[1] > n[m]) m = 1;
-    if (n[2] > n[m]) m = 2;
-    n[m]--;
-  }
-  for (int d = 0; d < 3; ++d) cs[d] = rs.box[d] / n[d];
-}
-
-__global__ void __launch_bounds__(kBlock) k_bin(DevPtrs P) {
+// Verlet-list cell of bead i from its 32-bit fractional coordinates: the
+// cell index along an axis is floor(f * n / 2^32), always in [0, n).
+__global__ void __launch_bounds__(kBlock) k_bin(DevPtrs P, int cur, int mixed) {
   if (!P.g->rebuild) return;
   const int i = blockIdx.x * kBlock + threadIdx.x;
   if (i >= P.n) return;
   const int r = rep_of(P, i);
-  int n[3];
-  double cs[3];
-  list_grid(P, r, n, cs);
-  const int cx = list_cell_coord(P.x[i], cs[0], n[0]);
-  const int cy = list_cell_coord(P.y[i], cs[1], n[1]);
-  const int cz = list_cell_coord(P.z[i], cs[2], n[2]);
-  const int key = P.rp[r].cell_begin + cx + n[0] * (cy + n[1] * cz);
+  const RepState& rs = P.rs[r];
+  unsigned int f[3];
+  if (mixed) {
+    const uint4 m = P.m4[cur][i];
+    f[0] = m.x;
+    f[1] = m.y;
+    f[2] = m.z;
+  } else {
+    f[0] = to_frac(P.x[i], rs.frac_per_len[0]);
+    f[1] = to_frac(P.y[i], rs.frac_per_len[1]);
+    f[2] = to_frac(P.z[i], rs.frac_per_len[2]);
+  }
+  const int n0 = rs.ncell[0], n1 = rs.ncell[1], n2 = rs.ncell[2];
+  const int cx = __umulhi(f[0], (unsigned)n0), cy = __umulhi(f[1], (unsigned)n1), cz = __umulhi(f[2], (unsigned)n2);
+  const int key = P.rp[r].cell_begin + cx + n0 * (cy + n1 * cz);
   P.key[i] = key;
   P.slot[i] = atomicAdd(&P.cell_count[key], 1);
-  if (i == P.rp[r].bead_begin) {
-    P.rs[r].ncell[0] = n[0];
-    P.rs[r].ncell[1] = n[1];
-    P.rs[r].ncell[2] = n[2];
-  }
 }
 
 // Exclusive scan of cell_count into cell_start in three passes: tile sums,
@@ -183,103 +183,363 @@ __global__ void __launch_bounds__(kBlock) k_reorder(DevPtrs P, int cur) {
   const int o = P.orig[i];
   P.torig[nw] = o;
   P.tcinfo[nw] = P.cinfo[i];
+  P.tkey[nw] = P.key[i];
   P.inv[o] = nw;
-  const int r = rep_of(P, i);
   if constexpr (MIXED) {
-    const RepState& rs = P.rs[r];
-    const uint4 old = P.m4[cur][i];
-    P.mt[nw] = make_uint4(to_frac(x, 1.0 / rs.box[0]), to_frac(y, 1.0 / rs.box[1]), to_frac(z, 1.0 / rs.box[2]),
-                          old.w);
+    P.mt[nw] = P.m4[cur][i];
   } else {
-    const double4 old = P.d4[cur][i];
-    P.dt4[nw] = make_double4(x, y, z, old.w);
+    P.dt4[nw] = P.d4[cur][i];
+  }
+}
+
+// Lanes of group g of size G within the warp.
+template <int G>
+__device__ __forceinline__ unsigned int group_mask() {
+  if constexpr (G == 32) {
+    return 0xffffffffu;
+  } else {
+    const unsigned int lane = threadIdx.x & 31;
+    return ((1u << G) - 1u) << (lane & ~(unsigned)(G - 1));
   }
 }
 
 // Copies the reordered state back and builds the Verlet list of bead i from
 // the 27 (or fewer, for thin boxes) surrounding cells, reading the reordered
-// mirror that k_reorder left in the scratch buffer.
-template <bool MIXED>
+// mirror that k_reorder left in the scratch buffer.  G lanes share one bead:
+// each tests every G-th candidate of a cell and the group appends its hits
+// with a ballot, so list entries of one bead are contiguous (bead-major).
+template <bool MIXED, int G>
 __global__ void __launch_bounds__(kBlock) k_nbr(DevPtrs P, int cur) {
   if (!P.g->rebuild) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    P.g->disp = 0.0;
+  const int t = blockIdx.x * kBlock + threadIdx.x;
+  const int i = t / G, sub = t % G;
+  if (t == 0) {
+    P.g->slack = 0.0;
     P.g->n_rebuilds++;
   }
-  if (i >= P.n) return;
-  P.x[i] = P.tx[i];
-  P.y[i] = P.ty[i];
-  P.z[i] = P.tz[i];
-  P.vx[i] = P.tvx[i];
-  P.vy[i] = P.tvy[i];
-  P.vz[i] = P.tvz[i];
-  P.ax[i] = P.tax[i];
-  P.ay[i] = P.tay[i];
-  P.az[i] = P.taz[i];
-  P.orig[i] = P.torig[i];
-  P.cinfo[i] = P.tcinfo[i];
-  if constexpr (MIXED) P.m4[cur][i] = P.mt[i]; else P.d4[cur][i] = P.dt4[i];
+  if (i >= P.n) return;  // whole groups leave together (n*G threads are grouped)
   const int r = rep_of(P, i);
   const RepState& rs = P.rs[r];
+  if (sub == 0) {
+    P.x[i] = P.tx[i];
+    P.y[i] = P.ty[i];
+    P.z[i] = P.tz[i];
+    P.vx[i] = P.tvx[i];
+    P.vy[i] = P.tvy[i];
+    P.vz[i] = P.tvz[i];
+    P.ax[i] = P.tax[i];
+    P.ay[i] = P.tay[i];
+    P.az[i] = P.taz[i];
+    P.orig[i] = P.torig[i];
+    P.cinfo[i] = P.tcinfo[i];
+    if constexpr (MIXED) {
+      P.m4[cur][i] = P.mt[i];
+      P.ref[i] = P.mt[i];
+    } else {
+      const double4 d = P.dt4[i];
+      P.d4[cur][i] = d;
+      P.ref[i] = make_uint4(to_frac(d.x, rs.frac_per_len[0]), to_frac(d.y, rs.frac_per_len[1]),
+                            to_frac(d.z, rs.frac_per_len[2]), 0u);
+    }
+  }
   const int n0 = rs.ncell[0], n1 = rs.ncell[1], n2 = rs.ncell[2];
   const int cb = P.rp[r].cell_begin;
-  double cs[3] = {rs.box[0] / n0, rs.box[1] / n1, rs.box[2] / n2};
-  const double xi = P.tx[i], yi = P.ty[i], zi = P.tz[i];
-  const int cx = list_cell_coord(xi, cs[0], n0), cy = list_cell_coord(yi, cs[1], n1),
-            cz = list_cell_coord(zi, cs[2], n2);
-  const double lc2 = P.tab->list_cut2;
-  int cnt = 0;
-  const int kmax = P.kmax;
-  int* out = P.nbr + i;
-  const int lo0 = n0 >= 3 ? -1 : 0, hi0 = n0 >= 2 ? 1 : 0;
+  const int local = P.tkey[i] - cb;
+  const int cx = local % n0, cy = (local / n0) % n1, cz = local / (n0 * n1);
+  // The stencil as contiguous bead ranges: cells are ordered x-fastest, so
+  // each (dy,dz) row of 3 cells is one range unless it wraps in x.
+  int seg_s[18], seg_e[18];
+  int nseg = 0;
   const int lo1 = n1 >= 3 ? -1 : 0, hi1 = n1 >= 2 ? 1 : 0;
   const int lo2 = n2 >= 3 ? -1 : 0, hi2 = n2 >= 2 ? 1 : 0;
-  uint4 mi;
-  double4 di;
-  double sc[3];
-  if constexpr (MIXED) {
-    mi = P.mt[i];
-    for (int d = 0; d < 3; ++d) sc[d] = rs.box[d] * (1.0 / 4294967296.0);
-  } else {
-    di = P.dt4[i];
+  int xa = cx - 1, xb = cx + 1;  // x run [xa, xb] before wrapping
+  if (n0 < 3) {
+    xa = 0;
+    xb = n0 - 1;
   }
   for (int oz = lo2; oz <= hi2; ++oz) {
     const int zz = (cz + oz + n2) % n2;
     for (int oy = lo1; oy <= hi1; ++oy) {
       const int yy = (cy + oy + n1) % n1;
-      for (int ox = lo0; ox <= hi0; ++ox) {
-        const int xx = (cx + ox + n0) % n0;
-        const int c = cb + xx + n0 * (yy + n1 * zz);
-        const int s = P.cell_start[c], e = P.cell_start[c + 1];
-        for (int j = s; j < e; ++j) {
-          if (j == i) continue;
-          double d2;
-          if constexpr (MIXED) {
-            const uint4 mj = P.mt[j];
-            const double dx = frac_delta_d(mi.x, mj.x, sc[0]), dy = frac_delta_d(mi.y, mj.y, sc[1]),
-                         dz = frac_delta_d(mi.z, mj.z, sc[2]);
-            d2 = dx * dx + dy * dy + dz * dz;
-          } else {
-            const double4 dj = P.dt4[j];
-            double dx = di.x - dj.x, dy = di.y - dj.y, dz = di.z - dj.z;
-            dx -= rs.box[0] * rint(dx / rs.box[0]);
-            dy -= rs.box[1] * rint(dy / rs.box[1]);
-            dz -= rs.box[2] * rint(dz / rs.box[2]);
-            d2 = dx * dx + dy * dy + dz * dz;
-          }
-          if (d2 < lc2) {
-            if (cnt < kmax) out[(size_t)cnt * P.npad] = j;
-            ++cnt;
-          }
-        }
+      const int row = cb + n0 * (yy + n1 * zz);
+      if (xa >= 0 && xb < n0) {
+        seg_s[nseg] = P.cell_start[row + xa];
+        seg_e[nseg++] = P.cell_start[row + xb + 1];
+      } else if (xa < 0) {  // cells n0-1 | 0..xb
+        seg_s[nseg] = P.cell_start[row + n0 - 1];
+        seg_e[nseg++] = P.cell_start[row + n0];
+        seg_s[nseg] = P.cell_start[row];
+        seg_e[nseg++] = P.cell_start[row + xb + 1];
+      } else {  // cells xa..n0-1 | 0
+        seg_s[nseg] = P.cell_start[row + xa];
+        seg_e[nseg++] = P.cell_start[row + n0];
+        seg_s[nseg] = P.cell_start[row];
+        seg_e[nseg++] = P.cell_start[row + 1];
       }
     }
   }
-  P.nnbr[i] = cnt < kmax ? cnt : kmax;
-  if (cnt > kmax) {
-    atomicOr(&P.g->error, 1);
-    atomicMax(&P.g->need_nbr, cnt);
+  const unsigned int gm = group_mask<G>();
+  const unsigned int below = (1u << (threadIdx.x & 31)) - 1u;
+  int cnt = 0;
+  const int kmax = P.kmax;
+  int* out = P.nbr + (size_t)i * kmax;
+  uint4 mi;
+  double4 di;
+  float sc[3];
+  const float lc2f = (float)P.tab->list_cut2;
+  if constexpr (MIXED) {
+    mi = P.mt[i];
+    for (int d = 0; d < 3; ++d) sc[d] = rs.len_per_frac[d];
+  } else {
+    di = P.dt4[i];
+  }
+  auto test = [&](int j, int e) -> bool {
+    if (j >= e || j == i) return false;
+    if constexpr (MIXED) {
+      const uint4 mj = P.mt[j];
+      const float dx = frac_delta(mi.x, mj.x, sc[0]), dy = frac_delta(mi.y, mj.y, sc[1]),
+                  dz = frac_delta(mi.z, mj.z, sc[2]);
+      return dx * dx + dy * dy + dz * dz < lc2f;
+    } else {
+      const double4 dj = P.dt4[j];
+      double dx = di.x - dj.x, dy = di.y - dj.y, dz = di.z - dj.z;
+      dx -= rs.box[0] * rint(dx / rs.box[0]);
+      dy -= rs.box[1] * rint(dy / rs.box[1]);
+      dz -= rs.box[2] * rint(dz / rs.box[2]);
+      return dx * dx + dy * dy + dz * dz < P.tab->list_cut2;
+    }
+  };
+  auto append = [&](bool hit, int j) {
+    const unsigned int hits = __ballot_sync(gm, hit) & gm;
+    if (hit) {
+      const int slot = cnt + __popc(hits & below);
+      if (slot < kmax) out[slot] = j;
+    }
+    cnt += __popc(hits);
+  };
+  for (int q = 0; q < nseg; ++q) {
+    const int s = seg_s[q], e = seg_e[q];
+    int j0 = s;
+    for (; j0 + G < e; j0 += 2 * G) {  // two candidate loads in flight per lane
+      const int ja = j0 + sub, jb = j0 + G + sub;
+      const bool ha = test(ja, e), hb = test(jb, e);
+      append(ha, ja);
+      append(hb, jb);
+    }
+    for (; j0 < e; j0 += G) {
+      const int ja = j0 + sub;
+      append(test(ja, e), ja);
+    }
+  }
+  if (sub == 0) {
+    P.nnbr[i] = cnt < kmax ? cnt : kmax;
+    if (cnt > kmax) {
+      atomicOr(&P.g->error, 1);
+      atomicMax(&P.g->need_nbr, cnt);
+    }
+  }
+}
+
+// Cell-centred Verlet-list build: one CTA per cell of the list grid.  The CTA
+// stages the stencil's beads (9 contiguous x-rows of the cell-sorted order, in
+// chunks of kNbrChunk) in shared memory; each warp then takes one bead of the
+// cell at a time, tests 32 staged candidates per round and appends the hits
+// with a ballot, so each bead's list is written contiguously.  The CTA also
+// copies its beads' reordered state back and records their build positions.
+constexpr int kNbrThreads = 128;
+constexpr int kNbrChunk = 1536;
+constexpr int kNbrMaxCell = 1024;
+
+template <bool MIXED, int kChunk>
+__device__ __forceinline__ void nbr_cell(const DevPtrs& P, int cur, int c);
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kNbrThreads) k_nbr_cells(DevPtrs P, int cur) {
+  constexpr int kChunk = MIXED ? kNbrChunk : kNbrChunk / 2;  // 24 KB of staged positions either way
+  if (!P.g->rebuild) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.g->slack = 0.0;
+    P.g->n_rebuilds++;
+  }
+  for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) {
+    nbr_cell<MIXED, kChunk>(P, cur, c);
+  }
+}
+
+// The work of k_nbr_cells for one cell c (block-uniform control flow).
+template <bool MIXED, int kChunk>
+__device__ __forceinline__ void nbr_cell(const DevPtrs& P, int cur, int c) {
+  const int s = P.cell_start[c], e = P.cell_start[c + 1];
+  if (s >= e) return;
+  // replica owning the cell
+  int lo = 0, hi = P.n_rep - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (P.rp[mid].cell_begin <= c) lo = mid; else hi = mid - 1;
+  }
+  const int r = lo;
+  const RepState& rs = P.rs[r];
+  const int cb = P.rp[r].cell_begin;
+  const int n0 = rs.ncell[0], n1 = rs.ncell[1], n2 = rs.ncell[2];
+  const int local = c - cb;
+  const int cx = local % n0, cy = (local / n0) % n1, cz = local / (n0 * n1);
+  // copy back this cell's reordered state
+  for (int i = s + threadIdx.x; i < e; i += kNbrThreads) {
+    P.x[i] = P.tx[i];
+    P.y[i] = P.ty[i];
+    P.z[i] = P.tz[i];
+    P.vx[i] = P.tvx[i];
+    P.vy[i] = P.tvy[i];
+    P.vz[i] = P.tvz[i];
+    P.ax[i] = P.tax[i];
+    P.ay[i] = P.tay[i];
+    P.az[i] = P.taz[i];
+    P.orig[i] = P.torig[i];
+    P.cinfo[i] = P.tcinfo[i];
+    if constexpr (MIXED) {
+      P.m4[cur][i] = P.mt[i];
+      P.ref[i] = P.mt[i];
+    } else {
+      const double4 d = P.dt4[i];
+      P.d4[cur][i] = d;
+      P.ref[i] = make_uint4(to_frac(d.x, rs.frac_per_len[0]), to_frac(d.y, rs.frac_per_len[1]),
+                            to_frac(d.z, rs.frac_per_len[2]), 0u);
+    }
+  }
+  // stencil segments (contiguous bead ranges) and their prefix sums
+  __shared__ int seg_s[18], seg_p[19];
+  __shared__ int nseg_sh;
+  __syncthreads();  // the previous cell of this CTA is done with the shared arrays
+  if (threadIdx.x == 0) {
+    int nseg = 0;
+    const int lo1 = n1 >= 3 ? -1 : 0, hi1 = n1 >= 2 ? 1 : 0;
+    const int lo2 = n2 >= 3 ? -1 : 0, hi2 = n2 >= 2 ? 1 : 0;
+    int xa = cx - 1, xb = cx + 1;
+    if (n0 < 3) {
+      xa = 0;
+      xb = n0 - 1;
+    }
+    int acc = 0;
+    for (int oz = lo2; oz <= hi2; ++oz) {
+      const int zz = (cz + oz + n2) % n2;
+      for (int oy = lo1; oy <= hi1; ++oy) {
+        const int yy = (cy + oy + n1) % n1;
+        const int row = cb + n0 * (yy + n1 * zz);
+        int a0, a1, b0 = 0, b1 = 0;
+        if (xa >= 0 && xb < n0) {
+          a0 = row + xa;
+          a1 = row + xb + 1;
+        } else if (xa < 0) {
+          a0 = row + n0 - 1;
+          a1 = row + n0;
+          b0 = row;
+          b1 = row + xb + 1;
+        } else {
+          a0 = row + xa;
+          a1 = row + n0;
+          b0 = row;
+          b1 = row + 1;
+        }
+        seg_s[nseg] = P.cell_start[a0];
+        seg_p[nseg] = acc;
+        acc += P.cell_start[a1] - seg_s[nseg];
+        ++nseg;
+        if (b1 > b0) {
+          seg_s[nseg] = P.cell_start[b0];
+          seg_p[nseg] = acc;
+          acc += P.cell_start[b1] - seg_s[nseg];
+          ++nseg;
+        }
+      }
+    }
+    seg_p[nseg] = acc;
+    nseg_sh = nseg;
+  }
+  __syncthreads();
+  const int nseg = nseg_sh;
+  const int M = seg_p[nseg];
+  const int nb = e - s;
+  if (nb > kNbrMaxCell) {
+    if (threadIdx.x == 0) atomicOr(&P.g->error, 2);
+    return;
+  }
+  __shared__ int cnt[kNbrMaxCell];
+  __shared__ int cidx[kChunk];
+  __shared__ uint4 cpos4[MIXED ? kChunk : 1];
+  __shared__ double4 cposd[MIXED ? 1 : kChunk];
+  for (int k = threadIdx.x; k < nb; k += kNbrThreads) cnt[k] = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned int below = (1u << lane) - 1u;
+  const int kmax = P.kmax;
+  float sc[3] = {rs.len_per_frac[0], rs.len_per_frac[1], rs.len_per_frac[2]};
+  const float lc2f = (float)P.tab->list_cut2;
+  const double lc2 = P.tab->list_cut2;
+  for (int base = 0; base < M; base += kChunk) {
+    const int m = min(kChunk, M - base);
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += kNbrThreads) {
+      const int g = base + k;
+      int q = 0;
+      while (q + 1 < nseg && seg_p[q + 1] <= g) ++q;
+      const int j = seg_s[q] + (g - seg_p[q]);
+      cidx[k] = j;
+      if constexpr (MIXED) cpos4[k] = P.mt[j]; else cposd[k] = P.dt4[j];
+    }
+    __syncthreads();
+    for (int b = warp; b < nb; b += kNbrThreads / 32) {
+      const int i = s + b;
+      int count = cnt[b];
+      int* out = P.nbr + (size_t)i * kmax;
+      if constexpr (MIXED) {
+        const uint4 mi = P.mt[i];
+        for (int k0 = 0; k0 < m; k0 += 32) {
+          const int k = k0 + lane;
+          bool hit = false;
+          if (k < m) {
+            const uint4 mj = cpos4[k];
+            const float dx = frac_delta(mi.x, mj.x, sc[0]), dy = frac_delta(mi.y, mj.y, sc[1]),
+                        dz = frac_delta(mi.z, mj.z, sc[2]);
+            hit = (dx * dx + dy * dy + dz * dz < lc2f) && (cidx[k] != i);
+          }
+          const unsigned int hits = __ballot_sync(0xffffffffu, hit);
+          if (hit) {
+            const int slot = count + __popc(hits & below);
+            if (slot < kmax) out[slot] = cidx[k];
+          }
+          count += __popc(hits);
+        }
+      } else {
+        const double4 di = P.dt4[i];
+        for (int k0 = 0; k0 < m; k0 += 32) {
+          const int k = k0 + lane;
+          bool hit = false;
+          if (k < m) {
+            const double4 dj = cposd[k];
+            double dx = di.x - dj.x, dy = di.y - dj.y, dz = di.z - dj.z;
+            dx -= rs.box[0] * rint(dx * (1.0 / 4294967296.0) * rs.frac_per_len[0]);
+            dy -= rs.box[1] * rint(dy * (1.0 / 4294967296.0) * rs.frac_per_len[1]);
+            dz -= rs.box[2] * rint(dz * (1.0 / 4294967296.0) * rs.frac_per_len[2]);
+            hit = (dx * dx + dy * dy + dz * dz < lc2) && (cidx[k] != i);
+          }
+          const unsigned int hits = __ballot_sync(0xffffffffu, hit);
+          if (hit) {
+            const int slot = count + __popc(hits & below);
+            if (slot < kmax) out[slot] = cidx[k];
+          }
+          count += __popc(hits);
+        }
+      }
+      if (lane == 0) cnt[b] = count;
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += kNbrThreads) {
+    const int count = cnt[b];
+    P.nnbr[s + b] = count < kmax ? count : kmax;
+    if (count > kmax) {
+      atomicOr(&P.g->error, 1);
+      atomicMax(&P.g->need_nbr, count);
+    }
   }
 }
 
@@ -348,10 +608,11 @@ __device__ __forceinline__ double bend_pot(Vec3<double> da, Vec3<double> db, con
 }
 
 // Difference vectors e[k] = x(p-2+k) - x(p-1+k), k = 0..3, of the chain
-// around bead i, as real-space vectors of type R; valid[k] marks existing ones.
-template <bool MIXED, typename R>
+// around bead i; valid[k] marks existing ones.  MIXED: exact from the 32-bit
+// fractional mirror (in FP64); PLAIN: FP64 with the bonded minimum image.
+template <bool MIXED, typename RT>
 __device__ __forceinline__ void chain_vectors(const DevPtrs& P, int cur, int i, int p, int len, const double box[3],
-                                              Vec3<R> e[4], bool valid[4]) {
+                                              Vec3<RT> e[4], bool valid[4]) {
   const int o = P.orig[i];
   int idx[5];
   bool have[5];
@@ -365,14 +626,23 @@ __device__ __forceinline__ void chain_vectors(const DevPtrs& P, int cur, int i, 
     uint4 m[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) m[k] = P.m4[cur][idx[k]];
-    const double s0 = box[0] * (1.0 / 4294967296.0), s1 = box[1] * (1.0 / 4294967296.0),
-                 s2 = box[2] * (1.0 / 4294967296.0);
+    RT s0, s1, s2;
+    if constexpr (std::is_same<RT, float>::value) {
+      const RepState& rs = P.rs[rep_of(P, i)];
+      s0 = rs.len_per_frac[0];
+      s1 = rs.len_per_frac[1];
+      s2 = rs.len_per_frac[2];
+    } else {
+      s0 = box[0] * (1.0 / 4294967296.0);
+      s1 = box[1] * (1.0 / 4294967296.0);
+      s2 = box[2] * (1.0 / 4294967296.0);
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       valid[k] = have[k] && have[k + 1];
-      e[k].x = (R)frac_delta_d(m[k].x, m[k + 1].x, s0);
-      e[k].y = (R)frac_delta_d(m[k].y, m[k + 1].y, s1);
-      e[k].z = (R)frac_delta_d(m[k].z, m[k + 1].z, s2);
+      e[k].x = (RT)(int)(m[k].x - m[k + 1].x) * s0;
+      e[k].y = (RT)(int)(m[k].y - m[k + 1].y) * s1;
+      e[k].z = (RT)(int)(m[k].z - m[k + 1].z) * s2;
     }
   } else {
     double4 m[5];
@@ -386,9 +656,9 @@ __device__ __forceinline__ void chain_vectors(const DevPtrs& P, int cur, int i, 
         if (d[a] > box[a] / 2.0) d[a] -= box[a];
         if (d[a] < -box[a] / 2.0) d[a] += box[a];
       }
-      e[k].x = (R)d[0];
-      e[k].y = (R)d[1];
-      e[k].z = (R)d[2];
+      e[k].x = (RT)d[0];
+      e[k].y = (RT)d[1];
+      e[k].z = (RT)d[2];
     }
   }
 }
@@ -403,9 +673,15 @@ __device__ __forceinline__ void warp_atomic_add(double v, double* dst, int r) {
   if (lane == __ffs(peers) - 1 && acc != 0.0) atomicAdd(dst, acc);
 }
 
-// The fused step.  One thread per bead (sorted order).
-template <bool MIXED, int FL>
-__global__ void __launch_bounds__(kBlock) k_step(DevPtrs P, int cur, long long it) {
+// Non-bonded pass: G lanes per bead walk the bead's Verlet-list entries
+// (bead-major, so a group reads G consecutive indices per round) and reduce
+// with shuffles.  MIXED: FP32 pair arithmetic, each pair force rounded to a
+// 32-bit fixed-point value and summed in int64, so the result does not depend
+// on the order of the pairs; PLAIN: FP64 with the reference's neighbour-shift
+// minimum image.  Writes the per-bead pair force (fixed point or FP64) and,
+// with F_DU / F_ENERGY, the replica's pair U(x)-U(s x) / pair energy.
+template <bool MIXED, int FL, int G>
+__global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
   using R = typename std::conditional<MIXED, float, double>::type;
   __shared__ R sF[6 * kMaxTypes * kMaxTypes];
   __shared__ R sU[6 * kMaxTypes * kMaxTypes];
@@ -421,74 +697,98 @@ __global__ void __launch_bounds__(kBlock) k_step(DevPtrs P, int cur, long long i
     }
   }
   __syncthreads();
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int t = blockIdx.x * kBlock + threadIdx.x;
+  const int i = t / G, sub = t % G;
   const bool active = i < P.n;
   const int r = active ? rep_of(P, i) : 0;
-  double dU_pair = 0.0, dU_bond = 0.0, e_pair = 0.0, e_bond = 0.0, e_kin = 0.0;
-  float vmax = 0.f;
+  double dU = 0.0, ep = 0.0;
+  long long qx = 0, qy = 0, qz = 0;
+  double fx = 0, fy = 0, fz = 0;
   if (active) {
-    const RepParams& rp = P.rp[r];
-    RepState& rs = P.rs[r];
-    const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
-    // ---- non-bonded, from the Verlet list
-    long long qx = 0, qy = 0, qz = 0;  // MIXED: fixed point
-    double fxd = 0, fyd = 0, fzd = 0;  // PLAIN
-    int ti;
-    R sq[3];  // (s_d^2 - 1) for the size-change difference
-    if constexpr ((FL & F_DU) != 0) {
-      for (int d = 0; d < 3; ++d) sq[d] = (R)(rs.scale[d] * rs.scale[d] - 1.0);
-    }
+    const RepState& rs = P.rs[r];
     const int nn = P.nnbr[i];
-    const int* nb = P.nbr + i;
+    const int* nb = P.nbr + (size_t)i * P.kmax;
     if constexpr (MIXED) {
       const uint4 me = P.m4[cur][i];
-      ti = me.w & 0xff;
-      const float s0 = (float)(box[0] * (1.0 / 4294967296.0)), s1 = (float)(box[1] * (1.0 / 4294967296.0)),
-                  s2 = (float)(box[2] * (1.0 / 4294967296.0));
+      const int ti = me.w & 0xff;
+      const float s0 = rs.len_per_frac[0], s1 = rs.len_per_frac[1], s2 = rs.len_per_frac[2];
+      float sq0 = 0.f, sq1 = 0.f, sq2 = 0.f;
+      if constexpr ((FL & F_DU) != 0) {
+        sq0 = (float)(rs.scale[0] * rs.scale[0] - 1.0);
+        sq1 = (float)(rs.scale[1] * rs.scale[1] - 1.0);
+        sq2 = (float)(rs.scale[2] * rs.scale[2] - 1.0);
+      }
       const float* rowF = sF + 6 * ti * nT;
       const float* rowU = sU + 6 * ti * nT;
       const float rc2 = T.rc2f, fs = T.fscale;
-      float eacc = 0.f;
-      for (int k = 0; k < nn; ++k) {
-        const int j = __ldg(nb + (size_t)k * P.npad);
+      float eacc = 0.f, dacc = 0.f;
+      int k = sub;
+      // two independent gathers in flight per lane
+      for (; k + G < nn; k += 2 * G) {
+        const int j0 = __ldg(nb + k), j1 = __ldg(nb + k + G);
+        const uint4 o0 = P.m4[cur][j0], o1 = P.m4[cur][j1];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const uint4 o = u ? o1 : o0;
+          const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          if constexpr ((FL & F_DU) != 0) {
+            const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
+            const float rn2 = r2 + q;
+            if (r2 < rc2 || rn2 < rc2) {
+              const float rr = sqrtf(r2), rn = sqrtf(rn2);
+              dacc += pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, q / (rn + rr), T.rcf);
+            }
+          }
+          if (r2 < rc2) {
+            const int tj = o.w & 0xff;
+            if constexpr ((FL & F_ENERGY) == 0) {
+              const float mag = pair_mag_rsqrt(rowF + 6 * tj, r2) * fs;
+              qx += (long long)__float2int_rn(dx * mag);
+              qy += (long long)__float2int_rn(dy * mag);
+              qz += (long long)__float2int_rn(dz * mag);
+            } else {
+              eacc += pair_pot<float>(rowU + 6 * tj, sqrtf(r2));
+            }
+          }
+        }
+      }
+      for (; k < nn; k += G) {
+        const int j = __ldg(nb + k);
         const uint4 o = P.m4[cur][j];
         const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
         const float r2 = dx * dx + dy * dy + dz * dz;
+        if constexpr ((FL & F_DU) != 0) {
+          const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
+          const float rn2 = r2 + q;
+          if (r2 < rc2 || rn2 < rc2) {
+            const float rr = sqrtf(r2), rn = sqrtf(rn2);
+            dacc += pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, q / (rn + rr), T.rcf);
+          }
+        }
         if (r2 < rc2) {
           const int tj = o.w & 0xff;
-          const float rr = sqrtf(r2);
           if constexpr ((FL & F_ENERGY) == 0) {
-            const float mag = pair_mag<float>(rowF + 6 * tj, rr) * fs;
+            const float mag = pair_mag_rsqrt(rowF + 6 * tj, r2) * fs;
             qx += (long long)__float2int_rn(dx * mag);
             qy += (long long)__float2int_rn(dy * mag);
             qz += (long long)__float2int_rn(dz * mag);
           } else {
-            eacc += pair_pot<float>(rowU + 6 * tj, rr);
-          }
-          if constexpr ((FL & F_DU) != 0) {
-            const float q = sq[0] * dx * dx + sq[1] * dy * dy + sq[2] * dz * dz;
-            const float rn = sqrtf(r2 + q);
-            dU_pair += 0.5 * (double)pair_dpot_f(rowU + 6 * tj, rr, rn, q / (rn + rr), T.rcf);
-          }
-        } else if constexpr ((FL & F_DU) != 0) {
-          // pairs just outside rc can move inside under the trial scale
-          const float q = sq[0] * dx * dx + sq[1] * dy * dy + sq[2] * dz * dz;
-          const float rn2 = r2 + q;
-          if (rn2 < rc2) {
-            const int tj = o.w & 0xff;
-            dU_pair -= 0.5 * (double)pair_pot<float>(rowU + 6 * tj, sqrtf(rn2));
+            eacc += pair_pot<float>(rowU + 6 * tj, sqrtf(r2));
           }
         }
       }
-      e_pair = 0.5 * (double)eacc;
+      ep = 0.5 * (double)eacc;
+      dU = 0.5 * (double)dacc;
     } else {
       const double4 me = P.d4[cur][i];
-      ti = __double_as_longlong(me.w) & 0xff;
+      const int ti = __double_as_longlong(me.w) & 0xff;
       const double* rowF = sF + 6 * ti * nT;
       const double* rowU = sU + 6 * ti * nT;
       const double rc2 = T.rc2;
-      for (int k = 0; k < nn; ++k) {
-        const int j = __ldg(nb + (size_t)k * P.npad);
+      const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
+      for (int k = sub; k < nn; k += G) {
+        const int j = __ldg(nb + k);
         const double4 o = P.d4[cur][j];
         // minimum image applied to the neighbour first, as CellOpt shifts the
         // neighbour cell's positions (cellOpt.h:810-840)
@@ -506,11 +806,11 @@ __global__ void __launch_bounds__(kBlock) k_step(DevPtrs P, int cur, long long i
           const double rr = sqrt(r2);
           if constexpr ((FL & F_ENERGY) == 0) {
             const double mag = pair_mag<double>(rowF + 6 * tj, rr);
-            fxd += dx * mag;
-            fyd += dy * mag;
-            fzd += dz * mag;
+            fx += dx * mag;
+            fy += dy * mag;
+            fz += dz * mag;
           } else {
-            e_pair += 0.5 * pair_pot<double>(rowU + 6 * tj, rr);
+            ep += 0.5 * pair_pot<double>(rowU + 6 * tj, rr);
           }
         }
         if constexpr ((FL & F_DU) != 0) {
@@ -518,135 +818,191 @@ __global__ void __launch_bounds__(kBlock) k_step(DevPtrs P, int cur, long long i
           const double rn2 = nx * nx + ny * ny + nz * nz;
           const double u0 = r2 < rc2 ? pair_pot<double>(rowU + 6 * tj, sqrt(r2)) : 0.0;
           const double u1 = rn2 < rc2 ? pair_pot<double>(rowU + 6 * tj, sqrt(rn2)) : 0.0;
-          dU_pair += 0.5 * (u0 - u1);
+          dU += 0.5 * (u0 - u1);
         }
       }
     }
-    // ---- CHAIN terms
+  }
+  // group reduction (integer sums are exact in any order)
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    if constexpr (MIXED) {
+      qx += __shfl_xor_sync(0xffffffffu, qx, o);
+      qy += __shfl_xor_sync(0xffffffffu, qy, o);
+      qz += __shfl_xor_sync(0xffffffffu, qz, o);
+    } else {
+      fx += __shfl_xor_sync(0xffffffffu, fx, o);
+      fy += __shfl_xor_sync(0xffffffffu, fy, o);
+      fz += __shfl_xor_sync(0xffffffffu, fz, o);
+    }
+  }
+  if (active && sub == 0 && (FL & F_ENERGY) == 0) {
+    if constexpr (MIXED) {
+      P.fq[i] = qx;
+      P.fq[i + P.n] = qy;
+      P.fq[i + 2 * P.n] = qz;
+    } else {
+      P.fp[i] = fx;
+      P.fp[i + P.n] = fy;
+      P.fp[i + 2 * P.n] = fz;
+    }
+  }
+  if constexpr ((FL & F_DU) != 0) warp_atomic_add(dU, &P.rs[r].dU_pair, r);
+  if constexpr ((FL & F_ENERGY) != 0) warp_atomic_add(ep, &P.rs[r].e_pair, r);
+}
+
+// Per-bead pass after k_force: CHAIN terms, the total force, the Langevin
+// term (include/algorithms/langevin.h:284-331) and the velocity-Verlet
+// updates (include/algorithms/verlet.h:288-355, 463-491): second half-kick of
+// this step, first half-kick and drift of the next, periodic wrap, and the
+// position mirror for the next force pass.  Flags select the stopped,
+// start-up, force-only and energy-only variants.
+template <bool MIXED, int FL>
+__global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, long long it) {
+  const Tables& T = *P.tab;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const bool active = i < P.n;
+  const int r = active ? rep_of(P, i) : 0;
+  double dU_bond = 0.0, e_bond = 0.0, e_kin = 0.0;
+  float vmax = 0.f;
+  if (active) {
+    const RepParams& rp = P.rp[r];
+    const RepState& rs = P.rs[r];
+    const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
+    int ti;
+    if constexpr (MIXED) ti = P.m4[cur][i].w & 0xff; else ti = __double_as_longlong(P.d4[cur][i].w) & 0xff;
+    // ---- CHAIN terms (FP32 in the mixed form, from exact FP64 differences)
+    using R = typename std::conditional<MIXED, float, double>::type;
     Vec3<R> fb{0, 0, 0};
     const int ci = P.cinfo[i];
     if ((FL & F_PAIRONLY) == 0 && ci < 0 && !(ci & 0x40000000)) {
       const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
-      Vec3<R> e[4];
+      // energies and size-change differences in FP64, forces in R
+      using RE = typename std::conditional<(FL & (F_DU | F_ENERGY)) != 0, double, R>::type;
+      Vec3<RE> ee[4];
       bool valid[4];
-      chain_vectors<MIXED, R>(P, cur, i, p, len, box, e, valid);
-      const R* cf;
-      if constexpr (MIXED) cf = T.chainF[set]; else cf = T.chainD[set];
+      chain_vectors<MIXED, RE>(P, cur, i, p, len, box, ee, valid);
+      Vec3<double> e[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) e[k] = Vec3<double>{(double)ee[k].x, (double)ee[k].y, (double)ee[k].z};
       if constexpr ((FL & F_ENERGY) == 0) {
-        if (valid[1]) bond_term<R>(e[1], cf, (R)-1, fb);          // bond (p-1,p): second
-        if (valid[2]) bond_term<R>(e[2], cf, (R)1, fb);           // bond (p,p+1): first
-        if (valid[0] && valid[1]) bend_term<R>(e[0], e[1], cf + 2, 2, fb);
-        if (valid[1] && valid[2]) bend_term<R>(e[1], e[2], cf + 2, 1, fb);
-        if (valid[2] && valid[3]) bend_term<R>(e[2], e[3], cf + 2, 0, fb);
+        const R* cf;
+        if constexpr (MIXED) cf = T.chainF[set]; else cf = T.chainD[set];
+        Vec3<R> er[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) er[k] = Vec3<R>{(R)ee[k].x, (R)ee[k].y, (R)ee[k].z};
+        if (valid[1]) bond_term<R>(er[1], cf, (R)-1, fb);  // bond (p-1,p): second
+        if (valid[2]) bond_term<R>(er[2], cf, (R)1, fb);   // bond (p,p+1): first
+        if (valid[0] && valid[1]) bend_term<R>(er[0], er[1], cf + 2, 2, fb);
+        if (valid[1] && valid[2]) bend_term<R>(er[1], er[2], cf + 2, 1, fb);
+        if (valid[2] && valid[3]) bend_term<R>(er[2], er[3], cf + 2, 0, fb);
       }
       if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
         // energy terms owned by the first bead of each bond / bend, in FP64
-        Vec3<double> a2{(double)e[2].x, (double)e[2].y, (double)e[2].z};
-        Vec3<double> a3{(double)e[3].x, (double)e[3].y, (double)e[3].z};
         const double* cd = T.chainD[set];
         if constexpr ((FL & F_ENERGY) != 0) {
-          if (valid[2]) e_bond += bond_pot(a2, cd);
-          if (valid[2] && valid[3]) e_bond += bend_pot(a2, a3, cd + 2);
+          if (valid[2]) e_bond += bond_pot(e[2], cd);
+          if (valid[2] && valid[3]) e_bond += bend_pot(e[2], e[3], cd + 2);
         }
         if constexpr ((FL & F_DU) != 0) {
-          const Vec3<double> s2{a2.x * rs.scale[0], a2.y * rs.scale[1], a2.z * rs.scale[2]};
-          const Vec3<double> s3{a3.x * rs.scale[0], a3.y * rs.scale[1], a3.z * rs.scale[2]};
-          if (valid[2]) dU_bond += bond_pot(a2, cd) - bond_pot(s2, cd);
-          if (valid[2] && valid[3]) dU_bond += bend_pot(a2, a3, cd + 2) - bend_pot(s2, s3, cd + 2);
+          const Vec3<double> s2{e[2].x * rs.scale[0], e[2].y * rs.scale[1], e[2].z * rs.scale[2]};
+          const Vec3<double> s3{e[3].x * rs.scale[0], e[3].y * rs.scale[1], e[3].z * rs.scale[2]};
+          if (valid[2]) dU_bond += bond_pot(e[2], cd) - bond_pot(s2, cd);
+          if (valid[2] && valid[3]) dU_bond += bend_pot(e[2], e[3], cd + 2) - bend_pot(s2, s3, cd + 2);
         }
       }
     }
-    // ---- total conservative force
-    double F[3];
-    if constexpr (MIXED) {
-      const float fs = T.fscale;
-      qx += __float2ll_rn(fb.x * fs);
-      qy += __float2ll_rn(fb.y * fs);
-      qz += __float2ll_rn(fb.z * fs);
-      F[0] = (double)qx * T.inv_fscale;
-      F[1] = (double)qy * T.inv_fscale;
-      F[2] = (double)qz * T.inv_fscale;
-    } else {
-      F[0] = fxd + fb.x;
-      F[1] = fyd + fb.y;
-      F[2] = fzd + fb.z;
-    }
-    if constexpr ((FL & F_FORCES) != 0) {
-      const int o = P.orig[i];
-      P.force_out[3 * o] = F[0];
-      P.force_out[3 * o + 1] = F[1];
-      P.force_out[3 * o + 2] = F[2];
-    } else if constexpr ((FL & F_ENERGY) != 0) {
+    if constexpr ((FL & F_ENERGY) != 0) {
       const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
       e_kin = (vx * vx + vy * vy + vz * vz) / 2.0;
     } else {
-      // ---- Langevin (include/algorithms/langevin.h:284-331) and Verlet
-      const int o = P.orig[i];
-      double psi[3];
-      if constexpr ((FL & F_EXTNOISE) != 0) {
-        psi[0] = P.ext_noise[3 * o];
-        psi[1] = P.ext_noise[3 * o + 1];
-        psi[2] = P.ext_noise[3 * o + 2];
+      double F[3];
+      if constexpr (MIXED) {
+        F[0] = (double)P.fq[i] * T.inv_fscale + (double)fb.x;
+        F[1] = (double)P.fq[i + P.n] * T.inv_fscale + (double)fb.y;
+        F[2] = (double)P.fq[i + 2 * P.n] * T.inv_fscale + (double)fb.z;
       } else {
-        langevin_noise(rp.seed, r, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, psi);
+        F[0] = P.fp[i] + fb.x;
+        F[1] = P.fp[i + P.n] + fb.y;
+        F[2] = P.fp[i + 2 * P.n] + fb.z;
       }
-      double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
-      double a[3];
-      for (int d = 0; d < 3; ++d) a[d] = F[d] + (-rp.gamma * v[d] + rp.sigma * psi[d]);
-      const bool sphere = (ci < 0) && (ci & 0x40000000);
-      if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
-        P.ax[i] = a[0];
-        P.ay[i] = a[1];
-        P.az[i] = a[2];
-        if constexpr ((FL & F_STOP) != 0) {
-          if (ti != 0 && !sphere) {
-            const double h = rp.dt * 0.5;
-            P.vx[i] = v[0] + a[0] * h;
-            P.vy[i] = v[1] + a[1] * h;
-            P.vz[i] = v[2] + a[2] * h;
-          }
-        }
-      } else if (!sphere) {
-        double x[3] = {P.x[i], P.y[i], P.z[i]};
-        if (ti != 0) {
-          const double h = rp.dt * 0.5;
-          for (int d = 0; d < 3; ++d) {
-            v[d] += (a[d] * h);  // second() of this step
-            v[d] += (a[d] * h);  // first() of the next step
-            x[d] += v[d] * rp.dt;
-            if (x[d] > box[d]) x[d] -= box[d];
-            if (x[d] < 0) x[d] += box[d];
-          }
-          P.vx[i] = v[0];
-          P.vy[i] = v[1];
-          P.vz[i] = v[2];
-          P.x[i] = x[0];
-          P.y[i] = x[1];
-          P.z[i] = x[2];
-          vmax = (float)sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-        }
-        if constexpr (MIXED) {
-          const uint4 me = P.m4[cur][i];
-          P.m4[cur ^ 1][i] = make_uint4(to_frac(x[0], 1.0 / box[0]), to_frac(x[1], 1.0 / box[1]),
-                                        to_frac(x[2], 1.0 / box[2]), me.w);
-        } else {
-          const double4 me = P.d4[cur][i];
-          P.d4[cur ^ 1][i] = make_double4(x[0], x[1], x[2], me.w);
-        }
+      if constexpr ((FL & F_FORCES) != 0) {
+        const int o = P.orig[i];
+        P.force_out[3 * o] = F[0];
+        P.force_out[3 * o + 1] = F[1];
+        P.force_out[3 * o + 2] = F[2];
       } else {
-        P.ax[i] = a[0];
-        P.ay[i] = a[1];
-        P.az[i] = a[2];
+        const int o = P.orig[i];
+        double noise[3];  // sigma * psi
+        if constexpr ((FL & F_EXTNOISE) != 0) {
+          for (int d = 0; d < 3; ++d) noise[d] = rp.sigma * P.ext_noise[3 * o + d];
+        } else {
+          langevin_noise(rp.seed, r, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
+        }
+        double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+        double a[3];
+        for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
+        const bool sphere = (ci < 0) && (ci & 0x40000000);
+        if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
+          P.ax[i] = a[0];
+          P.ay[i] = a[1];
+          P.az[i] = a[2];
+          if constexpr ((FL & F_STOP) != 0) {
+            if (ti != 0 && !sphere) {
+              const double h = rp.dt * 0.5;
+              P.vx[i] = v[0] + a[0] * h;
+              P.vy[i] = v[1] + a[1] * h;
+              P.vz[i] = v[2] + a[2] * h;
+            }
+          }
+        } else if (!sphere) {
+          double x[3] = {P.x[i], P.y[i], P.z[i]};
+          if (ti != 0) {
+            if constexpr (MIXED) {
+              // second() of this step and first() of the next as one kick
+              for (int d = 0; d < 3; ++d) {
+                v[d] = fma(a[d], rp.dt, v[d]);
+                x[d] = fma(v[d], rp.dt, x[d]);
+                if (x[d] > box[d]) x[d] -= box[d];
+                if (x[d] < 0) x[d] += box[d];
+              }
+            } else {
+              const double h = rp.dt * 0.5;
+              for (int d = 0; d < 3; ++d) {
+                v[d] += (a[d] * h);  // second() of this step
+                v[d] += (a[d] * h);  // first() of the next step
+                x[d] += v[d] * rp.dt;
+                if (x[d] > box[d]) x[d] -= box[d];
+                if (x[d] < 0) x[d] += box[d];
+              }
+            }
+            P.vx[i] = v[0];
+            P.vy[i] = v[1];
+            P.vz[i] = v[2];
+            P.x[i] = x[0];
+            P.y[i] = x[1];
+            P.z[i] = x[2];
+          }
+          const unsigned int fx = to_frac(x[0], rs.frac_per_len[0]), fy = to_frac(x[1], rs.frac_per_len[1]),
+                             fz = to_frac(x[2], rs.frac_per_len[2]);
+          vmax = displacement(P.ref[i], fx, fy, fz, rs);
+          if constexpr (MIXED) {
+            const uint4 me = P.m4[cur][i];
+            P.m4[cur ^ 1][i] = make_uint4(fx, fy, fz, me.w);
+          } else {
+            const double4 me = P.d4[cur][i];
+            P.d4[cur ^ 1][i] = make_double4(x[0], x[1], x[2], me.w);
+          }
+        } else {
+          P.ax[i] = a[0];
+          P.ay[i] = a[1];
+          P.az[i] = a[2];
+        }
       }
     }
   }
-  // ---- reductions
-  if constexpr ((FL & F_DU) != 0) {
-    warp_atomic_add(dU_pair, &P.rs[r].dU_pair, r);
-    warp_atomic_add(dU_bond, &P.rs[r].dU_bond, r);
-  }
+  if constexpr ((FL & F_DU) != 0) warp_atomic_add(dU_bond, &P.rs[r].dU_bond, r);
   if constexpr ((FL & F_ENERGY) != 0) {
-    warp_atomic_add(e_pair, &P.rs[r].e_pair, r);
     warp_atomic_add(e_bond, &P.rs[r].e_bond, r);
     warp_atomic_add(e_kin, &P.rs[r].e_kin, r);
   }
@@ -658,7 +1014,7 @@ __global__ void __launch_bounds__(kBlock) k_step(DevPtrs P, int cur, long long i
     float bm = 0.f;
     if (threadIdx.x == 0)
       for (int w = 0; w < kBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
-    finalize_step(P, bm, P.rp[0].dt, P.half_skin, 0.0);
+    finalize_step(P, bm);
   }
 }
 
@@ -699,11 +1055,12 @@ __global__ void k_mc(DevPtrs P, int trial) {
   rs.last_dU = dPot;
   rs.n_trial++;
   if (D >= u2 || -dPot <= 0) {
-    double shift = 0.0;
+    double shift = 0.0;  // pair distances within rc + skin change by at most this
     for (int d = 0; d < 3; ++d) {
-      shift = fmax(shift, fabs(rs.scale[d] - 1.0) * rs.box[d]);
+      shift = fmax(shift, fabs(rs.scale[d] - 1.0) * P.tab->list_cut);
       rs.box[d] = rs.trial_box[d];
     }
+    derive_box(rs, rp.cell_cap, P.tab->list_cut);
     rs.accept = 1;
     rs.n_accept++;
     P.accept_log[(size_t)trial * P.n_rep + r] = 1;
@@ -746,15 +1103,16 @@ __global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_se
         P.vx[i] = v[0];
         P.vy[i] = v[1];
         P.vz[i] = v[2];
-        vmax = (float)sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
       }
       P.x[i] = x[0];
       P.y[i] = x[1];
       P.z[i] = x[2];
+      const unsigned int fx = to_frac(x[0], rs.frac_per_len[0]), fy = to_frac(x[1], rs.frac_per_len[1]),
+                         fz = to_frac(x[2], rs.frac_per_len[2]);
+      vmax = displacement(P.ref[i], fx, fy, fz, rs);
       if constexpr (MIXED) {
         const uint4 me = P.m4[cur][i];
-        P.m4[cur ^ 1][i] = make_uint4(to_frac(x[0], 1.0 / rs.box[0]), to_frac(x[1], 1.0 / rs.box[1]),
-                                      to_frac(x[2], 1.0 / rs.box[2]), me.w);
+        P.m4[cur ^ 1][i] = make_uint4(fx, fy, fz, me.w);
       } else {
         const double4 me = P.d4[cur][i];
         P.d4[cur ^ 1][i] = make_double4(x[0], x[1], x[2], me.w);
@@ -768,7 +1126,7 @@ __global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_se
   float bm = 0.f;
   if (threadIdx.x == 0)
     for (int w = 0; w < kBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
-  finalize_step(P, bm, P.rp[0].dt, P.half_skin, 0.0);
+  finalize_step(P, bm);
 }
 
 // Mirror of the current positions in the other buffer (after set_state or a
@@ -781,8 +1139,8 @@ __global__ void __launch_bounds__(kBlock) k_mirror(DevPtrs P, int cur) {
   const RepState& rs = P.rs[r];
   if constexpr (MIXED) {
     const uint4 me = P.m4[cur][i];
-    P.m4[cur][i] = make_uint4(to_frac(P.x[i], 1.0 / rs.box[0]), to_frac(P.y[i], 1.0 / rs.box[1]),
-                              to_frac(P.z[i], 1.0 / rs.box[2]), me.w);
+    P.m4[cur][i] = make_uint4(to_frac(P.x[i], rs.frac_per_len[0]), to_frac(P.y[i], rs.frac_per_len[1]),
+                              to_frac(P.z[i], rs.frac_per_len[2]), me.w);
   } else {
     const double4 me = P.d4[cur][i];
     P.d4[cur][i] = make_double4(P.x[i], P.y[i], P.z[i], me.w);
@@ -819,7 +1177,7 @@ __global__ void __launch_bounds__(kBlock) k_pairs(DevPtrs P, int* out, long long
   const double xi = P.x[i], yi = P.y[i], zi = P.z[i];
   const int oi = P.orig[i];
   for (int k = 0; k < P.nnbr[i]; ++k) {
-    const int j = P.nbr[(size_t)k * P.npad + i];
+    const int j = P.nbr[(size_t)i * P.kmax + k];
     const int oj = P.orig[j];
     if (oi >= oj) continue;
     double ox = P.x[j], oy = P.y[j], oz = P.z[j];
