@@ -196,6 +196,25 @@ int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double ar
                              double box, double sphere_radius, double head_umin, double head_umax,
                              double gap);
 
+/* Non-bonded forces for callers that cannot allocate device memory (for
+ * example code running while another framework owns the device memory
+ * through its own pool, or a loop that must not take cudaMalloc's implicit
+ * device-wide synchronisation).  No counterpart in the reference: it is the
+ * FP64 non-bonded force of smd_compute_pair_forces for device-resident
+ * inputs, with its cell-list scratch in a fixed array inside the library
+ * instead of allocated memory.  d_pos (n*3), d_type (n), d_fconst
+ * (6*n_types^2) and d_force (n*3, overwritten) are device pointers owned by
+ * the caller; work is queued on `stream` (a cudaStream_t, NULL = default) and
+ * not waited for.  At most SMD_STATIC_MAX_BEADS beads and
+ * SMD_STATIC_MAX_CELLS cells (int(L/rc) per axis); larger inputs are
+ * rejected.  Calls share the scratch: calls that overlap on the GPU race.
+ * The first call on a device looks up the scratch address; make it before
+ * any stream capture. */
+#define SMD_STATIC_MAX_BEADS 32768
+#define SMD_STATIC_MAX_CELLS 32768
+int smd_pair_forces_static(const double* d_pos, const int* d_type, int n, const double box[3], double cutoff,
+                           int n_types, const double* d_fconst, double* d_force, void* stream);
+
 /* Rewrites the .mpd at in_path with new positions, velocities, box and
  * initialTime into out_path (the store of MD.cpp:373-377). */
 int smd_mpd_update_state(const char* in_path, const char* out_path, const double* pos, const double* vel,

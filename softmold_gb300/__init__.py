@@ -89,6 +89,8 @@ _SIGS = {
     "smd_synth_vesicle_sphere": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                            C.c_double, C.c_double, C.c_double]),
     "smd_md_main": (C.c_int, [C.c_char_p, C.c_int]),
+    "smd_pair_forces_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_int,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 

@@ -24,7 +24,7 @@ ORACLE_OUT = os.path.join(ORACLE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SRC = ["mpd_io.cpp", "observables.cpp", "synth.cpp", "md_driver.cpp", "abi_host.cpp"]
-CU_SRC = ["smd_api.cu"]
+CU_SRC = ["smd_api.cu", "smd_static.cu"]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 
 

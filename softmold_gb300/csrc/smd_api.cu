@@ -36,6 +36,11 @@ constexpr int kTrialChunk = 1024;  // barostat trials staged per upload
 
 using namespace smd;
 
+namespace smd {
+// Lets other translation units of the library report through smd_last_error.
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace smd
+
 struct smd_system {
   bool mixed = true;
   int n = 0, n_rep = 0, npad = 0, kmax = 0, n_cells = 0, n_tiles = 0;
