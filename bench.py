@@ -293,14 +293,16 @@ def main():
     if kernel_launches:
         avg_s = kernel_ms / kernel_launches / 1e3
         achieved = ALG_BYTES_PER_BEAD_STEP * n / avg_s / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
-    if os.path.exists(tf):
-        d = json.load(open(tf))
-        traffic = d.get("dram_bytes_per_bead") and d["dram_bytes_per_bead"] * n
+    traffic = None  # DRAM bytes of one step's force + integrate passes, from the committed ncu summary
+    tf = os.path.join(ROOT, "profiles", "step_kernels_bilayer60k.md")
+    if os.path.exists(tf) and args.workload == "bilayer20k":
+        import re
+        m_ = re.search(r"traffic_bytes_per_bead_step\s*=\s*([0-9.]+)", open(tf).read())
+        if m_:
+            traffic = float(m_.group(1)) * n
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "kernel": "k_step<mixed> (fused forces + Langevin + Verlet)",
+                "kernel": "k_force + k_integ (one step's pair pass and CHAIN/Langevin/Verlet pass)",
                 "kernel_avg_us": 1e3 * kernel_ms / kernel_launches if kernel_launches else None,
                 "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_bead_step": ALG_BYTES_PER_BEAD_STEP}
 
