@@ -14,7 +14,13 @@ through the C ABI with host buffers: per e2e step the state is uploaded, one
 measure interval (50 iterations) is advanced, the energies are measured and the
 state is read back.
 
+Other workloads (--workload): vesicle5k (15,000-bead vesicle, no barostat) and
+batch64 (64 independent bilayers of 1,000-8,000 lipids and tension 0-1, one
+handle, one set of launches per step).  Under torchrun every rank runs its own
+copy of the workload (weak scaling, no data-path collective).
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload bilayer20k|vesicle5k|batch64]
 """
 from __future__ import annotations
 
@@ -48,18 +54,35 @@ def load_peaks():
 
 
 def workload(args, rank, tmpdir):
+    """(paths, systems, config) of the benchmarked workload for one rank."""
     import softmold_gb300 as smd
-    path = os.path.join(tmpdir, f"bench{rank}.mpd")
     if args.workload == "bilayer20k":
+        path = os.path.join(tmpdir, f"bench{rank}.mpd")
         smd.synth_bilayer(path, 1000 + rank, 20000, 3.45, 15.0, 0.01, 0.0)
         cfg = {"workload": "flat tensionless bilayer, 20,000 3-bead lipids (60,000 beads), 3.45/sigma^2, "
                            "z 15 sigma, MC barostat deltaLXY 0.01 tension 0, kT 3, gamma 1, dt 0.02"}
+        paths = [path]
     elif args.workload == "vesicle5k":
+        path = os.path.join(tmpdir, f"bench{rank}.mpd")
         smd.synth_vesicle(path, 1000 + rank, 5000, 3.45, 60.0)
         cfg = {"workload": "vesicle, 5,000 3-bead lipids (15,000 beads), 60^3 box, kT 3, gamma 1, dt 0.02"}
+        paths = [path]
+    elif args.workload == "batch64":
+        rng = np.random.default_rng(64 + 1000 * rank)
+        lipids = rng.integers(1000, 8001, size=64)
+        tensions = rng.uniform(0.0, 1.0, size=64)
+        paths = []
+        for k in range(64):
+            path = os.path.join(tmpdir, f"bench{rank}_{k}.mpd")
+            smd.synth_bilayer(path, 5000 + 64 * rank + k, int(lipids[k]), 3.45, 15.0, 0.01, float(tensions[k]))
+            paths.append(path)
+        cfg = {"workload": "64 independent flat bilayers in one batch, 3-bead lipids per replica uniform in "
+                           "[1000, 8000] (seeded), tension uniform in [0, 1], own seed and box each, z 15 sigma, "
+                           "MC barostat deltaLXY 0.01, kT 3, gamma 1, dt 0.02",
+               "replicas": 64, "lipids_per_replica": [int(x) for x in lipids]}
     else:
         raise SystemExit(f"unknown workload {args.workload}")
-    return path, smd.read_mpd(path), cfg
+    return paths, [smd.read_mpd(p) for p in paths], cfg
 
 
 class ClockSampler:
@@ -134,24 +157,29 @@ def run_reference(args, rank, world):
     from softmold_gb300 import build
     build.build_oracle()
     with tempfile.TemporaryDirectory() as tmp:
-        path, m, cfg = workload(args, 0, tmp)
-        n = len(m.type)
+        paths, ms, cfg = workload(args, 0, tmp)
         threads = os.cpu_count() or 1
-        per_step = 10
         import ctypes as C
         lib = C.CDLL(os.path.join(ROOT, "oracle", "_build", "libsmd_oracle.so"))
         lib.orc_md_time.argtypes = [C.c_char_p, C.c_int, C.c_int]
         lib.orc_md_time.restype = C.c_double
-        name = path[:-4].encode()
-        for _ in range(args.warmup):
-            lib.orc_md_time(name, threads, 2)
-        times = [lib.orc_md_time(name, threads, per_step) for _ in range(args.steps)]
-        total = sum(times)
-        value = n * per_step * args.steps / total
-        sample = f"{args.steps} samples of {per_step} MD steps of the {n}-bead workload"
+        # one bench step: 10 MD steps of the system, or of one replica of a
+        # batch in turn (replicas are independent: bead-steps and times add)
+        per_step = 10
+        for k in range(args.warmup):
+            lib.orc_md_time(paths[k % len(paths)][:-4].encode(), threads, 2)
+        total, units = 0.0, 0
+        for k in range(args.steps):
+            j = k % len(paths)
+            total += lib.orc_md_time(paths[j][:-4].encode(), threads, per_step)
+            units += len(ms[j].type) * per_step
+        value = units / total
+        n = sum(len(m.type) for m in ms)
+        what = f"the {n}-bead workload" if len(ms) == 1 else f"replicas of the {len(ms)}-replica batch in turn"
+        sample = f"{args.steps} samples of {per_step} MD steps of {what}"
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / (args.steps * per_step),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
@@ -188,11 +216,13 @@ def main():
 
     import softmold_gb300 as smd
     from softmold_gb300 import build
+    from softmold_gb300.scaling import job_throughput
     build.build_library()
 
     tmp = tempfile.mkdtemp(prefix="smd_bench_")
-    path, m, cfg = workload(args, rank, tmp)
-    n = len(m.type)
+    paths, ms, cfg = workload(args, rank, tmp)
+    m = ms if len(ms) > 1 else ms[0]
+    n = sum(len(x.type) for x in ms)
     stream = torch.cuda.Stream()
     s = smd.System(m, precision=smd.MIXED, skin=args.skin)
     s.set_stream(stream.cuda_stream)
@@ -242,17 +272,15 @@ def main():
     rebuilds = s.rebuilds() - rebuilds0
     last_disp, slack = s.list_state()
 
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = n * world * K / (max_ms / 1e3)
+    value, _, max_s = job_throughput(n * K, total_ms / 1e3, dist, "cuda")
+    max_ms = 1e3 * max_s
 
     # FP64 plain form on the same state, and the mixed form's force error
     pos, vel = s.state()
     p = smd.System(m, precision=smd.PLAIN_FP64, skin=args.skin)
     p.set_stream(stream.cuda_stream)
-    p.set_box(s.box())
+    for r in range(len(ms)):
+        p.set_box(s.box(r), r)
     p.set_state(pos, vel)
     f_plain = p.forces()
     f_mixed = s.forces()
@@ -264,7 +292,7 @@ def main():
     kp = min(K, 40)
     timed_loop(p, 3)
     plain_ms, _ = timed_loop(p, kp)
-    plain_value = n * kp / (plain_ms / 1e3)
+    plain_value, _, _ = job_throughput(n * kp, plain_ms / 1e3, dist, "cuda")
     p.close()
 
     # end to end through the C ABI with host buffers
@@ -283,8 +311,8 @@ def main():
         t1 = time.perf_counter()
         if k >= 2:
             e2e_t.append(t1 - t0)
-    e2e_value = n * E2E_INTERVAL / statistics.mean(e2e_t)
-    e2e = {"value": e2e_value * world, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes + hv.nbytes),
+    e2e_value, _, _ = job_throughput(n * E2E_INTERVAL, statistics.mean(e2e_t), dist, "cuda")
+    e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes + hv.nbytes),
            "d2h_bytes_per_step": int(hp.nbytes + hv.nbytes + 32),
            "md_steps_per_e2e_step": E2E_INTERVAL, "potential_last": e[0]["pair"] + e[0]["bonded"]}
 
@@ -308,13 +336,23 @@ def main():
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        ck = os.path.join(tmp, "cpu.mpd")
-        smd.mpd_update_state(path, ck, pos, vel, s.box(), 0.0)
         threads = os.cpu_count() or 1
-        steps, secs = cpu_baseline(ck, threads)
-        base = {"value": n * steps / secs, "unit": UNIT, "cores": threads, "kind": "port",
-                "sample": f"{steps} MD steps of the same {n}-bead bilayer (equilibrated state), oracle port "
-                          f"of MD.cpp with OpenMP"}
+        # equilibrated state of (a sample of) the replicas, timed one after another
+        sample = range(len(ms)) if len(ms) == 1 else range(0, len(ms), 16)
+        units, secs = 0, 0.0
+        offs = np.cumsum([0] + [len(x.type) for x in ms])
+        for r in sample:
+            ck = os.path.join(tmp, f"cpu{r}.mpd")
+            a, b = offs[r], offs[r + 1]
+            smd.mpd_update_state(paths[r], ck, pos[a:b], vel[a:b], s.box(r), 0.0)
+            st, t_ = cpu_baseline(ck, threads, target_s=12.0 / len(sample))
+            units += (b - a) * st
+            secs += t_
+        what = (f"the same {n}-bead system" if len(ms) == 1 else
+                f"replicas {list(sample)} of the batch ({sum(offs[r + 1] - offs[r] for r in sample)} beads) "
+                f"one after another")
+        base = {"value": units / secs, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"MD steps of {what} (equilibrated state), oracle port of MD.cpp with OpenMP"}
     s.close()
     if rank == 0:
         cfg.update({"beads_per_gpu": n, "l2": "flushed (256 MiB write) between timed steps",
@@ -326,8 +364,8 @@ def main():
             "dtype": "f32+i64 fixed-point forces, f64 integrate", "data": "synthetic", "config": cfg,
             "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches,
-            "plain_fp64": {"value": plain_value * world, "ms_per_step": plain_ms / kp,
-                           "mixed_speedup": value / (plain_value * world)},
+            "plain_fp64": {"value": plain_value, "ms_per_step": plain_ms / kp,
+                           "mixed_speedup": value / plain_value},
             "force_err": force_err,
         }), flush=True)
     if dist:

@@ -731,13 +731,14 @@ int smd_compute_dU(smd_system* h, const double scale[3], double* dU) {
   std::vector<RepState> saved = rs;
   for (auto& s : rs) {
     s.dU_pair = s.dU_bond = 0;
+    s.dUq_pair = s.dUq_bond = 0;
     for (int k = 0; k < 3; ++k) s.scale[k] = scale[k];
   }
   SMD_CUDA(cudaMemcpyAsync(h->P.rs, rs.data(), h->n_rep * sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
   if ((rc = launch_step<F_DU | F_ENERGY>(h))) return rc;
   SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
-  for (int r = 0; r < h->n_rep; ++r) dU[r] = rs[r].dU_pair + rs[r].dU_bond;
+  for (int r = 0; r < h->n_rep; ++r) dU[r] = rep_dU(rs[r]);
   SMD_CUDA(cudaMemcpyAsync(h->P.rs, saved.data(), h->n_rep * sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
   return read_error(h);

@@ -50,7 +50,8 @@ struct RepState {  // per replica, updated on the device
   float pad_f;
   double trial_box[3];
   double scale[3];   // scale of the last accepted / current trial
-  double dU_pair, dU_bond;
+  double dU_pair, dU_bond;  // FP64 form: U(x) - U(s x) summed in any order
+  long long dUq_pair, dUq_bond;  // mixed form: the same in units of 2^-32, summed exactly
   double e_pair, e_bond, e_kin;
   double last_dU;
   long long n_trial, n_accept;
@@ -58,6 +59,15 @@ struct RepState {  // per replica, updated on the device
   int ncell[3];
   int pad;
 };
+
+// Size-change energy of a replica's current trial.  The mixed form rounds
+// each pair term (twice counted) and each bead's bonded term to 2^-32 before
+// summing, so the total, and with it every Metropolis decision, is the same
+// whatever the pair order or the replicas sharing a launch.
+__host__ __device__ inline double rep_dU(const RepState& rs) {
+  const double q = 0.5 * (double)rs.dUq_pair + (double)rs.dUq_bond;
+  return rs.dU_pair + rs.dU_bond + q * (1.0 / 4294967296.0);
+}
 
 struct Global {  // single instance
   double slack;                // list-distance slack used up by accepted box moves since the build
@@ -194,14 +204,16 @@ __device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
 }
 
 // Langevin noise sigma*psi with psi uniform in (-1,1) (the reference draws
-// 2u-1, include/algorithms/langevin.h:309-314) for bead `orig` of replica
-// `rep` at loop step `it`; phase 1 is the start-up thermostat call.  A draw r
-// gives psi = (signed(r - 2^31) + 1/2) 2^-31, so sigma*psi is one FMA with
+// 2u-1, include/algorithms/langevin.h:309-314) for bead `orig` (index within
+// its replica) at loop step `it`; phase 1 is the start-up thermostat call.
+// The stream depends on the replica's seed only, not on its position in a
+// batch, so a replica evolves the same alone or batched.  A draw r gives
+// psi = (signed(r - 2^31) + 1/2) 2^-31, so sigma*psi is one FMA with
 // sig31 = sigma 2^-31.
-__device__ __forceinline__ void langevin_noise(uint32_t seed, int rep, int orig, long long it, int phase,
-                                               double sig31, double out[3]) {
+__device__ __forceinline__ void langevin_noise(uint32_t seed, int orig, long long it, int phase, double sig31,
+                                               double out[3]) {
   const uint4 c = make_uint4((unsigned)orig, (unsigned)(it & 0xffffffff),
-                             (unsigned)((unsigned long long)it >> 32) ^ ((unsigned)phase << 31), (unsigned)rep);
+                             (unsigned)((unsigned long long)it >> 32) ^ ((unsigned)phase << 31), 0x6D2Bu);
   const uint4 r = philox4x32(c, make_uint2(seed, 0x5A17u));
   const double half = 0.5 * sig31;
   out[0] = fma((double)(int)(r.x ^ 0x80000000u), sig31, half);

@@ -673,6 +673,15 @@ __device__ __forceinline__ void warp_atomic_add(double v, double* dst, int r) {
   if (lane == __ffs(peers) - 1 && acc != 0.0) atomicAdd(dst, acc);
 }
 
+__device__ __forceinline__ void warp_atomic_add_q(long long v, long long* dst, int r) {
+  const unsigned int peers = __match_any_sync(0xffffffffu, r);
+  const int lane = threadIdx.x & 31;
+  long long acc = 0;
+  for (unsigned int rest = peers; rest; rest &= rest - 1) acc += __shfl_sync(peers, v, __ffs(rest) - 1);
+  if (lane == __ffs(peers) - 1 && acc != 0)
+    atomicAdd((unsigned long long*)dst, (unsigned long long)acc);
+}
+
 // Non-bonded pass: G lanes per bead walk the bead's Verlet-list entries
 // (bead-major, so a group reads G consecutive indices per round) and reduce
 // with shuffles.  MIXED: FP32 pair arithmetic, each pair force rounded to a
@@ -702,7 +711,7 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
   const bool active = i < P.n;
   const int r = active ? rep_of(P, i) : 0;
   double dU = 0.0, ep = 0.0;
-  long long qx = 0, qy = 0, qz = 0;
+  long long qx = 0, qy = 0, qz = 0, dq = 0;
   double fx = 0, fy = 0, fz = 0;
   if (active) {
     const RepState& rs = P.rs[r];
@@ -721,7 +730,7 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
       const float* rowF = sF + 6 * ti * nT;
       const float* rowU = sU + 6 * ti * nT;
       const float rc2 = T.rc2f, fs = T.fscale;
-      float eacc = 0.f, dacc = 0.f;
+      float eacc = 0.f;
       int k = sub;
       // two independent gathers in flight per lane
       for (; k + G < nn; k += 2 * G) {
@@ -737,7 +746,7 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
             const float rn2 = r2 + q;
             if (r2 < rc2 || rn2 < rc2) {
               const float rr = sqrtf(r2), rn = sqrtf(rn2);
-              dacc += pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, q / (rn + rr), T.rcf);
+              dq += __float2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, q / (rn + rr), T.rcf) * 4294967296.0f);
             }
           }
           if (r2 < rc2) {
@@ -763,7 +772,7 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
           const float rn2 = r2 + q;
           if (r2 < rc2 || rn2 < rc2) {
             const float rr = sqrtf(r2), rn = sqrtf(rn2);
-            dacc += pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, q / (rn + rr), T.rcf);
+            dq += __float2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, q / (rn + rr), T.rcf) * 4294967296.0f);
           }
         }
         if (r2 < rc2) {
@@ -779,7 +788,6 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
         }
       }
       ep = 0.5 * (double)eacc;
-      dU = 0.5 * (double)dacc;
     } else {
       const double4 me = P.d4[cur][i];
       const int ti = __double_as_longlong(me.w) & 0xff;
@@ -847,7 +855,10 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
       P.fp[i + 2 * P.n] = fz;
     }
   }
-  if constexpr ((FL & F_DU) != 0) warp_atomic_add(dU, &P.rs[r].dU_pair, r);
+  if constexpr ((FL & F_DU) != 0) {
+    if constexpr (MIXED) warp_atomic_add_q(dq, &P.rs[r].dUq_pair, r);
+    else warp_atomic_add(dU, &P.rs[r].dU_pair, r);
+  }
   if constexpr ((FL & F_ENERGY) != 0) warp_atomic_add(ep, &P.rs[r].e_pair, r);
 }
 
@@ -937,7 +948,7 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, long long 
         if constexpr ((FL & F_EXTNOISE) != 0) {
           for (int d = 0; d < 3; ++d) noise[d] = rp.sigma * P.ext_noise[3 * o + d];
         } else {
-          langevin_noise(rp.seed, r, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
+          langevin_noise(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
         }
         double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
         double a[3];
@@ -1001,7 +1012,10 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, long long 
       }
     }
   }
-  if constexpr ((FL & F_DU) != 0) warp_atomic_add(dU_bond, &P.rs[r].dU_bond, r);
+  if constexpr ((FL & F_DU) != 0) {
+    if constexpr (MIXED) warp_atomic_add_q(__double2ll_rn(dU_bond * 4294967296.0), &P.rs[r].dUq_bond, r);
+    else warp_atomic_add(dU_bond, &P.rs[r].dU_bond, r);
+  }
   if constexpr ((FL & F_ENERGY) != 0) {
     warp_atomic_add(e_bond, &P.rs[r].e_bond, r);
     warp_atomic_add(e_kin, &P.rs[r].e_kin, r);
@@ -1025,6 +1039,8 @@ __global__ void k_trial(DevPtrs P, int trial) {
   RepState& rs = P.rs[r];
   rs.dU_pair = 0.0;
   rs.dU_bond = 0.0;
+  rs.dUq_pair = 0;
+  rs.dUq_bond = 0;
   if (P.rp[r].dlxy == 0) {
     for (int d = 0; d < 3; ++d) rs.scale[d] = 1.0;
     return;
@@ -1038,6 +1054,8 @@ __global__ void k_trial(DevPtrs P, int trial) {
   }
   rs.dU_pair = 0.0;
   rs.dU_bond = 0.0;
+  rs.dUq_pair = 0;
+  rs.dUq_bond = 0;
 }
 
 // Metropolis decision (MD.cpp:677-720).
@@ -1048,7 +1066,7 @@ __global__ void k_mc(DevPtrs P, int trial) {
   const RepParams& rp = P.rp[r];
   rs.accept = 0;
   if (rp.dlxy == 0) return;
-  double dPot = rs.dU_pair + rs.dU_bond;
+  double dPot = rep_dU(rs);
   if (rp.tension != 0) dPot += rp.tension * ((rs.trial_box[0] * rs.trial_box[1]) - (rs.box[0] * rs.box[1]));
   const double D = exp(dPot / rp.kT);
   const double u2 = P.trial_u[((size_t)trial * P.n_rep + r) * 2 + 1];
