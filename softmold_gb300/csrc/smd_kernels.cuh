@@ -888,20 +888,23 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, long long 
     const int ci = P.cinfo[i];
     if ((FL & F_PAIRONLY) == 0 && ci < 0 && !(ci & 0x40000000)) {
       const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
-      // energies and size-change differences in FP64, forces in R
-      using RE = typename std::conditional<(FL & (F_DU | F_ENERGY)) != 0, double, R>::type;
-      Vec3<RE> ee[4];
+      // forces in R from the same vectors in every variant; energies and
+      // size-change differences in FP64
+      Vec3<R> er[4];
       bool valid[4];
-      chain_vectors<MIXED, RE>(P, cur, i, p, len, box, ee, valid);
+      chain_vectors<MIXED, R>(P, cur, i, p, len, box, er, valid);
       Vec3<double> e[4];
+      if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
+        if constexpr (MIXED) {
+          chain_vectors<MIXED, double>(P, cur, i, p, len, box, e, valid);
+        } else {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) e[k] = Vec3<double>{(double)ee[k].x, (double)ee[k].y, (double)ee[k].z};
+          for (int k = 0; k < 4; ++k) e[k] = Vec3<double>{er[k].x, er[k].y, er[k].z};
+        }
+      }
       if constexpr ((FL & F_ENERGY) == 0) {
         const R* cf;
         if constexpr (MIXED) cf = T.chainF[set]; else cf = T.chainD[set];
-        Vec3<R> er[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) er[k] = Vec3<R>{(R)ee[k].x, (R)ee[k].y, (R)ee[k].z};
         if (valid[1]) bond_term<R>(er[1], cf, (R)-1, fb);  // bond (p-1,p): second
         if (valid[2]) bond_term<R>(er[2], cf, (R)1, fb);   // bond (p,p+1): first
         if (valid[0] && valid[1]) bend_term<R>(er[0], er[1], cf + 2, 2, fb);
@@ -961,18 +964,21 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, long long 
           if constexpr ((FL & F_STOP) != 0) {
             if (ti != 0 && !sphere) {
               const double h = rp.dt * 0.5;
-              P.vx[i] = v[0] + a[0] * h;
-              P.vy[i] = v[1] + a[1] * h;
-              P.vz[i] = v[2] + a[2] * h;
+              P.vx[i] = fma(a[0], h, v[0]);
+              P.vy[i] = fma(a[1], h, v[1]);
+              P.vz[i] = fma(a[2], h, v[2]);
             }
           }
         } else if (!sphere) {
           double x[3] = {P.x[i], P.y[i], P.z[i]};
           if (ti != 0) {
             if constexpr (MIXED) {
-              // second() of this step and first() of the next as one kick
+              // second() of this step and first() of the next, rounded as the
+              // stopped step and k_finish round them, so that a replica's
+              // trajectory does not depend on where other replicas stop
+              const double h = rp.dt * 0.5;
               for (int d = 0; d < 3; ++d) {
-                v[d] = fma(a[d], rp.dt, v[d]);
+                v[d] = fma(a[d], h, fma(a[d], h, v[d]));
                 x[d] = fma(v[d], rp.dt, x[d]);
                 if (x[d] > box[d]) x[d] -= box[d];
                 if (x[d] < 0) x[d] += box[d];
@@ -1112,9 +1118,9 @@ __global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_se
         const double a[3] = {P.ax[i], P.ay[i], P.az[i]};
         double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
         for (int d = 0; d < 3; ++d) {
-          if (do_second) v[d] += (a[d] * h);
-          v[d] += (a[d] * h);
-          x[d] += v[d] * rp.dt;
+          if (do_second) v[d] = fma(a[d], h, v[d]);
+          v[d] = fma(a[d], h, v[d]);
+          x[d] = fma(v[d], rp.dt, x[d]);
           if (x[d] > rs.box[d]) x[d] -= rs.box[d];
           if (x[d] < 0) x[d] += rs.box[d];
         }

@@ -8,7 +8,6 @@ they are bitwise identical to the system run alone.
 """
 import numpy as np
 import pytest
-from conftest import load_golden, mpd_from_golden
 
 import softmold_gb300 as smd
 
@@ -16,10 +15,14 @@ pytestmark = pytest.mark.gpu
 
 
 def _systems(tmp_path):
-    ms = [mpd_from_golden(load_golden("bil400")), mpd_from_golden(load_golden("ves300"))]
-    p = str(tmp_path / "t.mpd")
-    smd.synth_bilayer(p, 31, 500, 3.45, 18.0, 0.01, 0.5)  # tension 0.5, own seed and box
-    ms.append(smd.read_mpd(p))
+    """Three bilayers sharing the pair tables: own sizes, seeds and boxes;
+    tension 0 and 0.5 with the barostat, and one without it."""
+    ms = []
+    for k, (seed, lipids, dlxy, tension) in enumerate(((31, 400, 0.01, 0.0), (32, 260, 0.0, 0.0),
+                                                       (33, 500, 0.01, 0.5))):
+        p = str(tmp_path / f"t{k}.mpd")
+        smd.synth_bilayer(p, seed, lipids, 3.45, 18.0, dlxy, tension)
+        ms.append(smd.read_mpd(p))
     return ms
 
 
@@ -59,4 +62,4 @@ def test_batch_trajectories_equal_single_runs(built, tmp_path):
         assert b.mc_stats(k) == s.mc_stats(), k
         off += n
     assert b.mc_stats(0)["trials"] >= 14 and b.mc_stats(2)["trials"] >= 14
-    assert b.mc_stats(1)["trials"] == 0  # the vesicle runs without the barostat
+    assert b.mc_stats(1)["trials"] == 0  # replica 1 runs without the barostat
