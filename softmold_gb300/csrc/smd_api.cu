@@ -129,10 +129,10 @@ int rebuild_if_needed(smd_system* h, bool clear_after = false) {
   SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, h->stream>>>(P));
   if (h->mixed) {
     SMD_LAUNCH(h, k_reorder<true><<<g, kBlock, 0, h->stream>>>(P, h->cur));
-    SMD_LAUNCH(h, (k_nbr_cells<true><<<h->nbr_grid(), kNbrThreads, 0, h->stream>>>(P, h->cur)));
+    SMD_LAUNCH(h, (k_nbr_cells_oct<<<h->nbr_grid(), kOctThreads, 0, h->stream>>>(P, h->cur)));
   } else {
     SMD_LAUNCH(h, k_reorder<false><<<g, kBlock, 0, h->stream>>>(P, h->cur));
-    SMD_LAUNCH(h, (k_nbr_cells<false><<<h->nbr_grid(), kNbrThreads, 0, h->stream>>>(P, h->cur)));
+    SMD_LAUNCH(h, (k_nbr_cells_plain<<<h->nbr_grid(), kNbrThreads, 0, h->stream>>>(P, h->cur)));
   }
   if (clear_after) SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 0));
   return 0;
@@ -369,6 +369,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   T.rc2f = (float)(d0.cutoff * d0.cutoff);
   T.list_cut = d0.cutoff + h->skin;
   T.list_cut2 = T.list_cut * T.list_cut;
+  T.list_cut_f = (float)T.list_cut;
   double maxF = 1.0;
   for (int k = 0; k < d0.n_types * d0.n_types; ++k) {
     const double* c = d0.fconst + 6 * k;

@@ -89,6 +89,7 @@ struct Tables {  // force/potential tables (float and double) in constant-like m
   double rc2, rc;
   double list_cut2;  // (rc+skin)^2
   double list_cut;
+  float list_cut_f;
   float fscale;      // fixed-point scale of one pair force (2^k)
   double inv_fscale;
   float fF[6 * kMaxTypes * kMaxTypes];

@@ -192,199 +192,49 @@ __global__ void __launch_bounds__(kBlock) k_reorder(DevPtrs P, int cur) {
   }
 }
 
-// Lanes of group g of size G within the warp.
-template <int G>
-__device__ __forceinline__ unsigned int group_mask() {
-  if constexpr (G == 32) {
-    return 0xffffffffu;
-  } else {
-    const unsigned int lane = threadIdx.x & 31;
-    return ((1u << G) - 1u) << (lane & ~(unsigned)(G - 1));
-  }
-}
-
-// Copies the reordered state back and builds the Verlet list of bead i from
-// the 27 (or fewer, for thin boxes) surrounding cells, reading the reordered
-// mirror that k_reorder left in the scratch buffer.  G lanes share one bead:
-// each tests every G-th candidate of a cell and the group appends its hits
-// with a ballot, so list entries of one bead are contiguous (bead-major).
-template <bool MIXED, int G>
-__global__ void __launch_bounds__(kBlock) k_nbr(DevPtrs P, int cur) {
-  if (!P.g->rebuild) return;
-  const int t = blockIdx.x * kBlock + threadIdx.x;
-  const int i = t / G, sub = t % G;
-  if (t == 0) {
-    P.g->slack = 0.0;
-    P.g->n_rebuilds++;
-  }
-  if (i >= P.n) return;  // whole groups leave together (n*G threads are grouped)
-  const int r = rep_of(P, i);
-  const RepState& rs = P.rs[r];
-  if (sub == 0) {
-    P.x[i] = P.tx[i];
-    P.y[i] = P.ty[i];
-    P.z[i] = P.tz[i];
-    P.vx[i] = P.tvx[i];
-    P.vy[i] = P.tvy[i];
-    P.vz[i] = P.tvz[i];
-    P.ax[i] = P.tax[i];
-    P.ay[i] = P.tay[i];
-    P.az[i] = P.taz[i];
-    P.orig[i] = P.torig[i];
-    P.cinfo[i] = P.tcinfo[i];
-    if constexpr (MIXED) {
-      P.m4[cur][i] = P.mt[i];
-      P.ref[i] = P.mt[i];
-    } else {
-      const double4 d = P.dt4[i];
-      P.d4[cur][i] = d;
-      P.ref[i] = make_uint4(to_frac(d.x, rs.frac_per_len[0]), to_frac(d.y, rs.frac_per_len[1]),
-                            to_frac(d.z, rs.frac_per_len[2]), 0u);
-    }
-  }
-  const int n0 = rs.ncell[0], n1 = rs.ncell[1], n2 = rs.ncell[2];
-  const int cb = P.rp[r].cell_begin;
-  const int local = P.tkey[i] - cb;
-  const int cx = local % n0, cy = (local / n0) % n1, cz = local / (n0 * n1);
-  // The stencil as contiguous bead ranges: cells are ordered x-fastest, so
-  // each (dy,dz) row of 3 cells is one range unless it wraps in x.
-  int seg_s[18], seg_e[18];
-  int nseg = 0;
-  const int lo1 = n1 >= 3 ? -1 : 0, hi1 = n1 >= 2 ? 1 : 0;
-  const int lo2 = n2 >= 3 ? -1 : 0, hi2 = n2 >= 2 ? 1 : 0;
-  int xa = cx - 1, xb = cx + 1;  // x run [xa, xb] before wrapping
-  if (n0 < 3) {
-    xa = 0;
-    xb = n0 - 1;
-  }
-  for (int oz = lo2; oz <= hi2; ++oz) {
-    const int zz = (cz + oz + n2) % n2;
-    for (int oy = lo1; oy <= hi1; ++oy) {
-      const int yy = (cy + oy + n1) % n1;
-      const int row = cb + n0 * (yy + n1 * zz);
-      if (xa >= 0 && xb < n0) {
-        seg_s[nseg] = P.cell_start[row + xa];
-        seg_e[nseg++] = P.cell_start[row + xb + 1];
-      } else if (xa < 0) {  // cells n0-1 | 0..xb
-        seg_s[nseg] = P.cell_start[row + n0 - 1];
-        seg_e[nseg++] = P.cell_start[row + n0];
-        seg_s[nseg] = P.cell_start[row];
-        seg_e[nseg++] = P.cell_start[row + xb + 1];
-      } else {  // cells xa..n0-1 | 0
-        seg_s[nseg] = P.cell_start[row + xa];
-        seg_e[nseg++] = P.cell_start[row + n0];
-        seg_s[nseg] = P.cell_start[row];
-        seg_e[nseg++] = P.cell_start[row + 1];
-      }
-    }
-  }
-  const unsigned int gm = group_mask<G>();
-  const unsigned int below = (1u << (threadIdx.x & 31)) - 1u;
-  int cnt = 0;
-  const int kmax = P.kmax;
-  int* out = P.nbr + (size_t)i * kmax;
-  uint4 mi;
-  double4 di;
-  float sc[3];
-  const float lc2f = (float)P.tab->list_cut2;
-  if constexpr (MIXED) {
-    mi = P.mt[i];
-    for (int d = 0; d < 3; ++d) sc[d] = rs.len_per_frac[d];
-  } else {
-    di = P.dt4[i];
-  }
-  auto test = [&](int j, int e) -> bool {
-    if (j >= e || j == i) return false;
-    if constexpr (MIXED) {
-      const uint4 mj = P.mt[j];
-      const float dx = frac_delta(mi.x, mj.x, sc[0]), dy = frac_delta(mi.y, mj.y, sc[1]),
-                  dz = frac_delta(mi.z, mj.z, sc[2]);
-      return dx * dx + dy * dy + dz * dz < lc2f;
-    } else {
-      const double4 dj = P.dt4[j];
-      double dx = di.x - dj.x, dy = di.y - dj.y, dz = di.z - dj.z;
-      dx -= rs.box[0] * rint(dx / rs.box[0]);
-      dy -= rs.box[1] * rint(dy / rs.box[1]);
-      dz -= rs.box[2] * rint(dz / rs.box[2]);
-      return dx * dx + dy * dy + dz * dz < P.tab->list_cut2;
-    }
-  };
-  auto append = [&](bool hit, int j) {
-    const unsigned int hits = __ballot_sync(gm, hit) & gm;
-    if (hit) {
-      const int slot = cnt + __popc(hits & below);
-      if (slot < kmax) out[slot] = j;
-    }
-    cnt += __popc(hits);
-  };
-  for (int q = 0; q < nseg; ++q) {
-    const int s = seg_s[q], e = seg_e[q];
-    int j0 = s;
-    for (; j0 + G < e; j0 += 2 * G) {  // two candidate loads in flight per lane
-      const int ja = j0 + sub, jb = j0 + G + sub;
-      const bool ha = test(ja, e), hb = test(jb, e);
-      append(ha, ja);
-      append(hb, jb);
-    }
-    for (; j0 < e; j0 += G) {
-      const int ja = j0 + sub;
-      append(test(ja, e), ja);
-    }
-  }
-  if (sub == 0) {
-    P.nnbr[i] = cnt < kmax ? cnt : kmax;
-    if (cnt > kmax) {
-      atomicOr(&P.g->error, 1);
-      atomicMax(&P.g->need_nbr, cnt);
-    }
-  }
-}
-
-// Cell-centred Verlet-list build: one CTA per cell of the list grid.  The CTA
-// stages the stencil's beads (9 contiguous x-rows of the cell-sorted order, in
-// chunks of kNbrChunk) in shared memory; each warp then takes one bead of the
-// cell at a time, tests 32 staged candidates per round and appends the hits
-// with a ballot, so each bead's list is written contiguously.  The CTA also
-// copies its beads' reordered state back and records their build positions.
-constexpr int kNbrThreads = 128;
-constexpr int kNbrChunk = 1536;
+// ------------------------------------------------------------ Verlet lists
+// One CTA per cell of the list grid.  The CTA copies its beads' reordered
+// state back, records their build positions, stages the beads of the 27
+// surrounding cells (contiguous x-rows of the cell-sorted order) in shared
+// memory and appends each bead's hits with a ballot, so a bead's list is
+// written contiguously (bead-major).
 constexpr int kNbrMaxCell = 1024;
 
-template <bool MIXED, int kChunk>
-__device__ __forceinline__ void nbr_cell(const DevPtrs& P, int cur, int c);
+struct CellCtx {
+  int s, e;          // bead range of the cell
+  int r, cb;         // replica and its first cell
+  int cx, cy, cz;    // cell coordinates
+  int n0, n1, n2;    // replica grid
+};
 
-template <bool MIXED>
-__global__ void __launch_bounds__(kNbrThreads) k_nbr_cells(DevPtrs P, int cur) {
-  constexpr int kChunk = MIXED ? kNbrChunk : kNbrChunk / 2;  // 24 KB of staged positions either way
-  if (!P.g->rebuild) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    P.g->slack = 0.0;
-    P.g->n_rebuilds++;
-  }
-  for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) {
-    nbr_cell<MIXED, kChunk>(P, cur, c);
-  }
-}
-
-// The work of k_nbr_cells for one cell c (block-uniform control flow).
-template <bool MIXED, int kChunk>
-__device__ __forceinline__ void nbr_cell(const DevPtrs& P, int cur, int c) {
-  const int s = P.cell_start[c], e = P.cell_start[c + 1];
-  if (s >= e) return;
-  // replica owning the cell
+// (Called for occupied cells only: most cells of a thin membrane box are
+// empty, and their CTAs should return after two loads.)
+__device__ __forceinline__ CellCtx cell_ctx(const DevPtrs& P, int c, int s, int e) {
+  CellCtx q;
+  q.s = s;
+  q.e = e;
   int lo = 0, hi = P.n_rep - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
     if (P.rp[mid].cell_begin <= c) lo = mid; else hi = mid - 1;
   }
-  const int r = lo;
-  const RepState& rs = P.rs[r];
-  const int cb = P.rp[r].cell_begin;
-  const int n0 = rs.ncell[0], n1 = rs.ncell[1], n2 = rs.ncell[2];
-  const int local = c - cb;
-  const int cx = local % n0, cy = (local / n0) % n1, cz = local / (n0 * n1);
-  // copy back this cell's reordered state
-  for (int i = s + threadIdx.x; i < e; i += kNbrThreads) {
+  q.r = lo;
+  q.cb = P.rp[lo].cell_begin;
+  const RepState& rs = P.rs[lo];
+  q.n0 = rs.ncell[0];
+  q.n1 = rs.ncell[1];
+  q.n2 = rs.ncell[2];
+  const int local = c - q.cb;
+  q.cx = local % q.n0;
+  q.cy = (local / q.n0) % q.n1;
+  q.cz = local / (q.n0 * q.n1);
+  return q;
+}
+
+// Copies the cell's reordered state back from the scratch arrays.
+template <bool MIXED, int NT>
+__device__ __forceinline__ void copy_back(const DevPtrs& P, int cur, const CellCtx& q, const RepState& rs) {
+  for (int i = q.s + threadIdx.x; i < q.e; i += NT) {
     P.x[i] = P.tx[i];
     P.y[i] = P.ty[i];
     P.z[i] = P.tz[i];
@@ -406,141 +256,399 @@ __device__ __forceinline__ void nbr_cell(const DevPtrs& P, int cur, int c) {
                             to_frac(d.z, rs.frac_per_len[2]), 0u);
     }
   }
-  // stencil segments (contiguous bead ranges) and their prefix sums
-  __shared__ int seg_s[18], seg_p[19];
-  __shared__ int nseg_sh;
-  __syncthreads();  // the previous cell of this CTA is done with the shared arrays
-  if (threadIdx.x == 0) {
-    int nseg = 0;
-    const int lo1 = n1 >= 3 ? -1 : 0, hi1 = n1 >= 2 ? 1 : 0;
-    const int lo2 = n2 >= 3 ? -1 : 0, hi2 = n2 >= 2 ? 1 : 0;
-    int xa = cx - 1, xb = cx + 1;
-    if (n0 < 3) {
-      xa = 0;
-      xb = n0 - 1;
-    }
-    int acc = 0;
-    for (int oz = lo2; oz <= hi2; ++oz) {
-      const int zz = (cz + oz + n2) % n2;
-      for (int oy = lo1; oy <= hi1; ++oy) {
-        const int yy = (cy + oy + n1) % n1;
-        const int row = cb + n0 * (yy + n1 * zz);
-        int a0, a1, b0 = 0, b1 = 0;
-        if (xa >= 0 && xb < n0) {
-          a0 = row + xa;
-          a1 = row + xb + 1;
-        } else if (xa < 0) {
-          a0 = row + n0 - 1;
-          a1 = row + n0;
-          b0 = row;
-          b1 = row + xb + 1;
-        } else {
-          a0 = row + xa;
-          a1 = row + n0;
-          b0 = row;
-          b1 = row + 1;
-        }
-        seg_s[nseg] = P.cell_start[a0];
+}
+
+// The stencil as contiguous bead ranges with prefix sums (one thread): cells
+// are ordered x-fastest, so each (dy,dz) row of 3 cells is one range unless
+// it wraps in x.  Axes with fewer than 3 cells take every cell once.
+__device__ __forceinline__ int stencil_segments(const DevPtrs& P, const CellCtx& q, int* seg_s, int* seg_p) {
+  int nseg = 0;
+  const int lo1 = q.n1 >= 3 ? -1 : 0, hi1 = q.n1 >= 2 ? 1 : 0;
+  const int lo2 = q.n2 >= 3 ? -1 : 0, hi2 = q.n2 >= 2 ? 1 : 0;
+  int xa = q.cx - 1, xb = q.cx + 1;
+  if (q.n0 < 3) {
+    xa = 0;
+    xb = q.n0 - 1;
+  }
+  int acc = 0;
+  for (int oz = lo2; oz <= hi2; ++oz) {
+    const int zz = (q.cz + oz + q.n2) % q.n2;
+    for (int oy = lo1; oy <= hi1; ++oy) {
+      const int yy = (q.cy + oy + q.n1) % q.n1;
+      const int row = q.cb + q.n0 * (yy + q.n1 * zz);
+      int a0, a1, b0 = 0, b1 = 0;
+      if (xa >= 0 && xb < q.n0) {
+        a0 = row + xa;
+        a1 = row + xb + 1;
+      } else if (xa < 0) {  // cells n0-1 | 0..xb
+        a0 = row + q.n0 - 1;
+        a1 = row + q.n0;
+        b0 = row;
+        b1 = row + xb + 1;
+      } else {  // cells xa..n0-1 | 0
+        a0 = row + xa;
+        a1 = row + q.n0;
+        b0 = row;
+        b1 = row + 1;
+      }
+      seg_s[nseg] = P.cell_start[a0];
+      seg_p[nseg] = acc;
+      acc += P.cell_start[a1] - seg_s[nseg];
+      ++nseg;
+      if (b1 > b0) {
+        seg_s[nseg] = P.cell_start[b0];
         seg_p[nseg] = acc;
-        acc += P.cell_start[a1] - seg_s[nseg];
+        acc += P.cell_start[b1] - seg_s[nseg];
         ++nseg;
-        if (b1 > b0) {
-          seg_s[nseg] = P.cell_start[b0];
-          seg_p[nseg] = acc;
-          acc += P.cell_start[b1] - seg_s[nseg];
-          ++nseg;
-        }
       }
     }
-    seg_p[nseg] = acc;
-    nseg_sh = nseg;
   }
-  __syncthreads();
-  const int nseg = nseg_sh;
-  const int M = seg_p[nseg];
-  const int nb = e - s;
+  seg_p[nseg] = acc;
+  return nseg;
+}
+
+// Bead of staged position g.
+__device__ __forceinline__ int seg_bead(const int* seg_s, const int* seg_p, int nseg, int g) {
+  int q = 0;
+  while (q + 1 < nseg && seg_p[q + 1] <= g) ++q;
+  return seg_s[q] + (g - seg_p[q]);
+}
+
+__device__ __forceinline__ void list_counts(const DevPtrs& P, const CellCtx& q, const int* cnt, int nt) {
+  for (int b = threadIdx.x; b < q.e - q.s; b += nt) {
+    const int count = cnt[b];
+    P.nnbr[q.s + b] = count < P.kmax ? count : P.kmax;
+    if (count > P.kmax) {
+      atomicOr(&P.g->error, 1);
+      atomicMax(&P.g->need_nbr, count);
+    }
+  }
+}
+
+__device__ __forceinline__ void list_build_begin(const DevPtrs& P) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.g->slack = 0.0;
+    P.g->n_rebuilds++;
+  }
+}
+
+// ---- FP64 form: each warp takes one bead of the cell at a time and tests
+// 32 staged candidates per round with the minimum image of the box.
+constexpr int kNbrThreads = 128;
+constexpr int kNbrChunkD = 768;  // 24 KB of staged double4
+
+__device__ __forceinline__ void nbr_cell_plain(const DevPtrs& P, int cur, int c) {
+  const int s0 = P.cell_start[c], e0 = P.cell_start[c + 1];
+  if (s0 >= e0) return;
+  const CellCtx q = cell_ctx(P, c, s0, e0);
+  const RepState& rs = P.rs[q.r];
+  copy_back<false, kNbrThreads>(P, cur, q, rs);
+  __shared__ int seg_s[18], seg_p[19];
+  __shared__ int nseg_sh;
+  __shared__ int cnt[kNbrMaxCell];
+  __shared__ int cidx[kNbrChunkD];
+  __shared__ double4 cposd[kNbrChunkD];
+  __syncthreads();  // the previous cell of this CTA is done with the shared arrays
+  const int nb = q.e - q.s;
   if (nb > kNbrMaxCell) {
     if (threadIdx.x == 0) atomicOr(&P.g->error, 2);
     return;
   }
-  __shared__ int cnt[kNbrMaxCell];
-  __shared__ int cidx[kChunk];
-  __shared__ uint4 cpos4[MIXED ? kChunk : 1];
-  __shared__ double4 cposd[MIXED ? 1 : kChunk];
+  if (threadIdx.x == 0) nseg_sh = stencil_segments(P, q, seg_s, seg_p);
   for (int k = threadIdx.x; k < nb; k += kNbrThreads) cnt[k] = 0;
+  __syncthreads();
+  const int nseg = nseg_sh;
+  const int M = seg_p[nseg];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned int below = (1u << lane) - 1u;
   const int kmax = P.kmax;
-  float sc[3] = {rs.len_per_frac[0], rs.len_per_frac[1], rs.len_per_frac[2]};
-  const float lc2f = (float)P.tab->list_cut2;
   const double lc2 = P.tab->list_cut2;
-  for (int base = 0; base < M; base += kChunk) {
-    const int m = min(kChunk, M - base);
+  for (int base = 0; base < M; base += kNbrChunkD) {
+    const int m = min(kNbrChunkD, M - base);
     __syncthreads();
     for (int k = threadIdx.x; k < m; k += kNbrThreads) {
-      const int g = base + k;
-      int q = 0;
-      while (q + 1 < nseg && seg_p[q + 1] <= g) ++q;
-      const int j = seg_s[q] + (g - seg_p[q]);
+      const int j = seg_bead(seg_s, seg_p, nseg, base + k);
       cidx[k] = j;
-      if constexpr (MIXED) cpos4[k] = P.mt[j]; else cposd[k] = P.dt4[j];
+      cposd[k] = P.dt4[j];
     }
     __syncthreads();
     for (int b = warp; b < nb; b += kNbrThreads / 32) {
-      const int i = s + b;
+      const int i = q.s + b;
       int count = cnt[b];
       int* out = P.nbr + (size_t)i * kmax;
-      if constexpr (MIXED) {
-        const uint4 mi = P.mt[i];
-        for (int k0 = 0; k0 < m; k0 += 32) {
-          const int k = k0 + lane;
-          bool hit = false;
-          if (k < m) {
-            const uint4 mj = cpos4[k];
-            const float dx = frac_delta(mi.x, mj.x, sc[0]), dy = frac_delta(mi.y, mj.y, sc[1]),
-                        dz = frac_delta(mi.z, mj.z, sc[2]);
-            hit = (dx * dx + dy * dy + dz * dz < lc2f) && (cidx[k] != i);
-          }
-          const unsigned int hits = __ballot_sync(0xffffffffu, hit);
-          if (hit) {
-            const int slot = count + __popc(hits & below);
-            if (slot < kmax) out[slot] = cidx[k];
-          }
-          count += __popc(hits);
+      const double4 di = P.dt4[i];
+      for (int k0 = 0; k0 < m; k0 += 32) {
+        const int k = k0 + lane;
+        bool hit = false;
+        if (k < m) {
+          const double4 dj = cposd[k];
+          double dx = di.x - dj.x, dy = di.y - dj.y, dz = di.z - dj.z;
+          dx -= rs.box[0] * rint(dx * (1.0 / 4294967296.0) * rs.frac_per_len[0]);
+          dy -= rs.box[1] * rint(dy * (1.0 / 4294967296.0) * rs.frac_per_len[1]);
+          dz -= rs.box[2] * rint(dz * (1.0 / 4294967296.0) * rs.frac_per_len[2]);
+          hit = (dx * dx + dy * dy + dz * dz < lc2) && (cidx[k] != i);
         }
-      } else {
-        const double4 di = P.dt4[i];
-        for (int k0 = 0; k0 < m; k0 += 32) {
-          const int k = k0 + lane;
-          bool hit = false;
-          if (k < m) {
-            const double4 dj = cposd[k];
-            double dx = di.x - dj.x, dy = di.y - dj.y, dz = di.z - dj.z;
-            dx -= rs.box[0] * rint(dx * (1.0 / 4294967296.0) * rs.frac_per_len[0]);
-            dy -= rs.box[1] * rint(dy * (1.0 / 4294967296.0) * rs.frac_per_len[1]);
-            dz -= rs.box[2] * rint(dz * (1.0 / 4294967296.0) * rs.frac_per_len[2]);
-            hit = (dx * dx + dy * dy + dz * dz < lc2) && (cidx[k] != i);
-          }
-          const unsigned int hits = __ballot_sync(0xffffffffu, hit);
-          if (hit) {
-            const int slot = count + __popc(hits & below);
-            if (slot < kmax) out[slot] = cidx[k];
-          }
-          count += __popc(hits);
+        const unsigned int hits = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+          const int slot = count + __popc(hits & below);
+          if (slot < kmax) out[slot] = cidx[k];
         }
+        count += __popc(hits);
       }
       if (lane == 0) cnt[b] = count;
     }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < nb; b += kNbrThreads) {
-    const int count = cnt[b];
-    P.nnbr[s + b] = count < kmax ? count : kmax;
-    if (count > kmax) {
-      atomicOr(&P.g->error, 1);
-      atomicMax(&P.g->need_nbr, count);
+  list_counts(P, q, cnt, kNbrThreads);
+}
+
+__global__ void __launch_bounds__(kNbrThreads) k_nbr_cells_plain(DevPtrs P, int cur) {
+  if (!P.g->rebuild) return;
+  list_build_begin(P);
+  for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) nbr_cell_plain(P, cur, c);
+}
+
+// ---- Mixed form, octant-filtered.  Candidates are staged as FP32 offsets
+// from the cell centre (exact 32-bit fractional differences, scaled once).
+// While staging, each thread also tests its candidate against the boxes of
+// the eight octants of the cell and appends it to the list of every octant
+// it lies within list_cut of (about 45 % of the stencil per octant).  Each
+// bead of the cell then tests only its octant's list, 32 candidates per
+// round; beads go to warps round-robin, whatever their octant.  The list cut
+// carries a 1e-4 sigma margin over the FP32 rounding of the offsets, so the
+// list is a superset of the exact one.
+constexpr int kOctThreads = 256;
+constexpr int kOctChunk = 1024;  // staged candidates per pass (16 KB)
+
+__device__ __forceinline__ unsigned int cell_centre_frac(int c, int n) {
+  return (unsigned int)((((unsigned long long)(2 * c + 1)) << 32) / (unsigned long long)(2 * n));
+}
+
+// Row segments of the stencil computed by nine threads at once: row t
+// (dy, dz) gives slots 2t and 2t+1 (the second is empty unless the row
+// wraps in x); thread 0 then forms the prefix sums.
+__device__ __forceinline__ void stencil_rows(const DevPtrs& P, const CellCtx& q, int* seg_s, int* seg_len) {
+  const int t = threadIdx.x;
+  if (t >= 9) return;
+  const int oy = t % 3 - 1, oz = t / 3 - 1;
+  const int lo1 = q.n1 >= 3 ? -1 : 0, hi1 = q.n1 >= 2 ? 1 : 0;
+  const int lo2 = q.n2 >= 3 ? -1 : 0, hi2 = q.n2 >= 2 ? 1 : 0;
+  seg_len[2 * t] = 0;
+  seg_len[2 * t + 1] = 0;
+  seg_s[2 * t] = 0;
+  seg_s[2 * t + 1] = 0;
+  if (oy < lo1 || oy > hi1 || oz < lo2 || oz > hi2) return;
+  int xa = q.cx - 1, xb = q.cx + 1;
+  if (q.n0 < 3) {
+    xa = 0;
+    xb = q.n0 - 1;
+  }
+  const int zz = (q.cz + oz + q.n2) % q.n2, yy = (q.cy + oy + q.n1) % q.n1;
+  const int row = q.cb + q.n0 * (yy + q.n1 * zz);
+  int a0, a1, b0 = 0, b1 = 0;
+  if (xa >= 0 && xb < q.n0) {
+    a0 = row + xa;
+    a1 = row + xb + 1;
+  } else if (xa < 0) {
+    a0 = row + q.n0 - 1;
+    a1 = row + q.n0;
+    b0 = row;
+    b1 = row + xb + 1;
+  } else {
+    a0 = row + xa;
+    a1 = row + q.n0;
+    b0 = row;
+    b1 = row + 1;
+  }
+  const int sa = P.cell_start[a0], ea = P.cell_start[a1];
+  seg_s[2 * t] = sa;
+  seg_len[2 * t] = ea - sa;
+  if (b1 > b0) {
+    const int sb = P.cell_start[b0], eb = P.cell_start[b1];
+    seg_s[2 * t + 1] = sb;
+    seg_len[2 * t + 1] = eb - sb;
+  }
+}
+
+__device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
+  const int s0 = P.cell_start[c], e0 = P.cell_start[c + 1];
+  if (s0 >= e0) return;
+  // per-cell constants, computed once and shared (the divisions are costly
+  // on every thread: FP64 runs at a small fraction of the FP32 rate here)
+  __shared__ CellCtx qs;
+  __shared__ unsigned int cr_s[3];
+  __shared__ float h_s[3];
+  __shared__ int seg_s[18], seg_len[18], seg_p[19];
+  __shared__ int oct_n[8], oct_s[9], oct_c[8];
+  __shared__ unsigned short ord[kNbrMaxCell];
+  __shared__ unsigned char octof[kNbrMaxCell];
+  __shared__ int cnt[kNbrMaxCell];
+  __shared__ float4 stage[kOctChunk];
+  __shared__ unsigned short clist[8][kOctChunk];
+  __syncthreads();  // the previous cell of this CTA is done with the shared arrays
+  if (threadIdx.x == 0) {
+    const CellCtx q0 = cell_ctx(P, c, s0, e0);
+    qs = q0;
+    const RepState& r0 = P.rs[q0.r];
+    cr_s[0] = cell_centre_frac(q0.cx, q0.n0);
+    cr_s[1] = cell_centre_frac(q0.cy, q0.n1);
+    cr_s[2] = cell_centre_frac(q0.cz, q0.n2);
+    // octant boxes: half a cell wide, centred a quarter cell off the cell centre
+    h_s[0] = (float)(0.25 * r0.box[0] / q0.n0) + 1e-4f;
+    h_s[1] = (float)(0.25 * r0.box[1] / q0.n1) + 1e-4f;
+    h_s[2] = (float)(0.25 * r0.box[2] / q0.n2) + 1e-4f;
+  }
+  if (threadIdx.x < 8) oct_n[threadIdx.x] = 0;
+  __syncthreads();
+  const CellCtx q = qs;
+  const RepState& rs = P.rs[q.r];
+  const int nb = q.e - q.s;
+  if (nb > kNbrMaxCell) {
+    if (threadIdx.x == 0) atomicOr(&P.g->error, 2);
+    return;
+  }
+  copy_back<true, kOctThreads>(P, cur, q, rs);
+  stencil_rows(P, q, seg_s, seg_len);
+  const unsigned int crx = cr_s[0], cry = cr_s[1], crz = cr_s[2];
+  const float hx = h_s[0], hy = h_s[1], hz = h_s[2];
+  const float sx = rs.len_per_frac[0], sy = rs.len_per_frac[1], sz = rs.len_per_frac[2];
+  __syncthreads();
+  if (threadIdx.x == 0) {  // prefix sums over the 18 slots, empty ones dropped
+    int k = 0, acc = 0;
+    for (int t = 0; t < 18; ++t) {
+      if (seg_len[t] == 0) continue;
+      seg_s[k] = seg_s[t];
+      seg_p[k] = acc;
+      acc += seg_len[t];
+      ++k;
+    }
+    seg_p[k] = acc;
+    seg_len[0] = k;  // number of segments
+  }
+  // bucket the cell's beads by octant
+  for (int b = threadIdx.x; b < nb; b += kOctThreads) {
+    const uint4 m = P.mt[q.s + b];
+    const int o = ((int)(m.x - crx) >= 0 ? 1 : 0) | ((int)(m.y - cry) >= 0 ? 2 : 0) | ((int)(m.z - crz) >= 0 ? 4 : 0);
+    octof[b] = (unsigned char)o;
+    cnt[b] = 0;
+    atomicAdd(&oct_n[o], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int a = 0;
+    for (int o = 0; o < 8; ++o) {
+      oct_s[o] = a;
+      a += oct_n[o];
+      oct_n[o] = 0;
+    }
+    oct_s[8] = a;
+  }
+  __syncthreads();
+  unsigned int busy = 0;  // octants holding beads
+  for (int o = 0; o < 8; ++o)
+    if (oct_s[o + 1] > oct_s[o]) busy |= 1u << o;
+  for (int b = threadIdx.x; b < nb; b += kOctThreads) {
+    const int o = octof[b];
+    ord[oct_s[o] + atomicAdd(&oct_n[o], 1)] = (unsigned short)b;
+  }
+  const int nseg = seg_len[0];
+  const int M = seg_p[nseg];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned int below = (1u << lane) - 1u;
+  const int kmax = P.kmax;
+  const float lcut = P.tab->list_cut_f + 1e-4f;
+  const float lc2 = lcut * lcut;
+  // thin boxes (fewer than 3 cells on an axis) keep every candidate and take
+  // the minimum image per pair
+  const bool thin = q.n0 < 3 || q.n1 < 3 || q.n2 < 3;
+  const float bx = rs.len_per_frac[0] * 4294967296.0f, by = rs.len_per_frac[1] * 4294967296.0f,
+              bz = rs.len_per_frac[2] * 4294967296.0f;
+  for (int base = 0; base < M; base += kOctChunk) {
+    const int m = min(kOctChunk, M - base);
+    __syncthreads();
+    if (threadIdx.x < 8) oct_c[threadIdx.x] = 0;
+    __syncthreads();
+    for (int k0 = warp * 32; k0 < m; k0 += kOctThreads) {
+      const int k = k0 + lane;
+      unsigned int pass = 0;
+      if (k < m) {
+        const int j = seg_bead(seg_s, seg_p, nseg, base + k);
+        const uint4 mj = P.mt[j];
+        const float x = (float)(int)(mj.x - crx) * sx, y = (float)(int)(mj.y - cry) * sy,
+                    z = (float)(int)(mj.z - crz) * sz;
+        stage[k] = make_float4(x, y, z, __int_as_float(j));
+        if (thin) {
+          pass = busy;
+        } else {
+          // squared distance to the lower / upper half of the cell per axis
+          const float xl = fmaxf(fabsf(x + hx) - hx, 0.f), xu = fmaxf(fabsf(x - hx) - hx, 0.f);
+          const float yl = fmaxf(fabsf(y + hy) - hy, 0.f), yu = fmaxf(fabsf(y - hy) - hy, 0.f);
+          const float zl = fmaxf(fabsf(z + hz) - hz, 0.f), zu = fmaxf(fabsf(z - hz) - hz, 0.f);
+          const float x0 = xl * xl, x1 = xu * xu;
+          const float yz0 = yl * yl + zl * zl, yz1 = yu * yu + zl * zl, yz2 = yl * yl + zu * zu,
+                      yz3 = yu * yu + zu * zu;
+          pass = (x0 + yz0 < lc2 ? 1u : 0u) | (x1 + yz0 < lc2 ? 2u : 0u) | (x0 + yz1 < lc2 ? 4u : 0u) |
+                 (x1 + yz1 < lc2 ? 8u : 0u) | (x0 + yz2 < lc2 ? 16u : 0u) | (x1 + yz2 < lc2 ? 32u : 0u) |
+                 (x0 + yz3 < lc2 ? 64u : 0u) | (x1 + yz3 < lc2 ? 128u : 0u);
+          pass &= busy;
+        }
+      }
+#pragma unroll
+      for (int o = 0; o < 8; ++o) {
+        if (!(busy & (1u << o))) continue;
+        const unsigned int bal = __ballot_sync(0xffffffffu, (pass >> o) & 1u);
+        if (bal == 0) continue;
+        int at = 0;
+        if (lane == 0) at = atomicAdd(&oct_c[o], __popc(bal));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if ((pass >> o) & 1u) clist[o][at + __popc(bal & below)] = (unsigned short)k;
+      }
+    }
+    __syncthreads();
+    for (int t = warp; t < nb; t += kOctThreads / 32) {
+      const int b = ord[t];
+      const int o = octof[b];
+      const int nc = oct_c[o];
+      const unsigned short* cl = clist[o];
+      const int i = q.s + b;
+      const uint4 mi = P.mt[i];
+      const float xi = (float)(int)(mi.x - crx) * sx, yi = (float)(int)(mi.y - cry) * sy,
+                  zi = (float)(int)(mi.z - crz) * sz;
+      int count = cnt[b];
+      int* out = P.nbr + (size_t)i * kmax;
+      for (int k0 = 0; k0 < nc; k0 += 32) {
+        const int k = k0 + lane;
+        bool hit = false;
+        int j = 0;
+        if (k < nc) {
+          const float4 cj = stage[cl[k]];
+          float dx = xi - cj.x, dy = yi - cj.y, dz = zi - cj.z;
+          if (thin) {
+            dx -= bx * rintf(dx / bx);
+            dy -= by * rintf(dy / by);
+            dz -= bz * rintf(dz / bz);
+          }
+          j = __float_as_int(cj.w);
+          hit = (dx * dx + dy * dy + dz * dz < lc2) && (j != i);
+        }
+        const unsigned int hits = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+          const int slot = count + __popc(hits & below);
+          if (slot < kmax) out[slot] = j;
+        }
+        count += __popc(hits);
+      }
+      if (lane == 0) cnt[b] = count;
     }
   }
+  __syncthreads();
+  list_counts(P, q, cnt, kOctThreads);
+}
+
+__global__ void __launch_bounds__(kOctThreads) k_nbr_cells_oct(DevPtrs P, int cur) {
+  if (!P.g->rebuild) return;
+  list_build_begin(P);
+  for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) nbr_cell_oct(P, cur, c);
 }
 
 // ------------------------------------------------------------ the step
