@@ -48,7 +48,6 @@ struct smd_system {
   long long it = 0;         // current loop step
   bool at_measure = false;  // stopped after the second half-kick of step `it`
   bool pending_trial = false;
-  int pending_trial_slot = 0;
   bool ext_noise_pending = false;
   double skin = 0.5, dt = 0, half_skin = 0;
   bool barostat = false;
@@ -72,6 +71,16 @@ struct smd_system {
   std::vector<std::vector<double>> mc_fluct;  // per replica, every trial so far
   std::vector<std::vector<int>> mc_accept;
   std::vector<int> log_host;
+  // one MC period of the loop as a CUDA graph (per parity of the mirror
+  // buffer): the list build of each step is a conditional node, set by the
+  // previous step's last block, so idle rebuild kernels are never launched
+  struct PeriodGraph {
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;  // kernel nodes outside the conditional bodies
+  } graph[2];
+  bool use_graphs = true;
+  cudaStream_t side = nullptr;  // captures the conditional bodies
+  long long graph_builds = 0;   // device count of list builds run inside graphs
 
   template <typename T>
   int alloc(T** p, size_t count) {
@@ -87,6 +96,9 @@ struct smd_system {
   }
   ~smd_system() {
     if (stream) cudaStreamSynchronize(stream);
+    for (auto& g : graph)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (side) cudaStreamDestroy(side);
     for (cudaEvent_t e : prof_events) cudaEventDestroy(e);
     for (void* q : allocs) cudaFree(q);
     if (own_stream && stream) cudaStreamDestroy(stream);
@@ -117,24 +129,40 @@ int check_launch(smd_system* h) {
 
 __global__ void k_set_rebuild(Global* g, int v) { g->rebuild = v; }
 
+__global__ void k_set_counters(Global* g, long long it, int set_it, int slot, int set_slot) {
+  if (set_it) g->it = it;
+  if (set_slot) g->trial_slot = slot;
+}
+
+// First node of a period graph: the rebuild decision of the step before it.
+__global__ void k_graph_cond(const Global* g, unsigned long long cond) {
+  cudaGraphSetConditional((cudaGraphConditionalHandle)cond, g->rebuild ? 1u : 0u);
+}
+
 // The list kernels run only when the device flag asks for a rebuild.  API
 // calls outside the loop clear the flag afterwards; in the loop the step's
 // last block recomputes it from the displacement bound.
-int rebuild_if_needed(smd_system* h, bool clear_after = false) {
+int launch_rebuild(smd_system* h, cudaStream_t st, int cur, int in_graph) {
   auto& P = h->P;
   const int g = h->grid();
-  SMD_LAUNCH(h, k_bin<<<g, kBlock, 0, h->stream>>>(P, h->cur, h->mixed ? 1 : 0));
-  SMD_LAUNCH(h, k_scan_tiles<<<h->n_tiles, kBlock, 0, h->stream>>>(P));
-  SMD_LAUNCH(h, k_scan_sums<<<1, kBlock, 0, h->stream>>>(P, h->n_tiles));
-  SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, h->stream>>>(P));
+  SMD_LAUNCH(h, k_bin<<<g, kBlock, 0, st>>>(P, cur, h->mixed ? 1 : 0, in_graph));
+  SMD_LAUNCH(h, k_scan_tiles<<<h->n_tiles, kBlock, 0, st>>>(P));
+  SMD_LAUNCH(h, k_scan_sums<<<1, kBlock, 0, st>>>(P, h->n_tiles));
+  SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, st>>>(P));
   if (h->mixed) {
-    SMD_LAUNCH(h, k_reorder<true><<<g, kBlock, 0, h->stream>>>(P, h->cur));
-    SMD_LAUNCH(h, (k_nbr_cells_oct<<<h->nbr_grid(), kOctThreads, 0, h->stream>>>(P, h->cur)));
+    SMD_LAUNCH(h, k_reorder<true><<<g, kBlock, 0, st>>>(P, cur));
+    SMD_LAUNCH(h, (k_nbr_cells_oct<<<h->nbr_grid(), kOctThreads, 0, st>>>(P, cur)));
   } else {
-    SMD_LAUNCH(h, k_reorder<false><<<g, kBlock, 0, h->stream>>>(P, h->cur));
-    SMD_LAUNCH(h, (k_nbr_cells_plain<<<h->nbr_grid(), kNbrThreads, 0, h->stream>>>(P, h->cur)));
+    SMD_LAUNCH(h, k_reorder<false><<<g, kBlock, 0, st>>>(P, cur));
+    SMD_LAUNCH(h, (k_nbr_cells_plain<<<h->nbr_grid(), kNbrThreads, 0, st>>>(P, cur)));
   }
-  if (clear_after) SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 0));
+  return 0;
+}
+constexpr int kRebuildKernels = 6;
+
+int rebuild_if_needed(smd_system* h, bool clear_after = false) {
+  if (int rc = launch_rebuild(h, h->stream, h->cur, 0)) return rc;
+  if (clear_after) SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(h->P.g, 0));
   return 0;
 }
 
@@ -171,7 +199,7 @@ int prof_mark(smd_system* h) {
 }
 
 template <int FL>
-int launch_step(smd_system* h) {
+int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   auto& P = h->P;
   const int g = h->grid();
   constexpr bool kLoopStep = (FL & (F_FORCES | F_ENERGY | F_INIT)) == 0;
@@ -181,10 +209,10 @@ int launch_step(smd_system* h) {
   const int gl = h->grid_lanes();
   if (h->mixed) {
     SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
-    SMD_LAUNCH(h, (k_integ<true, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, h->it)));
+    SMD_LAUNCH(h, (k_integ<true, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, se)));
   } else {
     SMD_LAUNCH(h, (k_force<false, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
-    SMD_LAUNCH(h, (k_integ<false, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, h->it)));
+    SMD_LAUNCH(h, (k_integ<false, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, se)));
   }
   if (kLoopStep && h->profile) {
     if (int rc = prof_mark(h)) return rc;
@@ -192,13 +220,13 @@ int launch_step(smd_system* h) {
   return 0;
 }
 
-int launch_finish(smd_system* h, int do_second, int apply_mc) {
+int launch_finish(smd_system* h, int do_second, int apply_mc, StepEnd se) {
   auto& P = h->P;
   const int g = h->grid();
   if (h->mixed)
-    SMD_LAUNCH(h, k_finish<true><<<g, kBlock, 0, h->stream>>>(P, h->cur, do_second, apply_mc));
+    SMD_LAUNCH(h, k_finish<true><<<g, kBlock, 0, h->stream>>>(P, h->cur, do_second, apply_mc, se));
   else
-    SMD_LAUNCH(h, k_finish<false><<<g, kBlock, 0, h->stream>>>(P, h->cur, do_second, apply_mc));
+    SMD_LAUNCH(h, k_finish<false><<<g, kBlock, 0, h->stream>>>(P, h->cur, do_second, apply_mc, se));
   h->cur ^= 1;
   return 0;
 }
@@ -246,6 +274,7 @@ int stage_trials(smd_system* h, long long from, int steps) {
   // pageable source: the copy is staged before cudaMemcpyAsync returns
   SMD_CUDA(cudaMemcpyAsync(h->P.trial_u, h->trial_host.data(), h->trial_host.size() * sizeof(double),
                            cudaMemcpyHostToDevice, h->stream));
+  SMD_LAUNCH(h, k_set_counters<<<1, 1, 0, h->stream>>>(h->P.g, 0, 0, 0, 1));
   h->trials_staged = count;
   h->trials_used = 0;
   return 0;
@@ -255,9 +284,9 @@ int complete_pending(smd_system* h) {
   if (!h->at_measure) return 0;
   const int apply = h->pending_trial ? 1 : 0;
   if (h->pending_trial) {
-    SMD_LAUNCH(h, k_mc<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P, h->pending_trial_slot));
+    SMD_LAUNCH(h, k_mc<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P));
   }
-  int rc = launch_finish(h, 0, apply);
+  int rc = launch_finish(h, 0, apply, StepEnd{0, 0, 1, apply, 0});
   if (rc) return rc;
   h->at_measure = false;
   h->pending_trial = false;
@@ -269,6 +298,7 @@ int read_error(smd_system* h) {
   Global g;
   SMD_CUDA(cudaMemcpyAsync(&g, h->P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
+  h->graph_builds = g.graph_builds;
   if (g.error & 2) return fail(8, "a Verlet-list cell holds more than 1024 beads (collapsed system)");
   if (g.error & 1) {
     char buf[256];
@@ -567,6 +597,9 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   g.need_nbr = 0;
   g.rebuild = 1;
   g.n_rebuilds = 0;
+  g.it = h->it;
+  g.trial_slot = 0;
+  g.graph_builds = 0;
   SMD_CUDA(cudaMemcpy(P.g, &g, sizeof(Global), cudaMemcpyHostToDevice));
   if ((rc = rebuild_if_needed(h.get()))) return rc;
   if ((rc = read_error(h.get()))) return rc;
@@ -784,6 +817,7 @@ int smd_set_noise_once(smd_system* h, const double* psi) {
 
 int smd_prepare(smd_system* h, int do_second, smd_energy* energy_out) {
   if (!h) return fail(1, "null handle");
+  SMD_LAUNCH(h, k_set_counters<<<1, 1, 0, h->stream>>>(h->P.g, h->it, 1, 0, 0));
   int rc = force_rebuild(h);
   if (rc) return rc;
   if (h->ext_noise_pending) {
@@ -794,11 +828,92 @@ int smd_prepare(smd_system* h, int do_second, smd_energy* energy_out) {
   }
   if (rc) return rc;
   if (energy_out && (rc = smd_compute_energy(h, energy_out))) return rc;
-  if ((rc = launch_finish(h, do_second ? 1 : 0, 0))) return rc;
+  if ((rc = launch_finish(h, do_second ? 1 : 0, 0, StepEnd{0, 0, 0, 0, 0}))) return rc;
   h->at_measure = false;
   h->it = h->first_step[0];
+  SMD_LAUNCH(h, k_set_counters<<<1, 1, 0, h->stream>>>(h->P.g, h->it, 1, 0, 0));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
   return read_error(h);
+}
+
+// Captures one MC period (resize_rate steps, the trial step last) as a graph
+// for mirror parity cur0.  Step s: IF(rebuild) { list build } then the step
+// kernels; the kernel completing step s sets the condition of step s+1.
+int capture_period(smd_system* h, int cur0) {
+  const int G = h->resize_rate;
+  auto& P = h->P;
+  if (!h->side) SMD_CUDA(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+  const long saved_launches = h->launches;
+  const int saved_cur = h->cur;
+  cudaStream_t st = h->stream;
+  SMD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  int rc = 0;
+  cudaGraph_t graph = nullptr;
+  auto body = [&]() -> int {
+    cudaStreamCaptureStatus status;
+    SMD_CUDA(cudaStreamGetCaptureInfo(st, &status, nullptr, &graph, nullptr, nullptr, nullptr));
+    std::vector<cudaGraphConditionalHandle> cond(G);
+    for (int k = 0; k < G; ++k) SMD_CUDA(cudaGraphConditionalHandleCreate(&cond[k], graph, 0, 0));
+    SMD_LAUNCH(h, k_graph_cond<<<1, 1, 0, st>>>(P.g, (unsigned long long)cond[0]));
+    for (int k = 0; k < G; ++k) {
+      const int cur = cur0 ^ (k & 1);
+      const cudaGraphNode_t* deps = nullptr;
+      size_t ndeps = 0;
+      SMD_CUDA(cudaStreamGetCaptureInfo(st, &status, nullptr, &graph, &deps, nullptr, &ndeps));
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = cond[k];
+      cp.conditional.type = cudaGraphCondTypeIf;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node;
+      SMD_CUDA(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp));
+      cudaGraph_t build = cp.conditional.phGraph_out[0];
+      SMD_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+      SMD_CUDA(cudaStreamBeginCaptureToGraph(h->side, build, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      const int rc1 = launch_rebuild(h, h->side, cur, 1);
+      SMD_CUDA(cudaStreamEndCapture(h->side, &build));
+      if (rc1) return rc1;
+      h->cur = cur;
+      const bool last = (k == G - 1);
+      const StepEnd se{last ? 0ull : (unsigned long long)cond[k + 1], last ? 0 : 1, 1, 0, 0};
+      if (last && h->barostat) {
+        SMD_LAUNCH(h, k_trial<<<(h->n_rep + 63) / 64, 64, 0, st>>>(P));
+        if (int r = launch_step<F_STOP | F_DU>(h)) return r;
+        SMD_LAUNCH(h, k_mc<<<(h->n_rep + 63) / 64, 64, 0, st>>>(P));
+        if (int r = launch_finish(h, 0, 1, StepEnd{0, 0, 1, 1, 0})) return r;
+      } else {
+        if (int r = launch_step<0>(h, se)) return r;
+      }
+    }
+    return 0;
+  };
+  rc = body();
+  cudaGraph_t done = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(st, &done);
+  h->cur = saved_cur;
+  const long kernels = h->launches - saved_launches - (long)G * kRebuildKernels;
+  h->launches = saved_launches;
+  if (rc) {
+    if (done) cudaGraphDestroy(done);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(100 + (int)e, std::string("graph capture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e2 = cudaGraphInstantiate(&exec, done, 0);
+  cudaGraphDestroy(done);
+  if (e2 != cudaSuccess) return fail(100 + (int)e2, std::string("graph instantiate: ") + cudaGetErrorString(e2));
+  h->graph[cur0].exec = exec;
+  h->graph[cur0].kernels = (int)kernels;
+  return 0;
+}
+
+// A period graph can run from step `it` when its trial step (the last) is a
+// barostat step of the reference loop, i.e. it % resize_rate == 1.
+bool graph_fits(const smd_system* h, long long it, int left) {
+  const int G = h->resize_rate;
+  if (!h->use_graphs || h->profile || h->ext_noise_pending || G < 2 || (G & 1) || left < G) return false;
+  if (h->stream == nullptr) return false;  // the legacy stream cannot be captured
+  return (it % G) == 1;
 }
 
 int smd_advance(smd_system* h, int steps, int flags) {
@@ -812,6 +927,18 @@ int smd_advance(smd_system* h, int steps, int flags) {
     const int chunk = std::min(steps - done, kTrialChunk * std::max(1, h->resize_rate) / 2);
     if ((rc = stage_trials(h, h->it, chunk))) return rc;
     for (int s = 0; s < chunk; ++s) {
+      // the last step of a stopping call runs alone (it stops after its second half-kick)
+      const int left = chunk - s - ((stop_at_measure && done + chunk == steps) ? 1 : 0);
+      if (graph_fits(h, h->it, left)) {
+        auto& g = h->graph[h->cur];
+        if (!g.exec && (rc = capture_period(h, h->cur))) return rc;
+        SMD_CUDA(cudaGraphLaunch(g.exec, h->stream));
+        h->launches += g.kernels;
+        h->it += h->resize_rate;
+        if (h->barostat) h->trials_used++;
+        s += h->resize_rate - 1;
+        continue;
+      }
       if ((rc = rebuild_if_needed(h))) return rc;
       const bool trial = is_trial_step(h, h->it);
       const bool stop = stop_at_measure && (done + s == steps - 1);
@@ -824,10 +951,9 @@ int smd_advance(smd_system* h, int steps, int flags) {
         h->it++;
         continue;
       }
-      int slot = 0;
       if (trial) {
-        slot = h->trials_used++;
-        SMD_LAUNCH(h, k_trial<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P, slot));
+        h->trials_used++;
+        SMD_LAUNCH(h, k_trial<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P));
         rc = ext ? launch_step<F_STOP | F_DU | F_EXTNOISE>(h) : launch_step<F_STOP | F_DU>(h);
       } else {
         rc = ext ? launch_step<F_STOP | F_EXTNOISE>(h) : launch_step<F_STOP>(h);
@@ -835,7 +961,6 @@ int smd_advance(smd_system* h, int steps, int flags) {
       if (rc) return rc;
       h->at_measure = true;
       h->pending_trial = trial;
-      h->pending_trial_slot = slot;
       if (stop) break;
       if ((rc = complete_pending(h))) return rc;
     }
@@ -911,7 +1036,8 @@ int smd_last_timing(smd_system* h, double* ms, long* step_launches, long* launch
   if (!h) return fail(1, "null handle");
   if (ms) *ms = h->step_ms;
   if (step_launches) *step_launches = h->step_launches;
-  if (launches) *launches = h->launches;
+  // list-build kernels that ran inside graph conditional bodies count too
+  if (launches) *launches = h->launches + (long)(h->graph_builds * kRebuildKernels);
   return 0;
 }
 

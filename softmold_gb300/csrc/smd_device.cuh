@@ -79,6 +79,19 @@ struct Global {  // single instance
   int rebuild;                 // 1: rebuild the Verlet list before the next force pass
   int error;                   // bit 0: list overflow, bit 1: cell overflow (>kMaxCell)
   int need_nbr;                // largest neighbour count seen on overflow
+  int trial_slot;              // staged barostat trial used by the next MC step
+  long long it;                // loop step (the Langevin noise key); advanced by the step's last kernel
+  long long graph_builds;      // list builds run inside graph conditional bodies
+};
+
+// Bookkeeping of the kernel that completes a step (its last block): advance
+// the step counter and the trial slot, and in a graph hand the rebuild
+// decision to the next step's conditional node.
+struct StepEnd {
+  unsigned long long cond;  // cudaGraphConditionalHandle of the next step's rebuild node
+  int set_cond;
+  int advance_it;
+  int advance_slot;
   int pad;
 };
 

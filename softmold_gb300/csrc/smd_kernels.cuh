@@ -28,7 +28,7 @@ enum StepFlags {
 // (a pair now inside rc was then inside rc + skin); accepted box moves use up
 // (rc + skin)|s - 1| of that margin each.  Decides whether the Verlet list
 // must be rebuilt before the next force pass.
-__device__ __forceinline__ void finalize_step(const DevPtrs& P, float dmax_block) {
+__device__ __forceinline__ void finalize_step(const DevPtrs& P, float dmax_block, StepEnd se) {
   __shared__ bool last;
   if (threadIdx.x == 0) {
     if (dmax_block > 0.f) atomicMax(&P.g->dmax_bits, __float_as_uint(dmax_block));
@@ -44,8 +44,12 @@ __device__ __forceinline__ void finalize_step(const DevPtrs& P, float dmax_block
     const double slack = P.g->slack + __longlong_as_double((long long)sb);
     P.g->slack = slack;
     P.g->last_disp = dmax;
-    P.g->rebuild = ((double)dmax + slack > P.half_skin) ? 1 : 0;
+    const int rebuild = ((double)dmax + slack > P.half_skin) ? 1 : 0;
+    P.g->rebuild = rebuild;
+    if (se.advance_it) P.g->it++;
+    if (se.advance_slot) P.g->trial_slot++;
     P.g->blocks_done = 0u;
+    if (se.set_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)se.cond, (unsigned int)rebuild);
   }
 }
 
@@ -62,9 +66,10 @@ __device__ __forceinline__ float displacement(uint4 ref, unsigned int fx, unsign
 // ------------------------------------------------------------ list build
 // Verlet-list cell of bead i from its 32-bit fractional coordinates: the
 // cell index along an axis is floor(f * n / 2^32), always in [0, n).
-__global__ void __launch_bounds__(kBlock) k_bin(DevPtrs P, int cur, int mixed) {
+__global__ void __launch_bounds__(kBlock) k_bin(DevPtrs P, int cur, int mixed, int in_graph) {
   if (!P.g->rebuild) return;
   const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (in_graph && i == 0) P.g->graph_builds++;
   if (i >= P.n) return;
   const int r = rep_of(P, i);
   const RepState& rs = P.rs[r];
@@ -977,7 +982,8 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
 // position mirror for the next force pass.  Flags select the stopped,
 // start-up, force-only and energy-only variants.
 template <bool MIXED, int FL>
-__global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, long long it) {
+__global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se) {
+  const long long it = P.g->it;
   const Tables& T = *P.tab;
   const int i = blockIdx.x * kBlock + threadIdx.x;
   const bool active = i < P.n;
@@ -1142,12 +1148,13 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, long long 
     float bm = 0.f;
     if (threadIdx.x == 0)
       for (int w = 0; w < kBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
-    finalize_step(P, bm);
+    finalize_step(P, bm, se);
   }
 }
 
 // Barostat trial box for every replica (MD.cpp:593-611).
-__global__ void k_trial(DevPtrs P, int trial) {
+__global__ void k_trial(DevPtrs P) {
+  const int trial = P.g->trial_slot;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= P.n_rep) return;
   RepState& rs = P.rs[r];
@@ -1173,7 +1180,8 @@ __global__ void k_trial(DevPtrs P, int trial) {
 }
 
 // Metropolis decision (MD.cpp:677-720).
-__global__ void k_mc(DevPtrs P, int trial) {
+__global__ void k_mc(DevPtrs P) {
+  const int trial = P.g->trial_slot;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= P.n_rep) return;
   RepState& rs = P.rs[r];
@@ -1206,7 +1214,7 @@ __global__ void k_mc(DevPtrs P, int trial) {
 // Completes a stopped step: optional restart half-kick, optional box rescale
 // of an accepted MC move, then the next step's first half-kick and drift.
 template <bool MIXED>
-__global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_second, int apply_mc) {
+__global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_second, int apply_mc, StepEnd se) {
   const int i = blockIdx.x * kBlock + threadIdx.x;
   float vmax = 0.f;
   if (i < P.n) {
@@ -1258,7 +1266,7 @@ __global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_se
   float bm = 0.f;
   if (threadIdx.x == 0)
     for (int w = 0; w < kBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
-  finalize_step(P, bm);
+  finalize_step(P, bm, se);
 }
 
 // Mirror of the current positions in the other buffer (after set_state or a
