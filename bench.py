@@ -14,13 +14,15 @@ CUDA events on the library's stream.  `e2e` runs the same metric through the C
 ABI with host buffers: per e2e step the state is uploaded, 48 iterations are
 advanced, the energies are measured and the state is read back.
 
-Other workloads (--workload): vesicle5k (15,000-bead vesicle, no barostat) and
+Other workloads (--workload): vesicle5k (15,000-bead vesicle, no barostat),
 batch64 (64 independent bilayers of 1,000-8,000 lipids and tension 0-1, one
-handle, one set of launches per step).  Under torchrun every rank runs its own
+handle, one set of launches per step), sphere80k (240,001-bead vesicle with a
+continuum sphere) and adjoint10k (gradient of a 200-step window of a
+30,000-bead bilayer: forward, recompute and backward passes).  Under torchrun every rank runs its own
 copy of the workload (weak scaling, no data-path collective).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload bilayer20k|vesicle5k|batch64]
+                  [--workload bilayer20k|vesicle5k|batch64|sphere80k|adjoint10k]
 """
 from __future__ import annotations
 
@@ -68,6 +70,21 @@ def workload(args, rank, tmpdir):
         smd.synth_vesicle(path, 1000 + rank, 5000, 3.45, 60.0)
         cfg = {"workload": "vesicle, 5,000 3-bead lipids (15,000 beads), 60^3 box, kT 3, gamma 1, dt 0.02"}
         paths = [path]
+    elif args.workload == "sphere80k":
+        path = os.path.join(tmpdir, f"bench{rank}.mpd")
+        # sphere radius 5, surface 2 sigma outside the outer heads; head well depth 10 with a
+        # repulsive core (Umax 100: the generator default of 10 lets heads collapse into the core)
+        smd.synth_vesicle_sphere(path, 1000 + rank, 80000, 3.45, 190.0, 5.0, -10.0, 100.0, 2.0)
+        cfg = {"workload": "vesicle of 80,000 3-bead lipids (240,001 beads with the sphere), 190^3 box, one "
+                           "continuum sphere R 5 sigma 2 sigma outside the outer heads (head well depth 10, "
+                           "range 2), kT 3, gamma 1, dt 0.02"}
+        paths = [path]
+    elif args.workload == "adjoint10k":
+        path = os.path.join(tmpdir, f"bench{rank}.mpd")
+        smd.synth_bilayer(path, 1000 + rank, 10000, 3.45, 15.0, 0.0, 0.0)
+        cfg = {"workload": "adjoint of a 200-step window (checkpoints every 20) of a flat bilayer of 10,000 "
+                           "3-bead lipids (30,000 beads), box fixed, kT 3, gamma 1, dt 0.02"}
+        paths = [path]
     elif args.workload == "batch64":
         rng = np.random.default_rng(64 + 1000 * rank)
         lipids = rng.integers(1000, 8001, size=64)
@@ -87,16 +104,54 @@ def workload(args, rank, tmpdir):
 
 
 class ClockSampler:
+    """SM clocks and throttle reasons sampled during the timed region: NVML
+    (read-only queries through ctypes) every 20 ms, else nvidia-smi every 200 ms."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReasons bits
+    REASONS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+               "hw_thermal_slowdown": 0x40, "hw_power_brake_slowdown": 0x80}
 
     def __init__(self, device_index):
         self.dev = device_index
         self.proc = None
+        self.nvml = None
         self.lines = []
+        self.samples = []  # (sm_mhz, sm_max_mhz, reason bits)
+        self.halt = threading.Event()
+
+    def _nvml_open(self):
+        import ctypes as C
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return False
+        if lib.nvmlInit_v2() != 0:
+            return False
+        h = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.dev), C.byref(h)) != 0:
+            return False
+        self.reason_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.nvml, self.handle, self.C = lib, h, C
+        return True
+
+    def _nvml_loop(self):
+        C, lib, h = self.C, self.nvml, self.handle
+        sm, smax, bits = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while not self.halt.is_set():
+            if (lib.nvmlDeviceGetClockInfo(h, 1, C.byref(sm)) == 0 and
+                    lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(smax)) == 0 and
+                    self.reason_fn(h, C.byref(bits)) == 0):
+                self.samples.append((float(sm.value), float(smax.value), int(bits.value)))
+            self.halt.wait(0.02)
 
     def start(self):
+        if self._nvml_open():
+            self.t = threading.Thread(target=self._nvml_loop, daemon=True)
+            self.t.start()
+            return
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -106,11 +161,23 @@ class ClockSampler:
         except OSError:
             self.proc = None
 
+    def started(self):
+        return bool(self.samples or self.lines)
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def stop(self):
+        if self.nvml is not None:
+            self.halt.set()
+            self.t.join(timeout=2)
+            self.nvml.nvmlShutdown()
+            sm = [s[0] for s in self.samples]
+            reasons = sorted({k for s in self.samples for k, b in self.REASONS.items() if s[2] & b})
+            return {"sm_mhz": statistics.median(sm) if sm else None,
+                    "sm_max_mhz": max(s[1] for s in self.samples) if sm else None,
+                    "reasons": reasons, "samples": len(sm), "source": "nvml, 20 ms"}
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -133,7 +200,7 @@ class ClockSampler:
                 if val.lower() == "active":
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
 def cpu_baseline(path, threads, target_s=12.0):
@@ -144,8 +211,12 @@ def cpu_baseline(path, threads, target_s=12.0):
     lib.orc_md_time.restype = C.c_double
     name = path[:-4].encode()
     t = lib.orc_md_time(name, threads, 4)
+    if t < 0:
+        raise RuntimeError(f"the oracle could not run {path}")
     steps = max(4, int(4 * target_s / max(t, 1e-3)))
     t = lib.orc_md_time(name, threads, steps)
+    if t < 0:
+        raise RuntimeError(f"the oracle could not run {path}")
     return steps, t
 
 
@@ -189,6 +260,36 @@ def run_reference(args, rank, world):
         }), flush=True)
 
 
+def bench_adjoint(args, s, stream, n, cfg, world, rank, dist):
+    """One bench step = smd_adjoint over a 200-step window, checkpoints every
+    20 (forward, recompute and backward passes); value = beads x window steps
+    per second of that call."""
+    import torch
+    T, ck = 200, 20
+    for _ in range(args.warmup):
+        s.adjoint(T, ck, segment_local=True)
+    torch.cuda.synchronize()
+    times, grads = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = s.adjoint(T, ck, segment_local=True)
+        times.append(time.perf_counter() - t0)
+        grads.append(r["grad"].tolist())
+    tot = sum(times)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "adjoint bead-steps/s on 1 GB300 (mixed, 200-step window, checkpoint every 20)",
+            "value": n * T * args.steps / tot, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair terms, f64 adjoint", "data": "synthetic",
+            "config": cfg, "segment_local_grad_last": grads[-1],
+            "note": "host wall clock around smd_adjoint (it synchronises); the reference has no adjoint"}),
+            flush=True)
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -199,6 +300,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--skin", type=float, default=0.5)
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch the step kernels one by one (for profilers that cannot see kernels in graphs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -228,11 +331,15 @@ def main():
     stream = torch.cuda.Stream()
     s = smd.System(m, precision=smd.MIXED, skin=args.skin)
     s.set_stream(stream.cuda_stream)
+    if args.no_graphs:
+        s.use_graphs(False)
     s.prepare()
     s.advance(1001)  # equilibration from the lattice start (untimed); leaves step % PERIOD == 1
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     K, W = args.steps, args.warmup
+    if args.workload == "adjoint10k":
+        return bench_adjoint(args, s, stream, n, cfg, world, rank, dist)
 
     def timed_loop(sys_, steps):
         """`steps` bench steps of PERIOD MD steps each, L2 flushed before each."""
@@ -259,7 +366,7 @@ def main():
     sampler = ClockSampler(local)
     sampler.start()
     t_wait = time.time()
-    while not sampler.lines and time.time() - t_wait < 5:  # NVML start-up outside the timed region
+    while not sampler.started() and time.time() - t_wait < 5:  # sampler start-up outside the timed region
         time.sleep(0.05)
     torch.cuda.nvtx.range_push("timed")
     total_ms, launches = timed_loop(s, K)
@@ -281,10 +388,11 @@ def main():
 
     # FP64 plain form on the same state, and the mixed form's force error
     pos, vel = s.state()
+    boxes = [s.box(r) for r in range(len(ms))]  # the boxes of this state (the e2e run below moves them on)
     p = smd.System(m, precision=smd.PLAIN_FP64, skin=args.skin)
     p.set_stream(stream.cuda_stream)
     for r in range(len(ms)):
-        p.set_box(s.box(r), r)
+        p.set_box(boxes[r], r)
     p.set_state(pos, vel)
     f_plain = p.forces()
     f_mixed = s.forces()
@@ -349,7 +457,7 @@ def main():
         for r in sample:
             ck = os.path.join(tmp, f"cpu{r}.mpd")
             a, b = offs[r], offs[r + 1]
-            smd.mpd_update_state(paths[r], ck, pos[a:b], vel[a:b], s.box(r), 0.0)
+            smd.mpd_update_state(paths[r], ck, pos[a:b], vel[a:b], boxes[r], 0.0)
             st, t_ = cpu_baseline(ck, threads, target_s=12.0 / len(sample))
             units += (b - a) * st
             secs += t_

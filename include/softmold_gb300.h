@@ -148,6 +148,13 @@ int smd_prepare(smd_system* h, int do_second, smd_energy* energy_out);
 #define SMD_ASYNC 2
 int smd_advance(smd_system* h, int steps, int flags);
 
+/* Launch mode of smd_advance: on = 1 (default) runs each barostat period as
+ * one CUDA graph whose list builds are conditional nodes; on = 0 launches the
+ * same kernels one by one (profilers that cannot see kernel nodes inside
+ * graphs with conditional nodes still see each kernel).  No reference
+ * counterpart: the reference launches nothing. */
+int smd_use_graphs(smd_system* h, int on);
+
 /* Waits for the handle's stream and reports any device-side error. */
 int smd_sync(smd_system* h);
 
@@ -214,6 +221,47 @@ int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double ar
 #define SMD_STATIC_MAX_CELLS 32768
 int smd_pair_forces_static(const double* d_pos, const int* d_type, int n, const double box[3], double cutoff,
                            int n_types, const double* d_fconst, double* d_force, void* stream);
+
+/* Gradient of a time average with respect to potential constants (no
+ * reference counterpart: the reference computes no derivatives).  From the
+ * handle's current state (x_1, h_1), h the half-step velocity, the observable
+ * J = (1/T) sum_{n=1..T} U(x_n), U the pair + CHAIN potential at the
+ * positions where step n evaluates its forces, is differentiated through T
+ * loop steps (MD.cpp:335-729) with the Langevin noise fixed by its seed and
+ * the box fixed (barostat off).  The forward pass stores the state every
+ * checkpoint_every steps; the backward pass recomputes each segment and runs
+ * the discrete adjoint of the step (Hessian-vector products over the Verlet
+ * list, FP32 pair terms in the mixed form, FP64 accumulation).  Parameters:
+ * Umin of the type pair umin_types (both ordered table rows,
+ * include/potentials/laradjiRevalee.h:84-152), and kbond and kbend, the CHAIN
+ * constants 1 and 3 of every CHAIN residue.  Afterwards the handle holds the
+ * state after the T steps, as smd_advance(h, T, 0) leaves it.  Single-system
+ * handles without BEAD residues. */
+typedef struct smd_adjoint_spec {
+  int steps;             /* T >= 1 */
+  int checkpoint_every;  /* >= 1 */
+  int umin_types[2];     /* type pair (a, b) of the Umin parameter */
+  int segment_local;     /* 0: the exact derivative of J; 1: each segment's
+                            terms differentiated through that segment only
+                            (the adjoint state restarts at every checkpoint),
+                            which stays bounded where the exact derivative of
+                            a long window grows exponentially (chaotic runs) */
+} smd_adjoint_spec;
+
+typedef struct smd_adjoint_result {
+  double mean_potential;       /* J */
+  double grad[3];              /* dJ/dUmin(a,b), dJ/dkbond, dJ/dkbend */
+  double mean_area_per_lipid;  /* box_x box_y / (CHAIN molecules / 2) */
+  double grad_area[3];         /* 0: the box does not depend on the constants here */
+} smd_adjoint_result;
+
+int smd_adjoint(smd_system* h, const smd_adjoint_spec* spec, smd_adjoint_result* out);
+
+/* K w with K = dF/dx the Jacobian of the conservative pair + CHAIN forces at
+ * the current positions (minus the Hessian of U), w and kw n*3 in file order.
+ * The product the adjoint step uses; exposed to check it against finite
+ * differences of the forces. */
+int smd_hessian_vector(smd_system* h, const double* w, double* kw);
 
 /* Rewrites the .mpd at in_path with new positions, velocities, box and
  * initialTime into out_path (the store of MD.cpp:373-377). */

@@ -53,6 +53,16 @@ class McStats(C.Structure):
 
 _lib = None
 
+class AdjointSpec(C.Structure):
+    _fields_ = [("steps", C.c_int), ("checkpoint_every", C.c_int), ("umin_types", C.c_int * 2),
+                ("segment_local", C.c_int)]
+
+
+class AdjointResult(C.Structure):
+    _fields_ = [("mean_potential", C.c_double), ("grad", C.c_double * 3), ("mean_area_per_lipid", C.c_double),
+                ("grad_area", C.c_double * 3)]
+
+
 # name -> (restype, argtypes); every function declared in the header
 _SIGS = {
     "smd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
@@ -80,6 +90,9 @@ _SIGS = {
     "smd_last_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "smd_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "smd_sync": (C.c_int, [C.c_void_p]),
+    "smd_use_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+    "smd_adjoint": (C.c_int, [C.c_void_p, C.POINTER(AdjointSpec), C.POINTER(AdjointResult)]),
+    "smd_hessian_vector": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "smd_mpd_update_state": (C.c_int, [C.c_char_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
     "smd_rebuild_count": (C.c_long, [C.c_void_p]),
     "smd_list_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -258,6 +271,9 @@ class System:
                         uc=np.ascontiguousarray(m.uconst, np.float64),
                         cb=np.ascontiguousarray(m.chain_blocks, np.int32),
                         cc=np.ascontiguousarray(m.chain_consts, np.float64))
+            if m.sphere_index is not None and len(m.sphere_index) > 0:
+                arrs["si"] = np.ascontiguousarray(m.sphere_index, np.int32)
+                arrs["sc"] = np.ascontiguousarray(m.sphere_consts, np.float64)
             self._keep.append(arrs)
             d = descs[k]
             d.n = len(m.type)
@@ -269,7 +285,11 @@ class System:
             d.fconst, d.uconst = _dp(arrs["fc"]), _dp(arrs["uc"])
             d.n_chain_blocks = len(arrs["cb"])
             d.chain_blocks, d.chain_consts = _ip(arrs["cb"]), _dp(arrs["cc"])
-            d.n_spheres = 0
+            if "si" in arrs:
+                d.n_spheres = len(arrs["si"])
+                d.sphere_index, d.sphere_consts = _ip(arrs["si"]), _dp(arrs["sc"])
+            else:
+                d.n_spheres = 0
             d.dt, d.gamma, d.temperature = m.dt, m.gamma, m.temperature
             d.seed = m.seed & 0xffffffff
             d.tension, d.delta_lxy = m.tension, m.delta_lxy
@@ -355,6 +375,25 @@ class System:
 
     def sync(self):
         _check(lib().smd_sync(self.h), "smd_sync")
+
+    def adjoint(self, steps, checkpoint_every=20, umin_types=(3, 3), segment_local=False):
+        """smd_adjoint: J = mean potential over the next `steps` loop steps and
+        dJ/d(Umin(a,b), kbond, kbend); the handle ends `steps` steps later."""
+        spec = AdjointSpec(int(steps), int(checkpoint_every), (C.c_int * 2)(*umin_types),
+                           1 if segment_local else 0)
+        res = AdjointResult()
+        _check(lib().smd_adjoint(self.h, C.byref(spec), C.byref(res)), "smd_adjoint")
+        return dict(mean_potential=res.mean_potential, grad=np.array(res.grad[:]),
+                    mean_area_per_lipid=res.mean_area_per_lipid, grad_area=np.array(res.grad_area[:]))
+
+    def hessian_vector(self, w):
+        ww = np.ascontiguousarray(w, np.float64)
+        out = np.zeros((self.n, 3))
+        _check(lib().smd_hessian_vector(self.h, ww.ctypes.data, out.ctypes.data), "smd_hessian_vector")
+        return out
+
+    def use_graphs(self, on=True):
+        _check(lib().smd_use_graphs(self.h, 1 if on else 0), "smd_use_graphs")
 
     def profile(self, on=True):
         _check(lib().smd_profile(self.h, 1 if on else 0), "smd_profile")

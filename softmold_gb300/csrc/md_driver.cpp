@@ -44,15 +44,24 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   // residues on the device path
   std::vector<int> blocks;
   std::vector<double> consts;
+  std::vector<int> sphere_idx;
+  const std::vector<double>* sphere_consts = nullptr;
   for (const smd::Molecule& m : S.mol) {
     if (m.type == smd::MOL_CHAIN) {
       for (const auto& b : m.bonds) {
         blocks.insert(blocks.end(), {b[0], b[1], b[2]});
         consts.insert(consts.end(), m.constants.begin(), m.constants.begin() + 4);
       }
+    } else if (m.type == smd::MOL_BEAD) {
+      if (sphere_consts) {
+        std::cout << "Error(MD): more than one BEAD residue is not on the GPU step of this build\n";
+        return 1;
+      }
+      for (const auto& b : m.bonds) sphere_idx.push_back(b[0]);
+      sphere_consts = &m.constants;
     } else if (m.type != smd::MOL_SOLID) {
       std::cout << "Error(MD): molecule type " << m.type
-                << " is not on the GPU step of this build (supported: CHAIN)\n";
+                << " is not on the GPU step of this build (supported: CHAIN, BEAD)\n";
       return 1;
     }
   }
@@ -95,6 +104,9 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   d.n_chain_blocks = (int)blocks.size() / 3;
   d.chain_blocks = blocks.data();
   d.chain_consts = consts.data();
+  d.n_spheres = (int)sphere_idx.size();
+  d.sphere_index = sphere_idx.data();
+  d.sphere_consts = sphere_consts ? sphere_consts->data() : nullptr;
   d.dt = S.deltaT;
   d.gamma = gamma;
   d.temperature = S.initialTemp;

@@ -12,7 +12,7 @@
 
 #include "../../include/softmold_gb300.h"
 #include "mt19937.h"
-#include "smd_kernels.cuh"
+#include "smd_adjoint.cuh"
 
 namespace {
 
@@ -31,6 +31,7 @@ int fail(int code, const std::string& msg) {
   } while (0)
 
 constexpr int kTrialChunk = 1024;  // barostat trials staged per upload
+constexpr int kBeadRadiusConst = 4;  // BEADRADIUS: the radius within a BEAD constant row
 
 }  // namespace
 
@@ -44,6 +45,16 @@ void set_last_error(const std::string& msg) { g_last_error = msg; }
 struct smd_system {
   bool mixed = true;
   int n = 0, n_rep = 0, npad = 0, kmax = 0, n_cells = 0, n_tiles = 0;
+  int n_sph = 0;  // BEAD sphere beads
+  long long n_chains = 0;  // CHAIN molecules (lipids)
+  // adjoint work arrays (allocated by the first adjoint call)
+  struct Adj {
+    double *w0 = nullptr, *w1 = nullptr, *xbar = nullptr, *hbar = nullptr, *kw = nullptr, *fpair = nullptr;
+    double *out = nullptr;
+    double4* ws = nullptr;
+    AdjAcc* acc = nullptr;
+    AdjTables* tab = nullptr;
+  } adj;
   int cur = 0;
   long long it = 0;         // current loop step
   bool at_measure = false;  // stopped after the second half-kick of step `it`
@@ -210,9 +221,11 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   if (h->mixed) {
     SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
     SMD_LAUNCH(h, (k_integ<true, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, se)));
+    if (h->n_sph) SMD_LAUNCH(h, (k_sphere<true, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   } else {
     SMD_LAUNCH(h, (k_force<false, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
     SMD_LAUNCH(h, (k_integ<false, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, se)));
+    if (h->n_sph) SMD_LAUNCH(h, (k_sphere<false, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   }
   if (kLoopStep && h->profile) {
     if (int rc = prof_mark(h)) return rc;
@@ -220,13 +233,14 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   return 0;
 }
 
-int launch_finish(smd_system* h, int do_second, int apply_mc, StepEnd se) {
+// mode bit 0: restart half-kick; bit 1: completes a stopped loop step.
+int launch_finish(smd_system* h, int mode, int apply_mc, StepEnd se) {
   auto& P = h->P;
   const int g = h->grid();
   if (h->mixed)
-    SMD_LAUNCH(h, k_finish<true><<<g, kBlock, 0, h->stream>>>(P, h->cur, do_second, apply_mc, se));
+    SMD_LAUNCH(h, k_finish<true><<<g, kBlock, 0, h->stream>>>(P, h->cur, mode, apply_mc, se));
   else
-    SMD_LAUNCH(h, k_finish<false><<<g, kBlock, 0, h->stream>>>(P, h->cur, do_second, apply_mc, se));
+    SMD_LAUNCH(h, k_finish<false><<<g, kBlock, 0, h->stream>>>(P, h->cur, mode, apply_mc, se));
   h->cur ^= 1;
   return 0;
 }
@@ -286,12 +300,38 @@ int complete_pending(smd_system* h) {
   if (h->pending_trial) {
     SMD_LAUNCH(h, k_mc<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P));
   }
-  int rc = launch_finish(h, 0, apply, StepEnd{0, 0, 1, apply, 0});
+  int rc = launch_finish(h, 2, apply, StepEnd{0, 0, 1, apply, 0});
   if (rc) return rc;
   h->at_measure = false;
   h->pending_trial = false;
   h->it++;
   return 0;
+}
+
+// List capacity for a largest neighbour count `need` (entries per bead).
+int list_capacity(int need) { return std::max(((int)(need * 2.0) + 64 + 7) / 8 * 8, 192); }
+
+// Grows the Verlet list to list_capacity(need) (the stream is idle): a new
+// buffer, graphs re-captured on their next use (they hold the old pointer),
+// and a rebuild.
+int grow_list(smd_system* h, int need) {
+  const int kmax = list_capacity(need);
+  int* nbr = nullptr;
+  SMD_CUDA(cudaMalloc(&nbr, (size_t)kmax * h->n * sizeof(int)));
+  for (auto& q : h->allocs)
+    if (q == (void*)h->P.nbr) {
+      cudaFree(q);
+      q = nbr;
+    }
+  h->P.nbr = nbr;
+  h->P.kmax = h->kmax = kmax;
+  for (auto& gr : h->graph)
+    if (gr.exec) {
+      cudaGraphExecDestroy(gr.exec);
+      gr.exec = nullptr;
+    }
+  SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(h->P.g, 1));
+  return rebuild_if_needed(h, true);
 }
 
 int read_error(smd_system* h) {
@@ -307,6 +347,11 @@ int read_error(smd_system* h) {
                   "(system density grew far beyond the start configuration)",
                   g.need_nbr, h->kmax);
     return fail(7, buf);
+  }
+  // between calls: grow the list before a denser state can overflow it
+  if (g.max_nbr > h->kmax * 4 / 5 && !h->at_measure) {
+    if (int rc = grow_list(h, g.max_nbr)) return rc;
+    SMD_CUDA(cudaStreamSynchronize(h->stream));
   }
   return 0;
 }
@@ -333,7 +378,17 @@ int validate(const smd_system_desc& d, std::string& why) {
     if (l < 3 || l > 4095) return why = "CHAIN length must be in 3..4095", 1;
     if (s < 0 || (long long)s + (long long)c * l > d.n) return why = "CHAIN block out of range", 1;
   }
-  if (d.n_spheres > 0) return why = "BEAD residues are not supported by this build of the device step", 1;
+  if (d.n_spheres < 0 || d.n_spheres > kMaxSpheres)
+    return why = "at most " + std::to_string(kMaxSpheres) + " BEAD beads per system", 1;
+  if (d.n_spheres > 0) {
+    if (!d.sphere_index || !d.sphere_consts) return why = "null BEAD array in descriptor", 1;
+    for (int k = 0; k < d.n_spheres; ++k) {
+      if (d.sphere_index[k] < 0 || d.sphere_index[k] >= d.n) return why = "BEAD bead index out of range", 1;
+      for (int q = 0; q < k; ++q)
+        if (d.sphere_index[q] == d.sphere_index[k]) return why = "BEAD bead listed twice", 1;
+    }
+    if (!(d.sphere_consts[kBeadRadiusConst] > 0)) return why = "BEAD radius must be positive", 1;
+  }
   if (!(d.dt > 0)) return why = "dt must be positive", 1;
   return 0;
 }
@@ -371,6 +426,9 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   for (int r = 0; r < n_rep; ++r)
     if (validate(descs[r], why)) return fail(1, "replica " + std::to_string(r) + ": " + why);
   const smd_system_desc& d0 = descs[0];
+  for (int r = 0; r < n_rep; ++r)
+    if (n_rep > 1 && descs[r].n_spheres > 0)
+      return fail(1, "BEAD residues are supported in single-system handles, not in batches");
   for (int r = 1; r < n_rep; ++r) {
     const smd_system_desc& d = descs[r];
     if (d.n_types != d0.n_types || d.cutoff != d0.cutoff || d.dt != d0.dt)
@@ -464,8 +522,13 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
         set = (int)sets.size() - 1;
       }
       const int s = d.chain_blocks[3 * b], nc = d.chain_blocks[3 * b + 1], l = d.chain_blocks[3 * b + 2];
+      h->n_chains += nc;
       for (int c2 = 0; c2 < nc; ++c2)
         for (int q = 0; q < l; ++q) cinfo[bead + s + c2 * l + q] = cinfo_pack(q, l, set);
+    }
+    for (int k = 0; k < d.n_spheres; ++k) {
+      if (cinfo[bead + d.sphere_index[k]] != 0) return fail(1, "a BEAD bead is also a CHAIN member");
+      cinfo[bead + d.sphere_index[k]] = (int)(0xC0000000u | (unsigned)k);
     }
     bead += d.n;
   }
@@ -530,6 +593,30 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   if ((rc = h->alloc(&P.trial_u, (size_t)kTrialChunk * n_rep * 2)) || (rc = h->alloc(&P.ext_noise, 3 * total)) ||
       (rc = h->alloc(&P.force_out, 3 * total)))
     return rc;
+  // ---- BEAD spheres (single-system handles)
+  if (d0.n_spheres > 0) {
+    const int nc = kBeadConst * d0.n_types * d0.n_types;
+    double* dC = nullptr;
+    float* fC = nullptr;
+    if ((rc = h->alloc(&P.sph, 1)) || (rc = h->alloc(&dC, nc)) || (rc = h->alloc(&fC, nc))) return rc;
+    std::vector<float> cf(nc);
+    for (int k = 0; k < nc; ++k) cf[k] = (float)d0.sphere_consts[k];
+    SphereDev sd;
+    std::memset(&sd, 0, sizeof sd);
+    sd.n = d0.n_spheres;
+    for (int k = 0; k < sd.n; ++k) sd.orig[k] = d0.sphere_index[k];
+    const double R = d0.sphere_consts[kBeadRadiusConst];
+    sd.mass = 4.0 * M_PI * R * R;  // MD.cpp:340-355
+    sd.cut2 = d0.sphere_consts[0] * d0.sphere_consts[0];
+    sd.bb_cut2 = (R + R + 2.0) * (R + R + 2.0);
+    SMD_CUDA(cudaMemcpy(P.sph, &sd, sizeof sd, cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(dC, d0.sphere_consts, nc * sizeof(double), cudaMemcpyHostToDevice));
+    SMD_CUDA(cudaMemcpy(fC, cf.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
+    P.sphC = dC;
+    P.sphCf = fC;
+    P.n_sph = sd.n;
+    h->n_sph = sd.n;
+  }
   // ---- upload state (sorted order = file order until the first build)
   {
     std::vector<double> hx(total), hy(total), hz(total), hvx(total), hvy(total), hvz(total);
@@ -590,11 +677,12 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   SMD_CUDA(cudaMemcpyAsync(&g, P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
   const int need = std::max(g.need_nbr, 1);
-  h->kmax = ((int)(need * 1.5) + 32 + 7) / 8 * 8;
+  h->kmax = list_capacity(need);
   P.kmax = h->kmax;
   if ((rc = h->alloc(&P.nbr, (size_t)h->kmax * total))) return rc;
   g.error = 0;
   g.need_nbr = 0;
+  g.max_nbr = 0;
   g.rebuild = 1;
   g.n_rebuilds = 0;
   g.it = h->it;
@@ -688,8 +776,27 @@ int smd_set_state(smd_system* h, const double* pos, const double* vel) {
     SMD_CUDA(cudaMemcpy(P.vy, vb.data(), n * sizeof(double), cudaMemcpyHostToDevice));
     SMD_CUDA(cudaMemcpy(P.vz, vc.data(), n * sizeof(double), cudaMemcpyHostToDevice));
   }
+  if (pos) {
+    // a new configuration may be denser than the list was sized for: count
+    // with zero capacity, then size and build
+    P.kmax = 0;
+    if (int rc = force_rebuild(h)) return rc;
+    Global g;
+    SMD_CUDA(cudaMemcpyAsync(&g, P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
+    SMD_CUDA(cudaStreamSynchronize(h->stream));
+    P.kmax = h->kmax;
+    const int need = std::max(g.need_nbr, g.max_nbr);
+    g.error &= ~1;
+    g.need_nbr = 0;
+    SMD_CUDA(cudaMemcpy(P.g, &g, sizeof(Global), cudaMemcpyHostToDevice));
+    if (need > h->kmax * 4 / 5) {
+      if (int rc = grow_list(h, need)) return rc;
+    } else if (int rc = force_rebuild(h)) {
+      return rc;
+    }
+  }
   SMD_CUDA(cudaStreamSynchronize(h->stream));
-  return 0;
+  return read_error(h);
 }
 
 int smd_get_box(smd_system* h, int replica, double box[3]) {
@@ -741,7 +848,7 @@ int smd_compute_energy(smd_system* h, smd_energy* e) {
   std::vector<RepState> rs(h->n_rep);
   SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
-  for (auto& s : rs) s.e_pair = s.e_bond = s.e_kin = 0;
+  for (auto& s : rs) s.e_pair = s.e_bond = s.e_kin = s.e_sphere = 0;
   SMD_CUDA(cudaMemcpyAsync(h->P.rs, rs.data(), h->n_rep * sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
   if ((rc = launch_step<F_ENERGY>(h))) return rc;
   SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
@@ -749,7 +856,7 @@ int smd_compute_energy(smd_system* h, smd_energy* e) {
   for (int r = 0; r < h->n_rep; ++r) {
     e[r].pair = rs[r].e_pair;
     e[r].bonded = rs[r].e_bond;
-    e[r].sphere = 0;
+    e[r].sphere = rs[r].e_sphere;
     e[r].kinetic = rs[r].e_kin;
   }
   return read_error(h);
@@ -880,7 +987,7 @@ int capture_period(smd_system* h, int cur0) {
         SMD_LAUNCH(h, k_trial<<<(h->n_rep + 63) / 64, 64, 0, st>>>(P));
         if (int r = launch_step<F_STOP | F_DU>(h)) return r;
         SMD_LAUNCH(h, k_mc<<<(h->n_rep + 63) / 64, 64, 0, st>>>(P));
-        if (int r = launch_finish(h, 0, 1, StepEnd{0, 0, 1, 1, 0})) return r;
+        if (int r = launch_finish(h, 2, 1, StepEnd{0, 0, 1, 1, 0})) return r;
       } else {
         if (int r = launch_step<0>(h, se)) return r;
       }
@@ -970,6 +1077,12 @@ int smd_advance(smd_system* h, int steps, int flags) {
   return smd_sync(h);
 }
 
+int smd_use_graphs(smd_system* h, int on) {
+  if (!h) return fail(1, "null handle");
+  h->use_graphs = on != 0;
+  return 0;
+}
+
 int smd_sync(smd_system* h) {
   if (!h) return fail(1, "null handle");
   SMD_CUDA(cudaStreamSynchronize(h->stream));
@@ -1057,6 +1170,204 @@ long smd_rebuild_count(smd_system* h) {
   if (cudaMemcpyAsync(&g, h->P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) return -1;
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return -1;
   return (long)g.n_rebuilds;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ adjoint
+namespace {
+
+int adj_alloc(smd_system* h) {
+  auto& A = h->adj;
+  if (A.acc) return 0;
+  const size_t n3 = 3 * (size_t)h->n;
+  int rc;
+  if ((rc = h->alloc(&A.w0, n3)) || (rc = h->alloc(&A.w1, n3)) || (rc = h->alloc(&A.xbar, n3)) ||
+      (rc = h->alloc(&A.hbar, n3)) || (rc = h->alloc(&A.kw, n3)) || (rc = h->alloc(&A.fpair, n3)) ||
+      (rc = h->alloc(&A.out, n3)) || (rc = h->alloc(&A.ws, (size_t)h->n)) || (rc = h->alloc(&A.acc, 1)) ||
+      (rc = h->alloc(&A.tab, 1)))
+    return rc;
+  return 0;
+}
+
+// K w (pair part into adj.kw, forces into adj.fpair) at the current
+// positions for w in file order on the device; adds to the accumulators.
+int adj_pair_pass(smd_system* h, const double* w, double dt, double invT) {
+  auto& P = h->P;
+  auto& A = h->adj;
+  const int g = h->grid(), gl = h->grid_lanes();
+  if (h->mixed) {
+    float4* ws = reinterpret_cast<float4*>(A.ws);
+    SMD_LAUNCH(h, k_adj_wsort<float4><<<g, kBlock, 0, h->stream>>>(P, w, ws));
+    SMD_LAUNCH(h, (k_adj_pair<true, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur, A.tab, ws, A.kw, A.fpair,
+                                                                            A.acc, dt, invT)));
+  } else {
+    SMD_LAUNCH(h, k_adj_wsort<double4><<<g, kBlock, 0, h->stream>>>(P, w, A.ws));
+    SMD_LAUNCH(h, (k_adj_pair<false, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur, A.tab, A.ws, A.kw,
+                                                                             A.fpair, A.acc, dt, invT)));
+  }
+  return 0;
+}
+
+// Positions (and velocities) in file order into the handle; the list is
+// rebuilt when they moved too far from its build positions (force: always).
+int adj_load(smd_system* h, const double* xs, const double* vs, bool force) {
+  auto& P = h->P;
+  if (h->mixed)
+    SMD_LAUNCH(h, k_adj_load<true><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur, xs, vs));
+  else
+    SMD_LAUNCH(h, k_adj_load<false><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur, xs, vs));
+  if (force) SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 1));
+  return rebuild_if_needed(h, true);
+}
+
+int adj_check_handle(smd_system* h) {
+  if (!h) return fail(1, "null handle");
+  if (h->n_rep != 1) return fail(1, "the adjoint runs on single-system handles");
+  if (h->n_sph) return fail(1, "the adjoint does not cover BEAD residues");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int smd_hessian_vector(smd_system* h, const double* w, double* kw) {
+  if (int rc = adj_check_handle(h)) return rc;
+  if (!w || !kw) return fail(1, "bad arguments");
+  if (int rc = complete_pending(h)) return rc;
+  if (int rc = adj_alloc(h)) return rc;
+  auto& A = h->adj;
+  const size_t n3 = 3 * (size_t)h->n;
+  if (int rc = rebuild_if_needed(h, true)) return rc;
+  SMD_CUDA(cudaMemcpyAsync(A.w0, w, n3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (int rc = adj_pair_pass(h, A.w0, 0.0, 0.0)) return rc;
+  if (h->mixed)
+    SMD_LAUNCH(h, k_adj_hvp_out<true><<<h->grid(), kBlock, 0, h->stream>>>(h->P, h->cur, A.w0, A.kw, A.out));
+  else
+    SMD_LAUNCH(h, k_adj_hvp_out<false><<<h->grid(), kBlock, 0, h->stream>>>(h->P, h->cur, A.w0, A.kw, A.out));
+  SMD_CUDA(cudaMemcpyAsync(kw, A.out, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  return read_error(h);
+}
+
+int smd_adjoint(smd_system* h, const smd_adjoint_spec* spec, smd_adjoint_result* out) {
+  if (int rc = adj_check_handle(h)) return rc;
+  if (!spec || !out || spec->steps < 1 || spec->checkpoint_every < 1) return fail(1, "bad adjoint spec");
+  const int nT = h->tab.nT;
+  const int ta = spec->umin_types[0], tb = spec->umin_types[1];
+  if (ta < 0 || tb < 0 || ta >= nT || tb >= nT) return fail(1, "Umin type pair out of range");
+  if (h->barostat) return fail(1, "the adjoint holds the box fixed: switch the barostat off (delta_lxy 0)");
+  if (int rc = complete_pending(h)) return rc;
+  if (int rc = adj_alloc(h)) return rc;
+  auto& P = h->P;
+  auto& A = h->adj;
+  const int T = spec->steps, K = spec->checkpoint_every;
+  const int ncp = (T + K - 1) / K;
+  const size_t n3 = 3 * (size_t)h->n;
+  const double dt = h->dt, invT = 1.0 / T;
+  // derivative rows of Umin(a, b): the tables are linear in Umin
+  {
+    AdjTables at;
+    std::memset(&at, 0, sizeof at);
+    for (int q = 0; q < 2; ++q) {
+      const int row = q == 0 ? (ta * nT + tb) : (tb * nT + ta);
+      const double rm = h->tab.dF[6 * row], rc = h->tab.dF[6 * row + 3], w = rc - rm;
+      const double dF[6] = {rm, -2.0 / (rm * rm), 0.0, rc, 6.0 / (w * w), 6.0 / (w * w * w)};
+      const double dU[6] = {rm, -1.0 / (rm * rm), 1.0, rc, 3.0 / (w * w), 2.0 / (w * w * w)};
+      for (int k = 0; k < 6; ++k) {
+        at.dF[6 * row + k] = dF[k];
+        at.dU[6 * row + k] = dU[k];
+        at.fF[6 * row + k] = (float)dF[k];
+        at.fU[6 * row + k] = (float)dU[k];
+      }
+    }
+    SMD_CUDA(cudaMemcpyAsync(A.tab, &at, sizeof at, cudaMemcpyHostToDevice, h->stream));
+    SMD_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  // storage of this call: checkpoints (x, h), one segment of positions, the end state
+  double *cp = nullptr, *seg = nullptr, *fin = nullptr;
+  auto release = [&]() {
+    if (cp) cudaFree(cp);
+    if (seg) cudaFree(seg);
+    if (fin) cudaFree(fin);
+  };
+  if (cudaMalloc(&cp, (size_t)ncp * 2 * n3 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&seg, (size_t)K * n3 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&fin, 2 * n3 * sizeof(double)) != cudaSuccess) {
+    release();
+    return fail(2, "cudaMalloc of the adjoint checkpoints failed");
+  }
+  std::vector<long long> cp_it(ncp);
+  int rc = 0;
+  auto body = [&]() -> int {
+    // ---- forward: the state at the start of every segment
+    for (int c = 0; c < ncp; ++c) {
+      double* x = cp + (size_t)c * 2 * n3;
+      SMD_LAUNCH(h, k_adj_save<<<h->grid(), kBlock, 0, h->stream>>>(P, x, x + n3));
+      cp_it[c] = h->it;
+      const int len = std::min(K, T - c * K);
+      if (int r = smd_advance(h, len, SMD_ASYNC)) return r;
+    }
+    SMD_LAUNCH(h, k_adj_save<<<h->grid(), kBlock, 0, h->stream>>>(P, fin, fin + n3));
+    const long long it_end = h->it;
+    SMD_CUDA(cudaMemsetAsync(A.w0, 0, n3 * sizeof(double), h->stream));
+    SMD_CUDA(cudaMemsetAsync(A.xbar, 0, n3 * sizeof(double), h->stream));
+    SMD_CUDA(cudaMemsetAsync(A.hbar, 0, n3 * sizeof(double), h->stream));
+    SMD_CUDA(cudaMemsetAsync(A.acc, 0, sizeof(AdjAcc), h->stream));
+    double* w = A.w0;
+    double* wn = A.w1;
+    // ---- backward, segment by segment
+    for (int c = ncp - 1; c >= 0; --c) {
+      const int len = std::min(K, T - c * K);
+      const double* x = cp + (size_t)c * 2 * n3;
+      if (spec->segment_local && c != ncp - 1) {
+        SMD_CUDA(cudaMemsetAsync(w, 0, n3 * sizeof(double), h->stream));
+        SMD_CUDA(cudaMemsetAsync(A.xbar, 0, n3 * sizeof(double), h->stream));
+        SMD_CUDA(cudaMemsetAsync(A.hbar, 0, n3 * sizeof(double), h->stream));
+      }
+      if (int r = adj_load(h, x, x + n3, true)) return r;
+      h->it = cp_it[c];
+      SMD_LAUNCH(h, k_set_counters<<<1, 1, 0, h->stream>>>(P.g, h->it, 1, 0, 0));
+      for (int m = 0; m < len; ++m) {  // recompute x_n of the segment
+        SMD_LAUNCH(h, k_adj_save<<<h->grid(), kBlock, 0, h->stream>>>(P, seg + (size_t)m * n3, nullptr));
+        if (m + 1 < len)
+          if (int r = smd_advance(h, 1, SMD_ASYNC)) return r;
+      }
+      for (int m = len - 1; m >= 0; --m) {
+        if (int r = adj_load(h, seg + (size_t)m * n3, nullptr, false)) return r;
+        if (int r = adj_pair_pass(h, w, dt, invT)) return r;
+        if (h->mixed)
+          SMD_LAUNCH(h, k_adj_chain<true><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur, w, wn, A.xbar, A.hbar,
+                                                                               A.kw, A.fpair, A.acc, dt, invT));
+        else
+          SMD_LAUNCH(h, k_adj_chain<false><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur, w, wn, A.xbar, A.hbar,
+                                                                                A.kw, A.fpair, A.acc, dt, invT));
+        std::swap(w, wn);
+      }
+    }
+    // ---- the state after the T steps
+    if (int r = adj_load(h, fin, fin + n3, true)) return r;
+    h->it = it_end;
+    SMD_LAUNCH(h, k_set_counters<<<1, 1, 0, h->stream>>>(P.g, h->it, 1, 0, 0));
+    return 0;
+  };
+  rc = body();
+  const cudaError_t se = cudaStreamSynchronize(h->stream);
+  release();
+  if (rc) return rc;
+  if (se != cudaSuccess) return fail(100 + (int)se, std::string("adjoint: ") + cudaGetErrorString(se));
+  AdjAcc acc;
+  SMD_CUDA(cudaMemcpy(&acc, A.acc, sizeof acc, cudaMemcpyDeviceToHost));
+  double box[3];
+  if (int r = smd_get_box(h, 0, box)) return r;
+  out->mean_potential = acc.J;
+  for (int k = 0; k < 3; ++k) {
+    out->grad[k] = acc.grad[k];
+    out->grad_area[k] = 0.0;
+  }
+  out->mean_area_per_lipid = h->n_chains > 0 ? box[0] * box[1] / (0.5 * (double)h->n_chains) : 0.0;
+  return read_error(h);
 }
 
 }  // extern "C"

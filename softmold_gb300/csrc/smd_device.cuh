@@ -26,6 +26,9 @@ constexpr int kMaxChainSets = 32;
 constexpr int kBlock = 256;
 constexpr int kScanTile = 2048;  // cells per scan block (256 threads x 8)
 constexpr int kLanes = 8;        // lanes per bead in the list build and the pair pass
+constexpr int kMaxSpheres = 16;  // BEAD beads of one handle (the reference's brute-force branch takes <= 20)
+constexpr int kBeadConst = 22;   // constants per ordered type pair of a BEAD residue (nBEADCONST)
+constexpr int kBeadBeadOff = 11; // BEADBEADOFFSET: bead-bead constants within a row
 
 // cinfo word: bit 31 chain member, bits 0..11 position in chain, bits 12..23
 // chain length, bits 24..28 chain-constant set; bit 30 marks a BEAD sphere.
@@ -43,6 +46,20 @@ struct RepParams {  // per replica, fixed
   int cell_begin, cell_cap;
 };
 
+// BEAD residue of a single-system handle (include/system.h:2043-2212): the
+// spheres' file-order indices, mass 4 pi R^2 (MD.cpp:340-355) and the sums of
+// the other beads' reactions on each sphere, gathered during k_integ and used
+// by k_sphere.  MIXED sums are int64 in units of 2^-32 (order-independent).
+struct SphereDev {
+  int n;
+  int orig[kMaxSpheres];
+  double mass;
+  double cut2;      // (R + rc)^2: bead-sphere range (row 0, constant 0)
+  double bb_cut2;   // (2R + 2)^2: sphere-sphere range
+  long long fq[kMaxSpheres][3];
+  double fd[kMaxSpheres][3];
+};
+
 struct RepState {  // per replica, updated on the device
   double box[3];
   double frac_per_len[3];  // 2^32 / box: real -> 32-bit fractional coordinate
@@ -52,7 +69,7 @@ struct RepState {  // per replica, updated on the device
   double scale[3];   // scale of the last accepted / current trial
   double dU_pair, dU_bond;  // FP64 form: U(x) - U(s x) summed in any order
   long long dUq_pair, dUq_bond;  // mixed form: the same in units of 2^-32, summed exactly
-  double e_pair, e_bond, e_kin;
+  double e_pair, e_bond, e_kin, e_sphere;
   double last_dU;
   long long n_trial, n_accept;
   int accept;
@@ -79,6 +96,7 @@ struct Global {  // single instance
   int rebuild;                 // 1: rebuild the Verlet list before the next force pass
   int error;                   // bit 0: list overflow, bit 1: cell overflow (>kMaxCell)
   int need_nbr;                // largest neighbour count seen on overflow
+  int max_nbr;                 // largest neighbour count of any list build so far
   int trial_slot;              // staged barostat trial used by the next MC step
   long long it;                // loop step (the Langevin noise key); advanced by the step's last kernel
   long long graph_builds;      // list builds run inside graph conditional bodies
@@ -141,6 +159,10 @@ struct DevPtrs {
   double* ext_noise; // n*3 noise in sorted order (test hook)
   double* force_out; // n*3 scratch for host reads (file order)
   int* key_out;
+  int n_sph;         // BEAD beads (0: none)
+  SphereDev* sph;
+  const double* sphC;  // kBeadConst * nT^2 BEAD constants
+  const float* sphCf;  // the same in FP32
 };
 
 // ------------------------------------------------------------------ helpers
@@ -321,6 +343,81 @@ __device__ __forceinline__ float pair_dpot_f(const float* c, float r, float rn, 
   const float u0 = in0 ? pair_pot<float>(c, r) : 0.f;
   const float u1 = in1 ? pair_pot<float>(c, rn) : 0.f;
   return u0 - u1;
+}
+
+// ------------------------------------------------------------------ BEAD
+// Continuum sphere <-> bead force and potential (beadForce / beadPotential,
+// include/MD.h:165-231) for d = x_sphere - x_bead and one 22-constant row C:
+// an outer well on E = C0 - r for r >= C4 + C5 and an inner polynomial in
+// B = C4 + C5 - r below it.  Returns mag with force mag*d on the sphere and
+// -mag*d on the bead.
+__device__ __forceinline__ double bead_mag(double dr2, const double* C, double cut2) {
+  const double rminD = C[4] + C[5];
+  const double rminD2 = rminD * rminD;
+  double mag = 0.0;
+  if (rminD2 <= dr2 && dr2 < cut2) {
+    const double dr = sqrt(dr2);
+    const double E = C[0] - dr, E2 = E * E, E3 = E * E2;
+    mag = 2.0 * (0.4 * E3 + C[1] * E2 + C[2] * E) / (dr);
+    mag += 4.0 * E2 + 8.0 * C[1] * E + 6.0 * C[2];
+    mag *= (E2 * C[3]) / (dr * dr);
+  } else if (dr2 < rminD2) {
+    const double dr = sqrt(dr2);
+    const double B = rminD - dr, B2 = B * B, B3 = B2 * B, B4 = B2 * B2;
+    mag = (B4 * C[6] + B3 * C[7] + B2 * C[8] + B * C[9] + C[10]) / (dr);
+    mag += (4.0 * B3 * C[6] + 3.0 * B2 * C[7] + 2.0 * B * C[8] + C[9]);
+    mag /= dr * dr;
+  }
+  return mag;
+}
+__device__ __forceinline__ double bead_pot(double dr2, const double* C, double cut2) {
+  const double rminD = C[4] + C[5];
+  const double rminD2 = rminD * rminD;
+  if (rminD2 <= dr2 && dr2 < cut2) {
+    const double dr = sqrt(dr2);
+    const double E = C[0] - dr, E2 = E * E, E3 = E * E2;
+    return 2.0 * E3 * (0.4 * E2 + C[1] * E + C[2]) * C[3] / (dr);
+  } else if (dr2 < rminD2) {
+    const double dr = sqrt(dr2);
+    const double B = rminD - dr, B2 = B * B, B3 = B2 * B, B4 = B2 * B2;
+    return (B4 * C[6] + B3 * C[7] + B2 * C[8] + B * C[9] + C[10]) / (dr);
+  }
+  return 0.0;
+}
+// Sphere <-> sphere (beadBeadForce / beadBeadPotential, include/MD.h:233-338)
+// from the row's constants at kBeadBeadOff; d = x_first - x_second, force
+// mag*d on the first.
+__device__ __forceinline__ double beadbead_mag(double dr2, const double* Cr, double cut2) {
+  const double* C = Cr + kBeadBeadOff;
+  const double rminD = C[0], rminD2 = rminD * rminD;
+  double mag = 0.0;
+  if (rminD2 <= dr2 && dr2 < cut2) {
+    const double dr = sqrt(dr2);
+    const double E = C[1] - dr, E2 = E * E, E3 = E * E2;
+    mag = E3 * (6.0 * C[2] * E2 + 5.0 * C[3] * E + 4.0 * C[4] + (C[2] * E3 + C[3] * E2 + C[4] * E) / dr) /
+          (dr * dr);
+  } else if (dr2 < rminD2) {
+    const double dr = sqrt(dr2);
+    const double B = rminD - dr, B2 = B * B, B3 = B2 * B, B4 = B2 * B2, B5 = B2 * B3;
+    mag = 5.0 * B4 * C[5] + 4.0 * B3 * C[6] + 3.0 * B2 * C[7] + 2.0 * B * C[8] + C[9];
+    mag += (B5 * C[5] + B4 * C[6] + B3 * C[7] + B2 * C[8] + B * C[9] + C[10]) / (dr);
+    mag /= dr * dr;
+  }
+  return mag;
+}
+__device__ __forceinline__ double beadbead_pot(double dr2, const double* Cr, double cut2) {
+  const double* C = Cr + kBeadBeadOff;
+  const double rminD = C[0], rminD2 = rminD * rminD;
+  if (rminD2 <= dr2 && dr2 < cut2) {
+    const double dr = sqrt(dr2);
+    const double E = C[1] - dr, E2 = E * E, E4 = E2 * E2;
+    return E4 * (C[2] * E2 + C[3] * E + C[4]) / dr;
+  } else if (dr2 < rminD2) {
+    const double dr = sqrt(dr2);
+    const double B = rminD - dr, B2 = B * B, B3 = B2 * B, B4 = B2 * B2, B5 = B2 * B3;
+    return (B5 * C[5] + B4 * C[6] + B3 * C[7] + B2 * C[8] + B * C[9] + C[10]) / (dr);
+  }
+  return 0.0;
 }
 
 }  // namespace smd

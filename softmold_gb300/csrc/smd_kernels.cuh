@@ -323,6 +323,7 @@ __device__ __forceinline__ void list_counts(const DevPtrs& P, const CellCtx& q, 
   for (int b = threadIdx.x; b < q.e - q.s; b += nt) {
     const int count = cnt[b];
     P.nnbr[q.s + b] = count < P.kmax ? count : P.kmax;
+    if (count > *(volatile int*)&P.g->max_nbr) atomicMax(&P.g->max_nbr, count);
     if (count > P.kmax) {
       atomicOr(&P.g->error, 1);
       atomicMax(&P.g->need_nbr, count);
@@ -795,6 +796,113 @@ __device__ __forceinline__ void warp_atomic_add_q(long long v, long long* dst, i
     atomicAdd((unsigned long long*)dst, (unsigned long long)acc);
 }
 
+// Sphere <-> bead terms of bead i for every BEAD sphere (Blob::doBeadForce
+// brute-force branch, include/system.h:2165-2210, and doBeadPotential /
+// doBeadDPotential): the force on the bead into fs, and the reaction on each
+// sphere summed over the warp into the sphere's accumulator (MIXED: int64 in
+// units of 2^-32, exact in any order).  Energies and size-change differences
+// include every bead k != sphere, forces exclude the other spheres, as the
+// reference does.  The separation d = x_sphere - x_bead takes the minimum
+// image (MIXED: exact from the 32-bit fractional mirror; PLAIN: the
+// reference's half-box shift).  Called by whole warps.
+template <bool MIXED, int FL>
+__device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, bool active, Vec3<double>& fs,
+                                             double& e_sph, double& du_sph) {
+  SphereDev* S = P.sph;
+  const int nT = P.tab->nT;
+  const RepState& rs = P.rs[0];
+  const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
+  const bool me_sphere = active && (P.cinfo[i] < 0) && (P.cinfo[i] & 0x40000000);
+  int ti = 0;
+  uint4 mu = make_uint4(0, 0, 0, 0);
+  double4 md = make_double4(0, 0, 0, 0);
+  if (active) {
+    if constexpr (MIXED) {
+      mu = P.m4[cur][i];
+      ti = mu.w & 0xff;
+    } else {
+      md = P.d4[cur][i];
+      ti = __double_as_longlong(md.w) & 0xff;
+    }
+  }
+  const int o = active ? P.orig[i] : -1;
+  for (int s = 0; s < P.n_sph; ++s) {
+    const int os = S->orig[s];
+    double r[3] = {0.0, 0.0, 0.0};
+    if (active && o != os) {
+      const int js = P.inv[os];
+      double d[3];
+      int ts;
+      bool near;
+      if constexpr (MIXED) {
+        const uint4 ms = P.m4[cur][js];
+        ts = ms.w & 0xff;
+        // FP32 range test first; FP64 from the exact fractional differences
+        const float fx = frac_delta(ms.x, mu.x, rs.len_per_frac[0]);
+        const float fy = frac_delta(ms.y, mu.y, rs.len_per_frac[1]);
+        const float fz = frac_delta(ms.z, mu.z, rs.len_per_frac[2]);
+        near = (fx * fx + fy * fy + fz * fz) < (float)S->cut2 * 1.001f + 0.01f;
+        if (near) {
+          d[0] = frac_delta_d(ms.x, mu.x, box[0] * (1.0 / 4294967296.0));
+          d[1] = frac_delta_d(ms.y, mu.y, box[1] * (1.0 / 4294967296.0));
+          d[2] = frac_delta_d(ms.z, mu.z, box[2] * (1.0 / 4294967296.0));
+        }
+      } else {
+        const double4 ms = P.d4[cur][js];
+        ts = __double_as_longlong(ms.w) & 0xff;
+        d[0] = ms.x - md.x;
+        d[1] = ms.y - md.y;
+        d[2] = ms.z - md.z;
+        for (int a = 0; a < 3; ++a) {
+          if (d[a] > box[a] / 2.0) d[a] -= box[a];
+          if (d[a] < -box[a] / 2.0) d[a] += box[a];
+        }
+        near = true;
+      }
+      if (near) {
+        const double* row = P.sphC + kBeadConst * (ts * nT + ti);
+        const double dr2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if constexpr ((FL & F_ENERGY) != 0) e_sph += bead_pot(dr2, row, S->cut2);
+        if constexpr ((FL & F_DU) != 0) {
+          const double e0 = d[0] * rs.scale[0], e1 = d[1] * rs.scale[1], e2 = d[2] * rs.scale[2];
+          du_sph += bead_pot(dr2, row, S->cut2) - bead_pot(e0 * e0 + e1 * e1 + e2 * e2, row, S->cut2);
+        }
+        if constexpr ((FL & F_ENERGY) == 0) {
+          if (!me_sphere) {
+            const double mag = bead_mag(dr2, row, S->cut2);
+            for (int a = 0; a < 3; ++a) r[a] = d[a] * mag;
+            fs.x -= r[0];
+            fs.y -= r[1];
+            fs.z -= r[2];
+          }
+        }
+      }
+    }
+    if constexpr ((FL & F_ENERGY) == 0) {
+      if constexpr (MIXED) {
+        long long q[3];
+        for (int a = 0; a < 3; ++a) q[a] = __double2ll_rn(r[a] * 4294967296.0);
+        if (__any_sync(0xffffffffu, (q[0] | q[1] | q[2]) != 0)) {
+          for (int a = 0; a < 3; ++a) {
+#pragma unroll
+            for (int w = 16; w > 0; w >>= 1) q[a] += __shfl_xor_sync(0xffffffffu, q[a], w);
+          }
+          if ((threadIdx.x & 31) == 0)
+            for (int a = 0; a < 3; ++a)
+              if (q[a]) atomicAdd((unsigned long long*)&S->fq[s][a], (unsigned long long)q[a]);
+        }
+      } else {
+        if (__any_sync(0xffffffffu, (r[0] != 0.0) || (r[1] != 0.0) || (r[2] != 0.0))) {
+          for (int a = 0; a < 3; ++a) r[a] = warp_sum(r[a]);
+          if ((threadIdx.x & 31) == 0)
+            for (int a = 0; a < 3; ++a)
+              if (r[a] != 0.0) atomicAdd(&S->fd[s][a], r[a]);
+        }
+      }
+    }
+  }
+}
+
 // Non-bonded pass: G lanes per bead walk the bead's Verlet-list entries
 // (bead-major, so a group reads G consecutive indices per round) and reduce
 // with shuffles.  MIXED: FP32 pair arithmetic, each pair force rounded to a
@@ -990,6 +1098,13 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
   const int r = active ? rep_of(P, i) : 0;
   double dU_bond = 0.0, e_bond = 0.0, e_kin = 0.0;
   float vmax = 0.f;
+  // sphere <-> bead terms (BEAD residues; whole warps)
+  Vec3<double> fs{0.0, 0.0, 0.0};
+  double e_sph = 0.0, du_sph = 0.0;
+  if constexpr ((FL & F_PAIRONLY) == 0) {
+    if (P.n_sph > 0) sphere_terms<MIXED, FL>(P, cur, i, active, fs, e_sph, du_sph);
+  }
+  dU_bond += du_sph;
   if (active) {
     const RepParams& rp = P.rp[r];
     const RepState& rs = P.rs[r];
@@ -1000,6 +1115,7 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
     using R = typename std::conditional<MIXED, float, double>::type;
     Vec3<R> fb{0, 0, 0};
     const int ci = P.cinfo[i];
+    const bool sphere = (ci < 0) && (ci & 0x40000000);  // integrated by k_sphere
     if ((FL & F_PAIRONLY) == 0 && ci < 0 && !(ci & 0x40000000)) {
       const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
       // forces in R from the same vectors in every variant; energies and
@@ -1054,12 +1170,19 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
         F[1] = P.fp[i + P.n] + fb.y;
         F[2] = P.fp[i + 2 * P.n] + fb.z;
       }
+      if (P.n_sph > 0) {
+        F[0] += fs.x;
+        F[1] += fs.y;
+        F[2] += fs.z;
+      }
       if constexpr ((FL & F_FORCES) != 0) {
-        const int o = P.orig[i];
-        P.force_out[3 * o] = F[0];
-        P.force_out[3 * o + 1] = F[1];
-        P.force_out[3 * o + 2] = F[2];
-      } else {
+        if (!sphere) {
+          const int o = P.orig[i];
+          P.force_out[3 * o] = F[0];
+          P.force_out[3 * o + 1] = F[1];
+          P.force_out[3 * o + 2] = F[2];
+        }
+      } else if (!sphere) {
         const int o = P.orig[i];
         double noise[3];  // sigma * psi
         if constexpr ((FL & F_EXTNOISE) != 0) {
@@ -1070,20 +1193,19 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
         double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
         double a[3];
         for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
-        const bool sphere = (ci < 0) && (ci & 0x40000000);
         if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
           P.ax[i] = a[0];
           P.ay[i] = a[1];
           P.az[i] = a[2];
           if constexpr ((FL & F_STOP) != 0) {
-            if (ti != 0 && !sphere) {
+            if (ti != 0) {
               const double h = rp.dt * 0.5;
               P.vx[i] = fma(a[0], h, v[0]);
               P.vy[i] = fma(a[1], h, v[1]);
               P.vz[i] = fma(a[2], h, v[2]);
             }
           }
-        } else if (!sphere) {
+        } else {
           double x[3] = {P.x[i], P.y[i], P.z[i]};
           if (ti != 0) {
             if constexpr (MIXED) {
@@ -1124,10 +1246,6 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
             const double4 me = P.d4[cur][i];
             P.d4[cur ^ 1][i] = make_double4(x[0], x[1], x[2], me.w);
           }
-        } else {
-          P.ax[i] = a[0];
-          P.ay[i] = a[1];
-          P.az[i] = a[2];
         }
       }
     }
@@ -1139,6 +1257,7 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
   if constexpr ((FL & F_ENERGY) != 0) {
     warp_atomic_add(e_bond, &P.rs[r].e_bond, r);
     warp_atomic_add(e_kin, &P.rs[r].e_kin, r);
+    if (P.n_sph > 0) warp_atomic_add(e_sph, &P.rs[r].e_sphere, r);
   }
   if constexpr ((FL & (F_STOP | F_INIT | F_FORCES | F_ENERGY)) == 0) {
     vmax = warp_max(vmax);
@@ -1148,7 +1267,12 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
     float bm = 0.f;
     if (threadIdx.x == 0)
       for (int w = 0; w < kBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
-    finalize_step(P, bm, se);
+    if (P.n_sph > 0) {
+      // k_sphere completes the step once the spheres have moved
+      if (threadIdx.x == 0 && bm > 0.f) atomicMax(&P.g->dmax_bits, __float_as_uint(bm));
+    } else {
+      finalize_step(P, bm, se);
+    }
   }
 }
 
@@ -1213,9 +1337,15 @@ __global__ void k_mc(DevPtrs P) {
 
 // Completes a stopped step: optional restart half-kick, optional box rescale
 // of an accepted MC move, then the next step's first half-kick and drift.
+// mode bit 0: restart half-kick (MD.cpp:300-308); bit 1: the stopped step was
+// a loop step.  A BEAD sphere's stored acceleration is its undivided force;
+// the reference divides it by the sphere mass after the forces and again
+// before first() (MD.cpp:340-355, 480-509), so a first half-kick that follows
+// a second one uses a / m^2, the one of a fresh start a / m.
 template <bool MIXED>
-__global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_second, int apply_mc, StepEnd se) {
+__global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int mode, int apply_mc, StepEnd se) {
   const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int do_second = mode & 1;
   float vmax = 0.f;
   if (i < P.n) {
     const int r = rep_of(P, i);
@@ -1223,40 +1353,46 @@ __global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_se
     const RepState& rs = P.rs[r];
     const int ci = P.cinfo[i];
     const bool sphere = (ci < 0) && (ci & 0x40000000);
-    if (!sphere) {
-      int ti;
-      if constexpr (MIXED) ti = P.m4[cur][i].w & 0xff; else ti = __double_as_longlong(P.d4[cur][i].w) & 0xff;
-      double x[3] = {P.x[i], P.y[i], P.z[i]};
-      if (apply_mc && rs.accept)
-        for (int d = 0; d < 3; ++d) x[d] *= rs.scale[d];
-      if (ti != 0) {
-        const double h = rp.dt * 0.5;
-        const double a[3] = {P.ax[i], P.ay[i], P.az[i]};
-        double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+    int ti;
+    if constexpr (MIXED) ti = P.m4[cur][i].w & 0xff; else ti = __double_as_longlong(P.d4[cur][i].w) & 0xff;
+    double x[3] = {P.x[i], P.y[i], P.z[i]};
+    if (apply_mc && rs.accept)
+      for (int d = 0; d < 3; ++d) x[d] *= rs.scale[d];
+    if (ti != 0) {
+      const double h = rp.dt * 0.5;
+      double a[3] = {P.ax[i], P.ay[i], P.az[i]};
+      double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+      double af[3] = {a[0], a[1], a[2]};
+      if (sphere) {
+        const double m = P.sph->mass;
         for (int d = 0; d < 3; ++d) {
-          if (do_second) v[d] = fma(a[d], h, v[d]);
-          v[d] = fma(a[d], h, v[d]);
-          x[d] = fma(v[d], rp.dt, x[d]);
-          if (x[d] > rs.box[d]) x[d] -= rs.box[d];
-          if (x[d] < 0) x[d] += rs.box[d];
+          a[d] = a[d] / m;
+          af[d] = (mode & 3) ? a[d] / m : a[d];
         }
-        P.vx[i] = v[0];
-        P.vy[i] = v[1];
-        P.vz[i] = v[2];
       }
-      P.x[i] = x[0];
-      P.y[i] = x[1];
-      P.z[i] = x[2];
-      const unsigned int fx = to_frac(x[0], rs.frac_per_len[0]), fy = to_frac(x[1], rs.frac_per_len[1]),
-                         fz = to_frac(x[2], rs.frac_per_len[2]);
-      vmax = displacement(P.ref[i], fx, fy, fz, rs);
-      if constexpr (MIXED) {
-        const uint4 me = P.m4[cur][i];
-        P.m4[cur ^ 1][i] = make_uint4(fx, fy, fz, me.w);
-      } else {
-        const double4 me = P.d4[cur][i];
-        P.d4[cur ^ 1][i] = make_double4(x[0], x[1], x[2], me.w);
+      for (int d = 0; d < 3; ++d) {
+        if (do_second) v[d] = fma(a[d], h, v[d]);
+        v[d] = fma(af[d], h, v[d]);
+        x[d] = fma(v[d], rp.dt, x[d]);
+        if (x[d] > rs.box[d]) x[d] -= rs.box[d];
+        if (x[d] < 0) x[d] += rs.box[d];
       }
+      P.vx[i] = v[0];
+      P.vy[i] = v[1];
+      P.vz[i] = v[2];
+    }
+    P.x[i] = x[0];
+    P.y[i] = x[1];
+    P.z[i] = x[2];
+    const unsigned int fx = to_frac(x[0], rs.frac_per_len[0]), fy = to_frac(x[1], rs.frac_per_len[1]),
+                       fz = to_frac(x[2], rs.frac_per_len[2]);
+    vmax = displacement(P.ref[i], fx, fy, fz, rs);
+    if constexpr (MIXED) {
+      const uint4 me = P.m4[cur][i];
+      P.m4[cur ^ 1][i] = make_uint4(fx, fy, fz, me.w);
+    } else {
+      const double4 me = P.d4[cur][i];
+      P.d4[cur ^ 1][i] = make_double4(x[0], x[1], x[2], me.w);
     }
   }
   vmax = warp_max(vmax);
@@ -1267,6 +1403,167 @@ __global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int do_se
   if (threadIdx.x == 0)
     for (int w = 0; w < kBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
   finalize_step(P, bm, se);
+}
+
+// BEAD spheres after k_integ (one warp, one sphere per lane): the total force
+// on each sphere (its non-bonded force, the reactions gathered in k_integ and
+// the sphere-sphere terms, include/system.h:2072-2098), its Langevin term,
+// the mass division of MD.cpp:480-509 and, in a loop step, both half-kicks,
+// the drift and the wrap; then the step's list-rebuild decision.  The same
+// flags as k_integ select the variant.
+template <bool MIXED, int FL>
+__global__ void __launch_bounds__(32) k_sphere(DevPtrs P, int cur, StepEnd se) {
+  SphereDev* S = P.sph;
+  const int s = threadIdx.x;
+  const long long it = P.g->it;
+  const Tables& T = *P.tab;
+  const RepParams& rp = P.rp[0];
+  const RepState& rs = P.rs[0];
+  const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
+  float vmax = 0.f;
+  double e = 0.0, du = 0.0;
+  if (s < S->n) {
+    const int o = S->orig[s], j = P.inv[o];
+    int ti;
+    if constexpr (MIXED) ti = P.m4[cur][j].w & 0xff; else ti = __double_as_longlong(P.d4[cur][j].w) & 0xff;
+    double F[3] = {0.0, 0.0, 0.0};
+    if constexpr ((FL & F_ENERGY) == 0) {
+      for (int d = 0; d < 3; ++d) {
+        if constexpr (MIXED) F[d] = (double)P.fq[j + d * P.n] * T.inv_fscale;
+        else F[d] = P.fp[j + d * P.n];
+      }
+      if constexpr ((FL & F_PAIRONLY) == 0) {
+        for (int d = 0; d < 3; ++d) {
+          if constexpr (MIXED) F[d] += (double)S->fq[s][d] * (1.0 / 4294967296.0);
+          else F[d] += S->fd[s][d];
+        }
+      }
+    }
+    if constexpr ((FL & F_PAIRONLY) == 0) {
+      for (int t = 0; t < S->n; ++t) {
+        if (t == s) continue;
+        const int jt = P.inv[S->orig[t]];
+        double d[3];
+        int tt;
+        if constexpr (MIXED) {
+          const uint4 a = P.m4[cur][j], b = P.m4[cur][jt];
+          tt = b.w & 0xff;
+          d[0] = frac_delta_d(a.x, b.x, box[0] * (1.0 / 4294967296.0));
+          d[1] = frac_delta_d(a.y, b.y, box[1] * (1.0 / 4294967296.0));
+          d[2] = frac_delta_d(a.z, b.z, box[2] * (1.0 / 4294967296.0));
+        } else {
+          const double4 a = P.d4[cur][j], b = P.d4[cur][jt];
+          tt = __double_as_longlong(b.w) & 0xff;
+          d[0] = a.x - b.x;
+          d[1] = a.y - b.y;
+          d[2] = a.z - b.z;
+          for (int q = 0; q < 3; ++q) {
+            if (d[q] > box[q] / 2.0) d[q] -= box[q];
+            if (d[q] < -box[q] / 2.0) d[q] += box[q];
+          }
+        }
+        // the pair's row is (type of the earlier bead of the residue, later)
+        const double* row = P.sphC + kBeadConst * ((s < t) ? (ti * T.nT + tt) : (tt * T.nT + ti));
+        const double dr2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if constexpr ((FL & F_ENERGY) == 0) {
+          const double mag = beadbead_mag(dr2, row, S->bb_cut2);
+          for (int q = 0; q < 3; ++q) F[q] += mag * d[q];
+        }
+        if (t > s) {
+          if constexpr ((FL & F_ENERGY) != 0) e += beadbead_pot(dr2, row, S->bb_cut2);
+          if constexpr ((FL & F_DU) != 0) {
+            const double e0 = d[0] * rs.scale[0], e1 = d[1] * rs.scale[1], e2 = d[2] * rs.scale[2];
+            du += beadbead_pot(dr2, row, S->bb_cut2) - beadbead_pot(e0 * e0 + e1 * e1 + e2 * e2, row, S->bb_cut2);
+          }
+        }
+      }
+    }
+    if constexpr ((FL & F_FORCES) != 0) {
+      for (int d = 0; d < 3; ++d) P.force_out[3 * o + d] = F[d];
+    } else if constexpr ((FL & F_ENERGY) == 0) {
+      double noise[3];
+      if constexpr ((FL & F_EXTNOISE) != 0) {
+        for (int d = 0; d < 3; ++d) noise[d] = rp.sigma * P.ext_noise[3 * o + d];
+      } else {
+        langevin_noise(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
+      }
+      double v[3] = {P.vx[j], P.vy[j], P.vz[j]};
+      double a[3];
+      for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
+      const double m = S->mass, h = rp.dt * 0.5;
+      if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
+        P.ax[j] = a[0];
+        P.ay[j] = a[1];
+        P.az[j] = a[2];
+        if constexpr ((FL & F_STOP) != 0) {
+          if (ti != 0) {
+            P.vx[j] = fma(a[0] / m, h, v[0]);
+            P.vy[j] = fma(a[1] / m, h, v[1]);
+            P.vz[j] = fma(a[2] / m, h, v[2]);
+          }
+        }
+      } else {
+        double x[3] = {P.x[j], P.y[j], P.z[j]};
+        if (ti != 0) {
+          for (int d = 0; d < 3; ++d) {
+            const double a1 = a[d] / m, a2 = a1 / m;
+            if constexpr (MIXED) {
+              v[d] = fma(a2, h, fma(a1, h, v[d]));
+              x[d] = fma(v[d], rp.dt, x[d]);
+            } else {
+              v[d] += a1 * h;
+              v[d] += a2 * h;
+              x[d] += v[d] * rp.dt;
+            }
+            if (x[d] > box[d]) x[d] -= box[d];
+            if (x[d] < 0) x[d] += box[d];
+          }
+          P.vx[j] = v[0];
+          P.vy[j] = v[1];
+          P.vz[j] = v[2];
+          P.x[j] = x[0];
+          P.y[j] = x[1];
+          P.z[j] = x[2];
+        }
+        const unsigned int fx = to_frac(x[0], rs.frac_per_len[0]), fy = to_frac(x[1], rs.frac_per_len[1]),
+                           fz = to_frac(x[2], rs.frac_per_len[2]);
+        vmax = displacement(P.ref[j], fx, fy, fz, rs);
+        if constexpr (MIXED) {
+          const uint4 me = P.m4[cur][j];
+          P.m4[cur ^ 1][j] = make_uint4(fx, fy, fz, me.w);
+        } else {
+          const double4 me = P.d4[cur][j];
+          P.d4[cur ^ 1][j] = make_double4(x[0], x[1], x[2], me.w);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  // every lane has read its accumulator: clear them for the next pass
+  if (s < S->n)
+    for (int d = 0; d < 3; ++d) {
+      S->fq[s][d] = 0;
+      S->fd[s][d] = 0.0;
+    }
+  if constexpr ((FL & F_ENERGY) != 0) {
+    e = warp_sum(e);
+    if (s == 0 && e != 0.0) atomicAdd(&P.rs[0].e_sphere, e);
+  }
+  if constexpr ((FL & F_DU) != 0) {
+    if constexpr (MIXED) {
+      long long q = __double2ll_rn(du * 4294967296.0);
+#pragma unroll
+      for (int w = 16; w > 0; w >>= 1) q += __shfl_xor_sync(0xffffffffu, q, w);
+      if (s == 0 && q != 0) atomicAdd((unsigned long long*)&P.rs[0].dUq_bond, (unsigned long long)q);
+    } else {
+      du = warp_sum(du);
+      if (s == 0 && du != 0.0) atomicAdd(&P.rs[0].dU_bond, du);
+    }
+  }
+  if constexpr ((FL & (F_STOP | F_INIT | F_FORCES | F_ENERGY)) == 0) {
+    vmax = warp_max(vmax);
+    finalize_step(P, vmax, se);
+  }
 }
 
 // Mirror of the current positions in the other buffer (after set_state or a

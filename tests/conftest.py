@@ -46,4 +46,6 @@ def mpd_from_golden(g):
                    chain_blocks=g["chain_blocks"].astype(np.int32), chain_consts=g["chain_consts"],
                    dt=float(g["dt"]), gamma=float(g["gamma"]), temperature=float(g["temperature"]),
                    seed=int(g["seed"]), tension=float(g["tension"]), delta_lxy=float(g["delta_lxy"]),
-                   initial_time=0.0, final_time=1.0)
+                   initial_time=0.0, final_time=1.0,
+                   sphere_index=g["sphere_index"].astype(np.int32) if len(g.get("sphere_index", [])) else None,
+                   sphere_consts=g["sphere_consts"] if len(g.get("sphere_index", [])) else None)

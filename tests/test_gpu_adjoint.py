@@ -1,0 +1,261 @@
+"""Adjoint of the step (smd_adjoint, smd_hessian_vector) on the GPU.
+
+The reference computes no derivatives, so these tests check the adjoint
+against finite differences of quantities the reference does define:
+  * K w (the force Jacobian times w) against central differences of the
+    oracle's FP64 forces (CellOpt::computeForce + Blob::doChainForce);
+  * dJ/d(Umin(TT), kbond, kbend), J the mean potential over a window of loop
+    steps with the Langevin noise fixed by its seed and the box fixed,
+    against central differences of J from forward runs;
+  * the mixed form's gradient against the plain FP64 form's (the FP64
+    reference gradient) on the same 500-lipid copy.
+The exact derivative of a window is checked where it is a derivative a
+finite difference can resolve: on this hot membrane (kT 3) the trajectory's
+sensitivity grows by ~e^(4.6 t / tau), so beyond ~50 steps no difference step
+converges, and the segment-local form (the adjoint restarted at every
+checkpoint) is the bounded estimate; it is checked against the sum of its
+segments' exact adjoints.  Gradient tolerance at the 1e-3 relative
+difference step: 1e-3 per component.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+from conftest import load_golden, mpd_from_golden
+
+import softmold_gb300 as smd
+
+pytestmark = pytest.mark.gpu
+
+PREC = [smd.PLAIN_FP64, smd.MIXED]
+TAIL = 3
+
+
+def with_params(m, umin=None, kbond=None, kbend=None, types=(TAIL, TAIL)):
+    """m with Umin of a type pair (both table rows, rebuilt as
+    laradjiRevaleeFC/PC build them), kbond and kbend replaced."""
+    m2 = dataclasses.replace(m, fconst=m.fconst.copy(), uconst=m.uconst.copy(),
+                             chain_consts=np.array(m.chain_consts, dtype=np.float64).copy())
+    nT = m.n_types
+    if umin is not None:
+        for a, b in {(types[0], types[1]), (types[1], types[0])}:
+            row = 6 * (a * nT + b)
+            U = m2.uconst[row:row + 6]
+            F = m2.fconst[row:row + 6]
+            rm, rc = U[0], U[3]
+            w = rc - rm
+            umax = U[1] * rm * rm + U[2]
+            U[1] = (umax - umin) / (rm * rm)
+            U[2] = umin
+            U[4] = (3.0 * umin) / (w * w)
+            U[5] = (2.0 * umin) / (w * w * w)
+            F[1] = (2.0 * (umax - umin)) / (rm * rm)
+            F[4] = (6.0 * umin) / (w * w)
+            F[5] = (6.0 * umin) / (w * w * w)
+    if kbond is not None:
+        m2.chain_consts[:, 1] = kbond
+    if kbend is not None:
+        m2.chain_consts[:, 3] = kbend
+    return m2
+
+
+def theta0(m, types=(TAIL, TAIL)):
+    row = 6 * (types[0] * m.n_types + types[1])
+    return np.array([m.uconst[row + 2], m.chain_consts[0, 1], m.chain_consts[0, 3]])
+
+
+def mean_potential(m, start, it0, steps, precision, theta=None):
+    """J from a forward run of `steps` steps from the state `start` at loop
+    step it0 (same noise keys as the adjoint's run)."""
+    if theta is not None:
+        m = with_params(m, *theta)
+    m = dataclasses.replace(m, initial_time=it0 * m.dt)
+    s = smd.System(m, precision=precision)
+    s.set_state(*start)
+    tot = 0.0
+    for _ in range(steps):
+        e = s.energy()[0]
+        tot += e["pair"] + e["bonded"]
+        s.advance(1)
+    s.close()
+    return tot / steps
+
+
+@pytest.fixture(scope="module")
+def bilayer500(tmp_path_factory):
+    """500-lipid flat bilayer, barostat off, after 200 steps from the lattice."""
+    p = str(tmp_path_factory.mktemp("adj") / "b.mpd")
+    smd.synth_bilayer(p, 4242, 500, 3.45, 15.0, 0.0, 0.0)
+    m = smd.read_mpd(p)
+    s = smd.System(m, precision=smd.PLAIN_FP64)
+    s.prepare()
+    s.advance(200)
+    start = s.state()
+    s.close()
+    return m, start, 200
+
+
+@pytest.mark.parametrize("precision", PREC)
+def test_hessian_vector_against_oracle_differences(built, oracle, precision):
+    g = load_golden("bil400")
+    s = smd.System(mpd_from_golden(g), precision=precision)
+    rng = np.random.default_rng(5)
+    w = rng.standard_normal(g["pos"].shape)
+    kw = s.hessian_vector(w)
+    eps = 1e-6
+    gp, gm = dict(g), dict(g)
+    gp["pos"] = np.mod(g["pos"] + eps * w, g["box"])
+    gm["pos"] = np.mod(g["pos"] - eps * w, g["box"])
+    fd = (oracle.forces(gp) - oracle.forces(gm)) / (2 * eps)
+    err = np.abs(kw - fd).max() / np.abs(fd).max()
+    print(f"precision {precision}: max |Kw - FD| / max |FD| = {err:.3e}")
+    assert err < (1e-6 if precision == smd.PLAIN_FP64 else 1e-4)
+
+
+def fd_gradient(m, start, it0, steps, precision, rel):
+    th = theta0(m)
+    fd = np.zeros(3)
+    for k in range(3):
+        h = rel * abs(th[k])
+        tp, tm = th.copy(), th.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd[k] = (mean_potential(m, start, it0, steps, precision, tp) -
+                 mean_potential(m, start, it0, steps, precision, tm)) / (2 * h)
+    return fd
+
+
+def adjoint_at(m, start, it0, precision, steps, ckpt, **kw):
+    s = smd.System(dataclasses.replace(m, initial_time=it0 * m.dt), precision=precision)
+    s.set_state(*start)
+    r = s.adjoint(steps, ckpt, **kw)
+    s.close()
+    return r
+
+
+def test_exact_adjoint_against_fp64_differences(built, bilayer500):
+    """FP64: 20 steps in 4 recomputed segments against central differences
+    at 1e-7 relative, where the difference quotient is converged."""
+    m, start, it0 = bilayer500
+    res = adjoint_at(m, start, it0, smd.PLAIN_FP64, 20, 5)
+    j0 = mean_potential(m, start, it0, 20, smd.PLAIN_FP64)
+    assert abs(res["mean_potential"] - j0) <= 1e-7 * abs(j0)  # FP64 sums differ only in order
+    fd = fd_gradient(m, start, it0, 20, smd.PLAIN_FP64, 1e-7)
+    rel = np.abs(res["grad"] - fd) / np.abs(fd)
+    print(f"adjoint {res['grad']}, FD {fd}, rel err {rel}")
+    assert (rel < 1e-5).all()
+    assert (res["grad_area"] == 0).all() and res["mean_area_per_lipid"] > 0
+
+
+@pytest.mark.parametrize("precision", PREC)
+def test_adjoint_against_differences_at_1e3(built, bilayer500, precision):
+    """Both forms, 10 steps in 2 segments, against central differences of
+    the same form at a 1e-3 relative step, Richardson-extrapolated with the
+    half step (the plain quotient's own O(h^2) error reaches 1e-3 on kbend)."""
+    m, start, it0 = bilayer500
+    res = adjoint_at(m, start, it0, precision, 10, 5)
+    j0 = mean_potential(m, start, it0, 10, precision)
+    assert abs(res["mean_potential"] - j0) <= (1e-7 if precision == smd.PLAIN_FP64 else 1e-6) * abs(j0)
+    f1 = fd_gradient(m, start, it0, 10, precision, 1e-3)
+    f2 = fd_gradient(m, start, it0, 10, precision, 5e-4)
+    fd = (4.0 * f2 - f1) / 3.0
+    rel = np.abs(res["grad"] - fd) / np.abs(fd)
+    print(f"precision {precision}: adjoint {res['grad']}, FD {fd}, rel err {rel}")
+    assert (rel < 1e-3).all()
+
+
+def test_mixed_gradient_against_fp64_reference_gradient(built, bilayer500):
+    m, start, it0 = bilayer500
+    out = [adjoint_at(m, start, it0, prec, 20, 10)["grad"] for prec in PREC]
+    rel = np.abs(out[1] - out[0]) / np.abs(out[0])
+    print(f"mixed {out[1]} vs FP64 {out[0]}: rel {rel}")
+    assert (rel < 1e-3).all()
+
+
+def test_segment_local_adjoint_is_the_sum_of_segment_adjoints(built, bilayer500):
+    """200 steps, checkpoints every 20, segment-local: equals the sum over the
+    ten segments of each segment's exact 20-step adjoint (weighted 20/200),
+    and stays bounded where the exact 200-step derivative does not."""
+    m, start, it0 = bilayer500
+    mm = dataclasses.replace(m, initial_time=it0 * m.dt)
+    s = smd.System(mm, precision=smd.MIXED)
+    s.set_state(*start)
+    loc = s.adjoint(200, 20, segment_local=True)
+    t = smd.System(mm, precision=smd.MIXED)
+    t.set_state(*start)
+    acc = np.zeros(3)
+    jsum = 0.0
+    for _ in range(10):
+        r = t.adjoint(20, 20)
+        acc += r["grad"] * (20 / 200)
+        jsum += r["mean_potential"] * (20 / 200)
+    # the same trajectory and terms; only the order of the FP64 atomic sums differs
+    assert np.allclose(loc["grad"], acc, rtol=1e-6, atol=0)
+    assert abs(loc["mean_potential"] - jsum) <= 1e-9 * abs(jsum)
+    exact = adjoint_at(m, start, it0, smd.MIXED, 200, 20)["grad"]
+    print(f"segment-local {loc['grad']}, exact 200-step {exact}")
+    assert np.abs(exact).max() > 100 * np.abs(loc["grad"]).max()
+
+
+def test_adjoint_leaves_the_state_of_the_forward_run(built, bilayer500):
+    """After smd_adjoint(T) the handle holds the state advance(T) reaches, and
+    checkpoint spacing does not change the gradient."""
+    m, start, it0 = bilayer500
+    mm = dataclasses.replace(m, initial_time=it0 * m.dt)
+    a, b, c = (smd.System(mm, precision=smd.MIXED) for _ in range(3))
+    for s in (a, b, c):
+        s.set_state(*start)
+    ga = a.adjoint(60, 20)["grad"]
+    gc = c.adjoint(60, 7)["grad"]
+    b.advance(60)
+    pa, va = a.state()
+    pb, vb = b.state()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    assert np.abs(ga - gc).max() <= 1e-9 * np.abs(ga).max()
+    a.advance(10)
+    b.advance(10)
+    assert np.array_equal(a.state()[0], b.state()[0])
+
+
+def test_autograd_function_wrapper(built, bilayer500):
+    """The C-ABI adjoint as a torch.autograd.Function (test harness only)."""
+    torch = pytest.importorskip("torch")
+    m, start, it0 = bilayer500
+    steps = 10
+
+    class MeanPotential(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, theta):
+            mm = dataclasses.replace(with_params(m, *theta.detach().cpu().numpy()), initial_time=it0 * m.dt)
+            s = smd.System(mm, precision=smd.MIXED)
+            s.set_state(*start)
+            r = s.adjoint(steps, 5)
+            s.close()
+            ctx.save_for_backward(torch.tensor(r["grad"], dtype=torch.float64))
+            return torch.tensor(r["mean_potential"], dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gout):
+            (grad,) = ctx.saved_tensors
+            return gout * grad
+
+    theta = torch.tensor(theta0(m), dtype=torch.float64, requires_grad=True)
+    J = MeanPotential.apply(theta)
+    (2.0 * J).backward()
+    th = theta0(m)
+    for k in range(3):
+        h = 1e-3 * abs(th[k])
+        tp, tm = th.copy(), th.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd = (mean_potential(m, start, it0, steps, smd.MIXED, tp) -
+              mean_potential(m, start, it0, steps, smd.MIXED, tm)) / (2 * h)
+        assert abs(theta.grad[k].item() - 2.0 * fd) <= 1e-3 * abs(2.0 * fd), (k, theta.grad[k].item(), fd)
+
+
+def test_adjoint_rejects_barostat(built, tmp_path):
+    p = str(tmp_path / "b.mpd")
+    smd.synth_bilayer(p, 1, 300, 3.45, 15.0, 0.01, 0.0)
+    s = smd.System(smd.read_mpd(p), precision=smd.MIXED)
+    with pytest.raises(smd.SmdError, match="barostat"):
+        s.adjoint(10, 5)
