@@ -58,6 +58,12 @@ typedef struct smd_system_desc {
   int resize_rate;              /* MC move every resize_rate steps (MD.cpp:67: 8) */
   int first_step;               /* loop index of the first step (initialTime/deltaT) */
   double skin;                  /* Verlet-list skin in sigma (<=0: default 0.5) */
+  int n_bonds;                  /* terms of BOND residues (Blob::doBondForce) */
+  const int* bonds;             /* n_bonds*2 bead indices: first, second */
+  const double* bond_consts;    /* n_bonds*2: l0, k of each term's residue */
+  int n_bends;                  /* terms of BEND residues (Blob::doBendForce) */
+  const int* bends;             /* n_bends*3 bead indices: first, second, third */
+  const double* bend_consts;    /* n_bends*2: a, k of each term's residue */
 } smd_system_desc;
 
 typedef struct smd_system smd_system;
@@ -147,6 +153,22 @@ int smd_prepare(smd_system* h, int do_second, smd_energy* energy_out);
 #define SMD_STOP_AT_MEASURE 1
 #define SMD_ASYNC 2
 int smd_advance(smd_system* h, int steps, int flags);
+
+/* Autotuner of the mixed form's launch configuration (no reference
+ * counterpart): times the Verlet-list build variants (flat stencil with 128 or
+ * 256 threads per cell, octant-filtered) and the pair pass at 4, 8 and 16
+ * lanes per bead on the handle's state, and keeps the fastest of each; every
+ * choice gives bitwise the same trajectory.  smd_advance runs it once per
+ * system shape before its first call of 64 steps or more (environment
+ * SMD_AUTOTUNE=0 turns that off); force = 1 re-times.  Reports the choice
+ * (lanes: 4/8/16; list_kernel: 0 flat-128, 1 flat-256, 2 octant) and, in
+ * ms[6] if not NULL, the best times of the three list variants and of the
+ * three lane counts.  The plain form keeps its fixed configuration. */
+int smd_autotune(smd_system* h, int force, int* lanes, int* list_kernel, float* ms);
+
+/* Sets the launch configuration the autotuner would choose (lanes 4, 8 or
+ * 16; list_kernel 0, 1 or 2) and marks the handle tuned. */
+int smd_set_tuning(smd_system* h, int lanes, int list_kernel);
 
 /* Launch mode of smd_advance: on = 1 (default) runs each barostat period as
  * one CUDA graph whose list builds are conditional nodes; on = 0 launches the

@@ -108,6 +108,12 @@ struct OracleMD {
         for (const auto& b : m.bonds) idx.push_back(b[0]);
         orc_bead_force(N, pos(), sys.type.data(), sys.size, sys.nTypes, (int)idx.size(), idx.data(),
                        m.constants.data(), acc.data());
+      } else if (m.type == smd::MOL_BOND || m.type == smd::MOL_BEND) {
+        const std::vector<int> L = flat_list(m);
+        if (m.type == smd::MOL_BOND)
+          orc_bond_force(pos(), sys.size, (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
+        else
+          orc_bend_force(pos(), sys.size, (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
       } else if (m.type == smd::MOL_SOLID) {
       } else {
         err = "molecule type " + std::to_string(m.type) + " is not supported";
@@ -129,6 +135,14 @@ struct OracleMD {
     orc_pair_force(N, pos(), sys.type.data(), sys.size, sys.cutoff, sys.nTypes,
                    sys.twoBodyFconst.data(), acc.data());
   }
+  // Index list of a BOND (pairs) or BEND (triplets) residue.
+  static std::vector<int> flat_list(const smd::Molecule& m) {
+    const int w = (m.type == smd::MOL_BOND) ? 2 : 3;
+    std::vector<int> L;
+    for (const auto& b : m.bonds)
+      for (int q = 0; q < w; ++q) L.push_back(b[q]);
+    return L;
+  }
   double total_potential(double* beadPot, int* nBeadRes) {
     double pot = orc_pair_potential(N, pos(), sys.type.data(), sys.size, sys.cutoff, sys.nTypes,
                                     sys.twoBodyUconst.data());
@@ -138,6 +152,10 @@ struct OracleMD {
       if (m.type == smd::MOL_CHAIN) {
         for (const auto& b : m.bonds)
           pot += orc_chain_potential(pos(), sys.size, b[0], b[1], b[2], m.constants.data());
+      } else if (m.type == smd::MOL_BOND) {
+        pot += orc_bond_potential(pos(), sys.size, (int)m.bonds.size(), flat_list(m).data(), m.constants.data());
+      } else if (m.type == smd::MOL_BEND) {
+        pot += orc_bend_potential(pos(), sys.size, (int)m.bonds.size(), flat_list(m).data(), m.constants.data());
       } else if (m.type == smd::MOL_BEAD) {
         std::vector<int> idx;
         for (const auto& b : m.bonds) idx.push_back(b[0]);
@@ -157,6 +175,10 @@ struct OracleMD {
       if (m.type == smd::MOL_CHAIN) {
         for (const auto& b : m.bonds)
           dp += orc_chain_dpotential(pos(), sys.size, b[0], b[1], b[2], m.constants.data(), s);
+      } else if (m.type == smd::MOL_BOND) {
+        dp += orc_bond_dpotential(pos(), sys.size, (int)m.bonds.size(), flat_list(m).data(), m.constants.data(), s);
+      } else if (m.type == smd::MOL_BEND) {
+        dp += orc_bend_dpotential(pos(), sys.size, (int)m.bonds.size(), flat_list(m).data(), m.constants.data(), s);
       } else if (m.type == smd::MOL_BEAD) {
         std::vector<int> idx;
         for (const auto& b : m.bonds) idx.push_back(b[0]);

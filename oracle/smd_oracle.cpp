@@ -647,6 +647,94 @@ double orc_chain_dpotential(const double* pos, const double box[3], int start, i
   return chain_potential_impl(pos, box, start, nChains, length, c, scale);
 }
 
+// BOND residue: pairs list[2k], list[2k+1] with constants {l0, k}
+// (Blob::doBondForce / doBondPotential / doBondDPotential,
+// include/system.h:1880-1934, 2718-2745, 3399-3435).
+void orc_bond_force(const double* pos, const double box[3], int nb, const int* list, const double* c,
+                    double* acc) {
+  for (int j = 0; j < nb; ++j) {
+    const int f = list[2 * j], s = list[2 * j + 1];
+    const V3 d = diff(pos, f, s, box);
+    V3 a1 = accv(acc, f), a2 = accv(acc, s);
+    harmonic_force(d, a1, a2, c);
+    setv(acc, f, a1);
+    setv(acc, s, a2);
+  }
+}
+
+static double bond_energy(const double* pos, const double box[3], int nb, const int* list, const double* c,
+                          const double* scale) {
+  double total = 0;
+  for (int j = 0; j < nb; ++j) {
+    V3 d = diff(pos, list[2 * j], list[2 * j + 1], box);
+    const double oldP = harmonic_potential(d, c);
+    if (!scale) {
+      total += oldP;
+      continue;
+    }
+    d.x *= scale[0];
+    d.y *= scale[1];
+    d.z *= scale[2];
+    total += oldP - harmonic_potential(d, c);
+  }
+  return total;
+}
+
+double orc_bond_potential(const double* pos, const double box[3], int nb, const int* list, const double* c) {
+  return bond_energy(pos, box, nb, list, c, nullptr);
+}
+
+double orc_bond_dpotential(const double* pos, const double box[3], int nb, const int* list, const double* c,
+                           const double scale[3]) {
+  return bond_energy(pos, box, nb, list, c, scale);
+}
+
+// BEND residue: triplets list[3k..3k+2] with constants {a, k}
+// (Blob::doBendForce / doBendPotential / doBendDPotential,
+// include/system.h:1975-2040, 2782-2821, 3477-3524).
+void orc_bend_force(const double* pos, const double box[3], int nb, const int* list, const double* c,
+                    double* acc) {
+  for (int j = 0; j < nb; ++j) {
+    const int f = list[3 * j], s = list[3 * j + 1], t = list[3 * j + 2];
+    const V3 da = diff(pos, f, s, box), db = diff(pos, s, t, box);
+    V3 a1 = accv(acc, f), a2 = accv(acc, s), a3 = accv(acc, t);
+    bend_force(da, db, a1, a2, a3, c);
+    setv(acc, f, a1);
+    setv(acc, s, a2);
+    setv(acc, t, a3);
+  }
+}
+
+static double bend_energy(const double* pos, const double box[3], int nb, const int* list, const double* c,
+                          const double* scale) {
+  double total = 0;
+  for (int j = 0; j < nb; ++j) {
+    V3 da = diff(pos, list[3 * j], list[3 * j + 1], box), db = diff(pos, list[3 * j + 1], list[3 * j + 2], box);
+    const double oldP = bend_potential(da, db, c);
+    if (!scale) {
+      total += oldP;
+      continue;
+    }
+    da.x *= scale[0];
+    da.y *= scale[1];
+    da.z *= scale[2];
+    db.x *= scale[0];
+    db.y *= scale[1];
+    db.z *= scale[2];
+    total += oldP - bend_potential(da, db, c);
+  }
+  return total;
+}
+
+double orc_bend_potential(const double* pos, const double box[3], int nb, const int* list, const double* c) {
+  return bend_energy(pos, box, nb, list, c, nullptr);
+}
+
+double orc_bend_dpotential(const double* pos, const double box[3], int nb, const int* list, const double* c,
+                           const double scale[3]) {
+  return bend_energy(pos, box, nb, list, c, scale);
+}
+
 void orc_bead_force(int n, const double* pos, const int* type, const double box[3], int nT, int nb,
                     const int* idx, const double* C, double* acc) {
   // bead-bead pairs (include/system.h:2072-2098); with a single residue the

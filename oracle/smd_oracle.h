@@ -62,6 +62,22 @@ double orc_chain_potential(const double* pos, const double box[3], int start, in
 double orc_chain_dpotential(const double* pos, const double box[3], int start, int nChains,
                             int length, const double* c, const double scale[3]);
 
+// BOND residue: nb pairs list[2k], list[2k+1], constants {l0, k}: forces
+// (Blob::doBondForce, include/system.h:1880-1934), potential (doBondPotential,
+// :2718-2745), size-change difference (doBondDPotential, :3399-3435).
+void orc_bond_force(const double* pos, const double box[3], int nb, const int* list, const double* c, double* acc);
+double orc_bond_potential(const double* pos, const double box[3], int nb, const int* list, const double* c);
+double orc_bond_dpotential(const double* pos, const double box[3], int nb, const int* list, const double* c,
+                           const double scale[3]);
+
+// BEND residue: nb triplets list[3k..3k+2], constants {a, k}: forces
+// (Blob::doBendForce, include/system.h:1975-2040), potential (doBendPotential,
+// :2782-2821), size-change difference (doBendDPotential, :3477-3524).
+void orc_bend_force(const double* pos, const double box[3], int nb, const int* list, const double* c, double* acc);
+double orc_bend_potential(const double* pos, const double box[3], int nb, const int* list, const double* c);
+double orc_bend_dpotential(const double* pos, const double box[3], int nb, const int* list, const double* c,
+                           const double scale[3]);
+
 // BEAD residue (continuum spheres) with bead indices idx[nb], constants
 // C[22*nTypes*nTypes]: force (Blob::doBeadForce brute-force branch,
 // include/system.h:2043-2212), potential (doBeadPotential, :2936-3074) and

@@ -40,6 +40,8 @@ class SystemDesc(C.Structure):
         ("dt", C.c_double), ("gamma", C.c_double), ("temperature", C.c_double),
         ("seed", C.c_uint32), ("tension", C.c_double), ("delta_lxy", C.c_double),
         ("resize_rate", C.c_int), ("first_step", C.c_int), ("skin", C.c_double),
+        ("n_bonds", C.c_int), ("bonds", C.POINTER(C.c_int)), ("bond_consts", C.POINTER(C.c_double)),
+        ("n_bends", C.c_int), ("bends", C.POINTER(C.c_int)), ("bend_consts", C.POINTER(C.c_double)),
     ]
 
 
@@ -91,6 +93,8 @@ _SIGS = {
     "smd_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "smd_sync": (C.c_int, [C.c_void_p]),
     "smd_use_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+    "smd_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "smd_adjoint": (C.c_int, [C.c_void_p, C.POINTER(AdjointSpec), C.POINTER(AdjointResult)]),
     "smd_hessian_vector": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "smd_mpd_update_state": (C.c_int, [C.c_char_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
@@ -170,6 +174,10 @@ class Mpd:
     final_time: float
     sphere_index: np.ndarray | None = None
     sphere_consts: np.ndarray | None = None
+    bonds: np.ndarray | None = None        # (k,2) BOND residue terms
+    bond_consts: np.ndarray | None = None  # (k,2) l0, k per term
+    bends: np.ndarray | None = None        # (k,3) BEND residue terms
+    bend_consts: np.ndarray | None = None  # (k,2) a, k per term
 
 
 def read_mpd(path: str) -> Mpd:
@@ -181,6 +189,7 @@ def read_mpd(path: str) -> Mpd:
     n_types = n_particles = n_mol = 0
     pos = vel = typ = None
     blocks, consts = [], []
+    bond_l, bond_c, bend_l, bend_c = [], [], [], []
     sph_idx, sph_c = None, None
     fc = uc = None
 
@@ -234,6 +243,12 @@ def read_mpd(path: str) -> Mpd:
                     for row in b:
                         blocks.append(row[:3])
                         consts.append(c[:4])
+                elif mt == 6:
+                    bond_l.extend(b[:, :2].tolist())
+                    bond_c.extend([c[:2].tolist()] * nb)
+                elif mt == 7:
+                    bend_l.extend(b[:, :3].tolist())
+                    bend_c.extend([c[:2].tolist()] * nb)
                 elif mt == 9:
                     sph_idx = b[:, 0].astype(np.int32)
                     sph_c = c
@@ -255,7 +270,11 @@ def read_mpd(path: str) -> Mpd:
                dt=vals["deltaT"], gamma=gamma, temperature=vals["initialTemp"], seed=vals["seed"],
                tension=vals.get("tension", 0.0), delta_lxy=vals.get("deltaLXY", 0.0),
                initial_time=vals.get("initialTime", 0.0), final_time=vals.get("finalTime", 0.0),
-               sphere_index=sph_idx, sphere_consts=sph_c)
+               sphere_index=sph_idx, sphere_consts=sph_c,
+               bonds=np.array(bond_l, np.int32).reshape(-1, 2) if bond_l else None,
+               bond_consts=np.array(bond_c, np.float64).reshape(-1, 2) if bond_c else None,
+               bends=np.array(bend_l, np.int32).reshape(-1, 3) if bend_l else None,
+               bend_consts=np.array(bend_c, np.float64).reshape(-1, 2) if bend_c else None)
 
 
 class System:
@@ -290,6 +309,15 @@ class System:
                 d.sphere_index, d.sphere_consts = _ip(arrs["si"]), _dp(arrs["sc"])
             else:
                 d.n_spheres = 0
+            for key, lk, ck in (("bonds", "bl", "bc"), ("bends", "el", "ec")):
+                lst = getattr(m, key, None)
+                if lst is not None and len(lst) > 0:
+                    arrs[lk] = np.ascontiguousarray(lst, np.int32)
+                    arrs[ck] = np.ascontiguousarray(getattr(m, key[:-1] + "_consts"), np.float64)
+            if "bl" in arrs:
+                d.n_bonds, d.bonds, d.bond_consts = len(arrs["bl"]), _ip(arrs["bl"]), _dp(arrs["bc"])
+            if "el" in arrs:
+                d.n_bends, d.bends, d.bend_consts = len(arrs["el"]), _ip(arrs["el"]), _dp(arrs["ec"])
             d.dt, d.gamma, d.temperature = m.dt, m.gamma, m.temperature
             d.seed = m.seed & 0xffffffff
             d.tension, d.delta_lxy = m.tension, m.delta_lxy
@@ -391,6 +419,16 @@ class System:
         out = np.zeros((self.n, 3))
         _check(lib().smd_hessian_vector(self.h, ww.ctypes.data, out.ctypes.data), "smd_hessian_vector")
         return out
+
+    def autotune(self, force=False):
+        """smd_autotune: (lanes per bead, list kernel, [list ms x3, pair-pass ms x3])."""
+        lanes, kern = C.c_int(0), C.c_int(0)
+        ms = (C.c_float * 6)()
+        _check(lib().smd_autotune(self.h, 1 if force else 0, C.byref(lanes), C.byref(kern), ms), "smd_autotune")
+        return lanes.value, kern.value, list(ms)
+
+    def set_tuning(self, lanes, list_kernel):
+        _check(lib().smd_set_tuning(self.h, int(lanes), int(list_kernel)), "smd_set_tuning")
 
     def use_graphs(self, on=True):
         _check(lib().smd_use_graphs(self.h, 1 if on else 0), "smd_use_graphs")

@@ -44,13 +44,24 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   // residues on the device path
   std::vector<int> blocks;
   std::vector<double> consts;
-  std::vector<int> sphere_idx;
+  std::vector<int> sphere_idx, bond_idx, bend_idx;
+  std::vector<double> bond_c, bend_c;
   const std::vector<double>* sphere_consts = nullptr;
   for (const smd::Molecule& m : S.mol) {
     if (m.type == smd::MOL_CHAIN) {
       for (const auto& b : m.bonds) {
         blocks.insert(blocks.end(), {b[0], b[1], b[2]});
         consts.insert(consts.end(), m.constants.begin(), m.constants.begin() + 4);
+      }
+    } else if (m.type == smd::MOL_BOND) {
+      for (const auto& b : m.bonds) {
+        bond_idx.insert(bond_idx.end(), {b[0], b[1]});
+        bond_c.insert(bond_c.end(), m.constants.begin(), m.constants.begin() + 2);
+      }
+    } else if (m.type == smd::MOL_BEND) {
+      for (const auto& b : m.bonds) {
+        bend_idx.insert(bend_idx.end(), {b[0], b[1], b[2]});
+        bend_c.insert(bend_c.end(), m.constants.begin(), m.constants.begin() + 2);
       }
     } else if (m.type == smd::MOL_BEAD) {
       if (sphere_consts) {
@@ -61,7 +72,7 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
       sphere_consts = &m.constants;
     } else if (m.type != smd::MOL_SOLID) {
       std::cout << "Error(MD): molecule type " << m.type
-                << " is not on the GPU step of this build (supported: CHAIN, BEAD)\n";
+                << " is not on the GPU step of this build (supported: CHAIN, BOND, BEND, BEAD)\n";
       return 1;
     }
   }
@@ -107,6 +118,12 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   d.n_spheres = (int)sphere_idx.size();
   d.sphere_index = sphere_idx.data();
   d.sphere_consts = sphere_consts ? sphere_consts->data() : nullptr;
+  d.n_bonds = (int)bond_idx.size() / 2;
+  d.bonds = bond_idx.data();
+  d.bond_consts = bond_c.data();
+  d.n_bends = (int)bend_idx.size() / 3;
+  d.bends = bend_idx.data();
+  d.bend_consts = bend_c.data();
   d.dt = S.deltaT;
   d.gamma = gamma;
   d.temperature = S.initialTemp;

@@ -5,7 +5,12 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <memory>
 #include <string>
 #include <vector>
@@ -46,6 +51,7 @@ struct smd_system {
   bool mixed = true;
   int n = 0, n_rep = 0, npad = 0, kmax = 0, n_cells = 0, n_tiles = 0;
   int n_sph = 0;  // BEAD sphere beads
+  int n_terms = 0;  // BOND / BEND term entries
   long long n_chains = 0;  // CHAIN molecules (lipids)
   // adjoint work arrays (allocated by the first adjoint call)
   struct Adj {
@@ -90,6 +96,16 @@ struct smd_system {
     int kernels = 0;  // kernel nodes outside the conditional bodies
   } graph[2];
   bool use_graphs = true;
+  // launch configuration chosen by the autotuner (mixed form): lanes per bead
+  // of the pair pass and the list-build kernel (0 flat/128, 1 flat/256,
+  // 2 octant/256); every choice gives bitwise the same trajectory
+  struct Tune {
+    int lanes = kLanes;
+    int list = 0;
+    bool done = false;
+    float ms_list[3] = {0, 0, 0};
+    float ms_force[3] = {0, 0, 0};
+  } tune;
   cudaStream_t side = nullptr;  // captures the conditional bodies
   long long graph_builds = 0;   // device count of list builds run inside graphs
 
@@ -115,7 +131,7 @@ struct smd_system {
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
   int grid() const { return (n + kBlock - 1) / kBlock; }
-  int grid_lanes() const { return (int)(((long long)n * kLanes + kBlock - 1) / kBlock); }
+  int grid_lanes(int g = kLanes) const { return (int)(((long long)n * g + kBlock - 1) / kBlock); }
   int sms = 152;
   // list build: one CTA per cell; the hardware scheduler balances the very
   // uneven cell occupancy of a membrane better than a fixed stride does
@@ -162,7 +178,11 @@ int launch_rebuild(smd_system* h, cudaStream_t st, int cur, int in_graph) {
   SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, st>>>(P));
   if (h->mixed) {
     SMD_LAUNCH(h, k_reorder<true><<<g, kBlock, 0, st>>>(P, cur));
-    SMD_LAUNCH(h, (k_nbr_cells_oct<<<h->nbr_grid(), kOctThreads, 0, st>>>(P, cur)));
+    switch (h->tune.list) {
+      case 1: SMD_LAUNCH(h, (k_nbr_cells_flat<256><<<h->nbr_grid(), 256, 0, st>>>(P, cur))); break;
+      case 2: SMD_LAUNCH(h, (k_nbr_cells_oct<<<h->nbr_grid(), kOctThreads, 0, st>>>(P, cur))); break;
+      default: SMD_LAUNCH(h, (k_nbr_cells_flat<128><<<h->nbr_grid(), 128, 0, st>>>(P, cur))); break;
+    }
   } else {
     SMD_LAUNCH(h, k_reorder<false><<<g, kBlock, 0, st>>>(P, cur));
     SMD_LAUNCH(h, (k_nbr_cells_plain<<<h->nbr_grid(), kNbrThreads, 0, st>>>(P, cur)));
@@ -219,7 +239,20 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   }
   const int gl = h->grid_lanes();
   if (h->mixed) {
-    SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
+    if constexpr (FL == 0 || FL == (F_STOP | F_DU)) {  // the loop's pair passes follow the tuner
+      switch (h->tune.lanes) {
+        case 4:
+          SMD_LAUNCH(h, (k_force<true, FL, 4><<<h->grid_lanes(4), kBlock, 0, h->stream>>>(P, h->cur)));
+          break;
+        case 16:
+          SMD_LAUNCH(h, (k_force<true, FL, 16><<<h->grid_lanes(16), kBlock, 0, h->stream>>>(P, h->cur)));
+          break;
+        default:
+          SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
+      }
+    } else {
+      SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
+    }
     SMD_LAUNCH(h, (k_integ<true, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, se)));
     if (h->n_sph) SMD_LAUNCH(h, (k_sphere<true, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   } else {
@@ -229,6 +262,17 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   }
   if (kLoopStep && h->profile) {
     if (int rc = prof_mark(h)) return rc;
+  }
+  return 0;
+}
+
+// The loop's pair pass alone (its output is scratch until k_integ reads it).
+int launch_force_only(smd_system* h) {
+  auto& P = h->P;
+  switch (h->tune.lanes) {
+    case 4: SMD_LAUNCH(h, (k_force<true, 0, 4><<<h->grid_lanes(4), kBlock, 0, h->stream>>>(P, h->cur))); break;
+    case 16: SMD_LAUNCH(h, (k_force<true, 0, 16><<<h->grid_lanes(16), kBlock, 0, h->stream>>>(P, h->cur))); break;
+    default: SMD_LAUNCH(h, (k_force<true, 0, kLanes><<<h->grid_lanes(), kBlock, 0, h->stream>>>(P, h->cur)));
   }
   return 0;
 }
@@ -389,6 +433,13 @@ int validate(const smd_system_desc& d, std::string& why) {
     }
     if (!(d.sphere_consts[kBeadRadiusConst] > 0)) return why = "BEAD radius must be positive", 1;
   }
+  if (d.n_bonds < 0 || d.n_bends < 0) return why = "negative BOND / BEND term count", 1;
+  if (d.n_bonds > 0 && (!d.bonds || !d.bond_consts)) return why = "null BOND array in descriptor", 1;
+  if (d.n_bends > 0 && (!d.bends || !d.bend_consts)) return why = "null BEND array in descriptor", 1;
+  for (int k = 0; k < 2 * d.n_bonds; ++k)
+    if (d.bonds[k] < 0 || d.bonds[k] >= d.n) return why = "BOND bead index out of range", 1;
+  for (int k = 0; k < 3 * d.n_bends; ++k)
+    if (d.bends[k] < 0 || d.bends[k] >= d.n) return why = "BEND bead index out of range", 1;
   if (!(d.dt > 0)) return why = "dt must be positive", 1;
   return 0;
 }
@@ -481,6 +532,8 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   T.inv_fscale = 1.0 / (double)T.fscale;
   // chain constant sets
   std::vector<std::array<double, 4>> sets;
+  std::vector<std::array<double, 2>> tsets;
+  std::vector<std::vector<int4>> bead_terms(total);
   std::vector<int> cinfo(total, 0);
   std::vector<int> type(total, 0);
   h->rp.resize(n_rep);
@@ -494,6 +547,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     p.kT = d.temperature;
     p.sigma = std::sqrt((6.0 * d.temperature * d.gamma) / d.dt);
     p.sig31 = p.sigma * (1.0 / 2147483648.0);
+    p.sig31f = (float)p.sig31;
     p.tension = d.tension;
     p.dlxy = d.delta_lxy;
     p.seed = d.seed;
@@ -530,12 +584,40 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
       if (cinfo[bead + d.sphere_index[k]] != 0) return fail(1, "a BEAD bead is also a CHAIN member");
       cinfo[bead + d.sphere_index[k]] = (int)(0xC0000000u | (unsigned)k);
     }
+    // BOND / BEND terms: per-bead entries (file order), constant sets shared
+    auto term_set = [&](double c0, double c1) -> int {
+      const std::array<double, 2> c = {c0, c1};
+      for (size_t q = 0; q < tsets.size(); ++q)
+        if (tsets[q] == c) return (int)q;
+      if ((int)tsets.size() >= kMaxTermSets) return -1;
+      tsets.push_back(c);
+      return (int)tsets.size() - 1;
+    };
+    for (int k = 0; k < d.n_bonds; ++k) {
+      const int set = term_set(d.bond_consts[2 * k], d.bond_consts[2 * k + 1]);
+      if (set < 0) return fail(1, "too many distinct BOND / BEND constant sets");
+      const int a = bead + d.bonds[2 * k], b = bead + d.bonds[2 * k + 1];
+      bead_terms[a].push_back(make_int4(0 | (0 << 1) | (set << 3), a, b, -1));
+      bead_terms[b].push_back(make_int4(0 | (1 << 1) | (set << 3), a, b, -1));
+    }
+    for (int k = 0; k < d.n_bends; ++k) {
+      const int set = term_set(d.bend_consts[2 * k], d.bend_consts[2 * k + 1]);
+      if (set < 0) return fail(1, "too many distinct BOND / BEND constant sets");
+      const int a = bead + d.bends[3 * k], b = bead + d.bends[3 * k + 1], c = bead + d.bends[3 * k + 2];
+      for (int role = 0; role < 3; ++role)
+        bead_terms[role == 0 ? a : (role == 1 ? b : c)].push_back(make_int4(1 | (role << 1) | (set << 3), a, b, c));
+    }
     bead += d.n;
   }
   for (int r = 1; r < n_rep; ++r)
     if (h->first_step[r] != h->first_step[0]) return fail(1, "replicas of a batch must start at the same step");
   h->it = h->first_step[0];
   T.n_sets = (int)sets.size();
+  for (size_t q = 0; q < tsets.size(); ++q)
+    for (int k = 0; k < 2; ++k) {
+      T.termD[q][k] = tsets[q][k];
+      T.termF[q][k] = (float)tsets[q][k];
+    }
   for (size_t q = 0; q < sets.size(); ++q)
     for (int k = 0; k < 4; ++k) {
       T.chainD[q][k] = sets[q][k];
@@ -616,6 +698,27 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     P.sphCf = fC;
     P.n_sph = sd.n;
     h->n_sph = sd.n;
+  }
+  // ---- BOND / BEND term entries
+  {
+    std::vector<int> off(total + 1, 0);
+    std::vector<int4> flat;
+    for (int b = 0; b < total; ++b) {
+      off[b] = (int)flat.size();
+      flat.insert(flat.end(), bead_terms[b].begin(), bead_terms[b].end());
+    }
+    off[total] = (int)flat.size();
+    if (!flat.empty()) {
+      int* doff = nullptr;
+      int4* dterms = nullptr;
+      if ((rc = h->alloc(&doff, total + 1)) || (rc = h->alloc(&dterms, flat.size()))) return rc;
+      SMD_CUDA(cudaMemcpy(doff, off.data(), (total + 1) * sizeof(int), cudaMemcpyHostToDevice));
+      SMD_CUDA(cudaMemcpy(dterms, flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice));
+      P.term_off = doff;
+      P.terms = dterms;
+      P.n_terms = (int)flat.size();
+      h->n_terms = P.n_terms;
+    }
   }
   // ---- upload state (sorted order = file order until the first build)
   {
@@ -1014,6 +1117,113 @@ int capture_period(smd_system* h, int cur0) {
   return 0;
 }
 
+// ------------------------------------------------------------ autotuner
+// Times the list-build variants (whole rebuild sequence) and the pair pass at
+// 4, 8 and 16 lanes per bead on the handle's own state with CUDA events and
+// keeps the fastest of each.  Both are safe to repeat on a live state: a
+// rebuild re-sorts the same positions, the pair pass only writes its scratch
+// accumulator.  Choices are cached per device and system shape.
+struct TuneKey {
+  int dev, n, n_rep, n_cells;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(dev, n, n_rep, n_cells) < std::tie(o.dev, o.n, o.n_rep, o.n_cells);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+
+int time_ms(smd_system* h, const std::function<int()>& work, int reps, float* best) {
+  cudaEvent_t a, b;
+  SMD_CUDA(cudaEventCreate(&a));
+  SMD_CUDA(cudaEventCreate(&b));
+  float m = 1e30f;
+  int rc = 0;
+  for (int k = 0; k < reps && !rc; ++k) {
+    cudaEventRecord(a, h->stream);
+    rc = work();
+    cudaEventRecord(b, h->stream);
+    if (cudaEventSynchronize(b) != cudaSuccess) rc = fail(2, "autotune: event synchronisation failed");
+    float t = 0;
+    cudaEventElapsedTime(&t, a, b);
+    m = std::min(m, t);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *best = m;
+  return rc;
+}
+
+void drop_graphs(smd_system* h) {
+  for (auto& gr : h->graph)
+    if (gr.exec) {
+      cudaGraphExecDestroy(gr.exec);
+      gr.exec = nullptr;
+    }
+}
+
+int autotune(smd_system* h, bool force) {
+  if (!h->mixed || (h->tune.done && !force)) return 0;
+  int dev = 0;
+  SMD_CUDA(cudaGetDevice(&dev));
+  const TuneKey key{dev, h->n, h->n_rep, h->n_cells};
+  if (!force) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      h->tune.lanes = it->second.first;
+      h->tune.list = it->second.second;
+      h->tune.done = true;
+      drop_graphs(h);
+      return 0;
+    }
+  }
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (int rc = complete_pending(h)) return rc;
+  const long saved = h->launches;
+  auto& P = h->P;
+  // the tuning rebuilds are not list rebuilds of the run: keep the count
+  long long rebuilds0 = 0;
+  SMD_CUDA(cudaMemcpy(&rebuilds0, &P.g->n_rebuilds, sizeof rebuilds0, cudaMemcpyDeviceToHost));
+  int best_list = 0;
+  for (int v = 0; v < 3; ++v) {
+    h->tune.list = v;
+    int rc = time_ms(h, [&]() -> int {
+      SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 1));
+      return rebuild_if_needed(h, true);
+    }, 3, &h->tune.ms_list[v]);
+    if (rc) return rc;
+    if (h->tune.ms_list[v] < h->tune.ms_list[best_list]) best_list = v;
+  }
+  h->tune.list = best_list;
+  // leave a list built by the chosen kernel
+  SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 1));
+  if (int rc = rebuild_if_needed(h, true)) return rc;
+  const int lanes[3] = {4, 8, 16};
+  int best_lanes = 1;
+  for (int v = 0; v < 3; ++v) {
+    h->tune.lanes = lanes[v];
+    int rc = time_ms(h, [&]() -> int { return launch_force_only(h); }, 5, &h->tune.ms_force[v]);
+    if (rc) return rc;
+    if (h->tune.ms_force[v] < h->tune.ms_force[best_lanes]) best_lanes = v;
+  }
+  h->tune.lanes = lanes[best_lanes];
+  h->tune.done = true;
+  h->launches = saved;  // tuning launches are not step work
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  SMD_CUDA(cudaMemcpy(&P.g->n_rebuilds, &rebuilds0, sizeof rebuilds0, cudaMemcpyHostToDevice));
+  drop_graphs(h);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = {h->tune.lanes, h->tune.list};
+  }
+  return read_error(h);
+}
+
+bool autotune_enabled() {
+  const char* e = std::getenv("SMD_AUTOTUNE");
+  return !(e && e[0] == '0');
+}
+
 // A period graph can run from step `it` when its trial step (the last) is a
 // barostat step of the reference loop, i.e. it % resize_rate == 1.
 bool graph_fits(const smd_system* h, long long it, int left) {
@@ -1029,6 +1239,7 @@ int smd_advance(smd_system* h, int steps, int flags) {
   const bool async = (flags & SMD_ASYNC) != 0;
   int rc = complete_pending(h);
   if (rc) return rc;
+  if (!h->tune.done && steps >= 64 && autotune_enabled() && (rc = autotune(h, false))) return rc;
   int done = 0;
   while (done < steps) {
     const int chunk = std::min(steps - done, kTrialChunk * std::max(1, h->resize_rate) / 2);
@@ -1075,6 +1286,31 @@ int smd_advance(smd_system* h, int steps, int flags) {
   }
   if (async) return 0;
   return smd_sync(h);
+}
+
+int smd_autotune(smd_system* h, int force, int* lanes, int* list_kernel, float* ms) {
+  if (!h) return fail(1, "null handle");
+  if (int rc = autotune(h, force != 0)) return rc;
+  if (lanes) *lanes = h->tune.lanes;
+  if (list_kernel) *list_kernel = h->tune.list;
+  if (ms)
+    for (int k = 0; k < 3; ++k) {
+      ms[k] = h->tune.ms_list[k];
+      ms[3 + k] = h->tune.ms_force[k];
+    }
+  return 0;
+}
+
+int smd_set_tuning(smd_system* h, int lanes, int list_kernel) {
+  if (!h) return fail(1, "null handle");
+  if (!(lanes == 4 || lanes == 8 || lanes == 16) || list_kernel < 0 || list_kernel > 2)
+    return fail(1, "lanes must be 4, 8 or 16 and list_kernel 0, 1 or 2");
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  h->tune.lanes = lanes;
+  h->tune.list = list_kernel;
+  h->tune.done = true;
+  drop_graphs(h);
+  return 0;
 }
 
 int smd_use_graphs(smd_system* h, int on) {
@@ -1137,6 +1373,7 @@ int smd_set_temperature(smd_system* h, int replica, double kT, int update_sigma)
     if (update_sigma) {
       h->rp[r].sigma = std::sqrt((6.0 * kT * h->rp[r].gamma) / h->rp[r].dt);
       h->rp[r].sig31 = h->rp[r].sigma * (1.0 / 2147483648.0);
+      h->rp[r].sig31f = (float)h->rp[r].sig31;
     }
   }
   SMD_CUDA(cudaMemcpyAsync(h->P.rp, h->rp.data(), h->n_rep * sizeof(RepParams), cudaMemcpyHostToDevice,
@@ -1225,6 +1462,7 @@ int adj_check_handle(smd_system* h) {
   if (!h) return fail(1, "null handle");
   if (h->n_rep != 1) return fail(1, "the adjoint runs on single-system handles");
   if (h->n_sph) return fail(1, "the adjoint does not cover BEAD residues");
+  if (h->n_terms) return fail(1, "the adjoint does not cover BOND / BEND residues");
   return 0;
 }
 

@@ -23,6 +23,7 @@ namespace smd {
 
 constexpr int kMaxTypes = 8;
 constexpr int kMaxChainSets = 32;
+constexpr int kMaxTermSets = 64;  // distinct constant pairs of BOND / BEND residues
 constexpr int kBlock = 256;
 constexpr int kScanTile = 2048;  // cells per scan block (256 threads x 8)
 constexpr int kLanes = 8;        // lanes per bead in the list build and the pair pass
@@ -40,6 +41,7 @@ __host__ __device__ inline int cinfo_pack(int p, int len, int set) {
 struct RepParams {  // per replica, fixed
   double dt, gamma, kT, sigma, tension, dlxy;
   double sig31;      // sigma * 2^-31: noise amplitude per unit of a signed 32-bit draw
+  float sig31f;      // the same in FP32 (the mixed form's noise is a force term, FP32)
   uint32_t seed;
   int resize_rate;
   int bead_begin, bead_end;
@@ -129,6 +131,8 @@ struct Tables {  // force/potential tables (float and double) in constant-like m
   double dU[6 * kMaxTypes * kMaxTypes];
   float chainF[kMaxChainSets][4];
   double chainD[kMaxChainSets][4];
+  float termF[kMaxTermSets][2];   // BOND {l0, k} / BEND {a, k} constant sets
+  double termD[kMaxTermSets][2];
 };
 
 // All device pointers of one handle.
@@ -159,6 +163,13 @@ struct DevPtrs {
   double* ext_noise; // n*3 noise in sorted order (test hook)
   double* force_out; // n*3 scratch for host reads (file order)
   int* key_out;
+  // BOND / BEND residue terms of each bead, file order: entries
+  // terms[term_off[o] .. term_off[o+1]) of bead o; an entry is {kind | role<<1
+  // | set<<3, first, second, third} (kind 0 bond, 1 bend; role = the bead's
+  // position in the term; global bead indices, third -1 for a bond)
+  int n_terms;
+  const int* term_off;
+  const int4* terms;
   int n_sph;         // BEAD beads (0: none)
   SphereDev* sph;
   const double* sphC;  // kBeadConst * nT^2 BEAD constants
@@ -255,6 +266,19 @@ __device__ __forceinline__ void langevin_noise(uint32_t seed, int orig, long lon
   out[0] = fma((double)(int)(r.x ^ 0x80000000u), sig31, half);
   out[1] = fma((double)(int)(r.y ^ 0x80000000u), sig31, half);
   out[2] = fma((double)(int)(r.z ^ 0x80000000u), sig31, half);
+}
+
+// The same draws in FP32 for the mixed form, where the noise is summed with
+// the other FP32 force terms: psi keeps 24 of its 32 bits.
+__device__ __forceinline__ void langevin_noise_f(uint32_t seed, int orig, long long it, int phase, float sig31f,
+                                                 float out[3]) {
+  const uint4 c = make_uint4((unsigned)orig, (unsigned)(it & 0xffffffff),
+                             (unsigned)((unsigned long long)it >> 32) ^ ((unsigned)phase << 31), 0x6D2Bu);
+  const uint4 r = philox4x32(c, make_uint2(seed, 0x5A17u));
+  const float half = 0.5f * sig31f;
+  out[0] = fmaf((float)(int)(r.x ^ 0x80000000u), sig31f, half);
+  out[1] = fmaf((float)(int)(r.y ^ 0x80000000u), sig31f, half);
+  out[2] = fmaf((float)(int)(r.z ^ 0x80000000u), sig31f, half);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {

@@ -657,6 +657,135 @@ __global__ void __launch_bounds__(kOctThreads) k_nbr_cells_oct(DevPtrs P, int cu
   for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) nbr_cell_oct(P, cur, c);
 }
 
+// ---- Mixed form, flat stencil.  The CTA stages the stencil's beads as FP32
+// offsets from the cell centre (exact 32-bit fractional differences, scaled
+// once), one x-row segment after another with no per-candidate search, and
+// each warp tests one bead of the cell against every staged candidate.  Few
+// barriers and 16 KB of shared memory per CTA: at the ~30 beads of an
+// occupied membrane cell this costs fewer instructions than filtering the
+// stencil per octant first.
+constexpr int kFlatChunk = 1024;  // staged candidates per pass (16 KB)
+
+// One bead (one warp) against mpad staged candidates (a multiple of 32):
+// appends the hits within lc2 to the bead's list from position count.
+template <bool THIN>
+__device__ __forceinline__ int flat_scan(const float4* stage, int mpad, float xi, float yi, float zi, int i,
+                                         float lc2, float bx, float by, float bz, int* out, int count, int kmax,
+                                         int lane) {
+  const unsigned int below = (1u << lane) - 1u;
+#pragma unroll 4
+  for (int k0 = 0; k0 < mpad; k0 += 32) {
+    const float4 cj = stage[k0 + lane];
+    float dx = xi - cj.x, dy = yi - cj.y, dz = zi - cj.z;
+    if constexpr (THIN) {  // fewer than 3 cells on an axis: minimum image per pair
+      dx -= bx * rintf(dx / bx);
+      dy -= by * rintf(dy / by);
+      dz -= bz * rintf(dz / bz);
+    }
+    const int j = __float_as_int(cj.w);
+    bool hit = (dx * dx + dy * dy + dz * dz < lc2) & (j != i);
+    if constexpr (THIN) hit = hit & (j >= 0);  // the minimum image can fold a sentinel back
+    const unsigned int hits = __ballot_sync(0xffffffffu, hit);
+    if (hits) {
+      const int slot = count + __popc(hits & below);
+      if (hit && slot < kmax) out[slot] = j;
+      count += __popc(hits);
+    }
+  }
+  return count;
+}
+
+template <int NT>
+__device__ __forceinline__ void nbr_cell_flat(const DevPtrs& P, int cur, int c) {
+  const int s0 = P.cell_start[c], e0 = P.cell_start[c + 1];
+  if (s0 >= e0) return;
+  __shared__ CellCtx qs;
+  __shared__ unsigned int cr_s[3];
+  __shared__ int seg_s[18], seg_len[18], seg_p[19];
+  __shared__ int cnt[kNbrMaxCell];
+  __shared__ float4 stage[kFlatChunk];
+  __syncthreads();  // the previous cell of this CTA is done with the shared arrays
+  if (threadIdx.x == 0) {
+    const CellCtx q0 = cell_ctx(P, c, s0, e0);
+    qs = q0;
+    cr_s[0] = cell_centre_frac(q0.cx, q0.n0);
+    cr_s[1] = cell_centre_frac(q0.cy, q0.n1);
+    cr_s[2] = cell_centre_frac(q0.cz, q0.n2);
+  }
+  __syncthreads();
+  const CellCtx q = qs;
+  const RepState& rs = P.rs[q.r];
+  const int nb = q.e - q.s;
+  if (nb > kNbrMaxCell) {
+    if (threadIdx.x == 0) atomicOr(&P.g->error, 2);
+    return;
+  }
+  copy_back<true, NT>(P, cur, q, rs);
+  stencil_rows(P, q, seg_s, seg_len);
+  for (int b = threadIdx.x; b < nb; b += NT) cnt[b] = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {  // prefix sums over the 18 slots, empty ones dropped
+    int k = 0, acc = 0;
+    for (int t = 0; t < 18; ++t) {
+      if (seg_len[t] == 0) continue;
+      seg_s[k] = seg_s[t];
+      seg_p[k] = acc;
+      acc += seg_len[t];
+      ++k;
+    }
+    seg_p[k] = acc;
+    seg_len[0] = k;
+  }
+  __syncthreads();
+  const int nseg = seg_len[0];
+  const int M = seg_p[nseg];
+  const unsigned int crx = cr_s[0], cry = cr_s[1], crz = cr_s[2];
+  const float sx = rs.len_per_frac[0], sy = rs.len_per_frac[1], sz = rs.len_per_frac[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int kmax = P.kmax;
+  const float lcut = P.tab->list_cut_f + 1e-4f;
+  const float lc2 = lcut * lcut;
+  const bool thin = q.n0 < 3 || q.n1 < 3 || q.n2 < 3;
+  const float bx = sx * 4294967296.0f, by = sy * 4294967296.0f, bz = sz * 4294967296.0f;
+  for (int base = 0; base < M; base += kFlatChunk) {
+    const int m = min(kFlatChunk, M - base);
+    const int mpad = (m + 31) & ~31;
+    if (base > 0) __syncthreads();  // every warp is done with the previous chunk
+    for (int t = 0; t < nseg; ++t) {
+      const int ps = seg_p[t];
+      const int lo = max(ps, base), hi = min(seg_p[t + 1], base + m);
+      for (int g = lo + threadIdx.x; g < hi; g += NT) {
+        const int j = seg_s[t] + (g - ps);
+        const uint4 mj = P.mt[j];
+        stage[g - base] = make_float4((float)(int)(mj.x - crx) * sx, (float)(int)(mj.y - cry) * sy,
+                                      (float)(int)(mj.z - crz) * sz, __int_as_float(j));
+      }
+    }
+    // far sentinels complete the last round of 32 (index -1 matches no bead)
+    for (int k = m + threadIdx.x; k < mpad; k += NT) stage[k] = make_float4(1e30f, 1e30f, 1e30f, __int_as_float(-1));
+    __syncthreads();
+    for (int b = warp; b < nb; b += NT / 32) {
+      const int i = q.s + b;
+      const uint4 mi = P.mt[i];
+      const float xi = (float)(int)(mi.x - crx) * sx, yi = (float)(int)(mi.y - cry) * sy,
+                  zi = (float)(int)(mi.z - crz) * sz;
+      int* out = P.nbr + (size_t)i * kmax;
+      const int count = thin ? flat_scan<true>(stage, mpad, xi, yi, zi, i, lc2, bx, by, bz, out, cnt[b], kmax, lane)
+                             : flat_scan<false>(stage, mpad, xi, yi, zi, i, lc2, bx, by, bz, out, cnt[b], kmax, lane);
+      if (lane == 0) cnt[b] = count;
+    }
+  }
+  __syncthreads();
+  list_counts(P, q, cnt, NT);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_nbr_cells_flat(DevPtrs P, int cur) {
+  if (!P.g->rebuild) return;
+  list_build_begin(P);
+  for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) nbr_cell_flat<NT>(P, cur, c);
+}
+
 // ------------------------------------------------------------ the step
 // Per-bead CHAIN terms.  The bead at chain position p takes its share of the
 // bonds (p-1,p), (p,p+1) and of the bends (p-2,p-1,p), (p-1,p,p+1),
@@ -774,6 +903,37 @@ __device__ __forceinline__ void chain_vectors(const DevPtrs& P, int cur, int i, 
       e[k].y = (RT)d[1];
       e[k].z = (RT)d[2];
     }
+  }
+}
+
+// x(a) - x(b) for global (file-order) bead indices of a BOND / BEND term
+// (include/system.h:1897-1906, 1992-2011).  MIXED: exact from the 32-bit
+// fractional mirror; PLAIN: FP64 with the reference's half-box shift.
+template <bool MIXED, typename RT>
+__device__ __forceinline__ Vec3<RT> term_vec(const DevPtrs& P, int cur, int a, int b, const double box[3],
+                                             const RepState& rs) {
+  const int ia = P.inv[a], ib = P.inv[b];
+  if constexpr (MIXED) {
+    const uint4 ma = P.m4[cur][ia], mb = P.m4[cur][ib];
+    RT s0, s1, s2;
+    if constexpr (std::is_same<RT, float>::value) {
+      s0 = rs.len_per_frac[0];
+      s1 = rs.len_per_frac[1];
+      s2 = rs.len_per_frac[2];
+    } else {
+      s0 = box[0] * (1.0 / 4294967296.0);
+      s1 = box[1] * (1.0 / 4294967296.0);
+      s2 = box[2] * (1.0 / 4294967296.0);
+    }
+    return Vec3<RT>{(RT)(int)(ma.x - mb.x) * s0, (RT)(int)(ma.y - mb.y) * s1, (RT)(int)(ma.z - mb.z) * s2};
+  } else {
+    const double4 ma = P.d4[cur][ia], mb = P.d4[cur][ib];
+    double d[3] = {ma.x - mb.x, ma.y - mb.y, ma.z - mb.z};
+    for (int k = 0; k < 3; ++k) {
+      if (d[k] > box[k] / 2.0) d[k] -= box[k];
+      if (d[k] < -box[k] / 2.0) d[k] += box[k];
+    }
+    return Vec3<RT>{(RT)d[0], (RT)d[1], (RT)d[2]};
   }
 }
 
@@ -966,8 +1126,9 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
             const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
             const float rn2 = r2 + q;
             if (r2 < rc2 || rn2 < rc2) {
-              const float rr = sqrtf(r2), rn = sqrtf(rn2);
-              dq += __float2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, q / (rn + rr), T.rcf) * 4294967296.0f);
+              const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
+              dq += __float2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
+                                  4294967296.0f);
             }
           }
           if (r2 < rc2) {
@@ -992,8 +1153,9 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
           const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
           const float rn2 = r2 + q;
           if (r2 < rc2 || rn2 < rc2) {
-            const float rr = sqrtf(r2), rn = sqrtf(rn2);
-            dq += __float2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, q / (rn + rr), T.rcf) * 4294967296.0f);
+            const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
+            dq += __float2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
+                                4294967296.0f);
           }
         }
         if (r2 < rc2) {
@@ -1156,6 +1318,50 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
         }
       }
     }
+    // ---- BOND / BEND residue terms of this bead, in entry order
+    if constexpr ((FL & F_PAIRONLY) == 0) {
+      if (P.n_terms > 0) {
+        const int o = P.orig[i];
+        const int e1 = P.term_off[o + 1];
+        for (int e = P.term_off[o]; e < e1; ++e) {
+          const int4 t = P.terms[e];
+          const int role = (t.x >> 1) & 3, set = t.x >> 3;
+          const R* cf;
+          if constexpr (MIXED) cf = T.termF[set]; else cf = T.termD[set];
+          const double* cd = T.termD[set];
+          if ((t.x & 1) == 0) {  // bond (first, second): the bead's force is mag (x_self - x_other)
+            if constexpr ((FL & F_ENERGY) == 0)
+              bond_term<R>(term_vec<MIXED, R>(P, cur, o, role == 0 ? t.z : t.y, box, rs), cf, (R)1, fb);
+            if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
+              if (role == 0) {  // energy terms owned by the first bead
+                const Vec3<double> d = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
+                if constexpr ((FL & F_ENERGY) != 0) e_bond += bond_pot(d, cd);
+                if constexpr ((FL & F_DU) != 0) {
+                  const Vec3<double> sd{d.x * rs.scale[0], d.y * rs.scale[1], d.z * rs.scale[2]};
+                  dU_bond += bond_pot(d, cd) - bond_pot(sd, cd);
+                }
+              }
+            }
+          } else {  // bend (first, second, third): da = x1 - x2, db = x2 - x3
+            if constexpr ((FL & F_ENERGY) == 0)
+              bend_term<R>(term_vec<MIXED, R>(P, cur, t.y, t.z, box, rs), term_vec<MIXED, R>(P, cur, t.z, t.w, box, rs),
+                           cf, role, fb);
+            if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
+              if (role == 0) {
+                const Vec3<double> da = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
+                const Vec3<double> db = term_vec<MIXED, double>(P, cur, t.z, t.w, box, rs);
+                if constexpr ((FL & F_ENERGY) != 0) e_bond += bend_pot(da, db, cd);
+                if constexpr ((FL & F_DU) != 0) {
+                  const Vec3<double> sa{da.x * rs.scale[0], da.y * rs.scale[1], da.z * rs.scale[2]};
+                  const Vec3<double> sb{db.x * rs.scale[0], db.y * rs.scale[1], db.z * rs.scale[2]};
+                  dU_bond += bend_pot(da, db, cd) - bend_pot(sa, sb, cd);
+                }
+              }
+            }
+          }
+        }
+      }
+    }
     if constexpr ((FL & F_ENERGY) != 0) {
       const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
       e_kin = (vx * vx + vy * vy + vz * vz) / 2.0;
@@ -1184,15 +1390,31 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
         }
       } else if (!sphere) {
         const int o = P.orig[i];
-        double noise[3];  // sigma * psi
-        if constexpr ((FL & F_EXTNOISE) != 0) {
-          for (int d = 0; d < 3; ++d) noise[d] = rp.sigma * P.ext_noise[3 * o + d];
-        } else {
-          langevin_noise(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
-        }
         double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
         double a[3];
-        for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
+        if constexpr (MIXED && (FL & F_EXTNOISE) == 0) {
+          // CHAIN force and noise summed in FP32 (both force terms of the
+          // mixed form), the pair force exact from its fixed-point sum:
+          // a = -gamma v + (q 2^-k + (f_chain + sigma psi))
+          float nf[3];
+          langevin_noise_f(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31f, nf);
+          double e[3] = {(double)(fb.x + nf[0]), (double)(fb.y + nf[1]), (double)(fb.z + nf[2])};
+          if (P.n_sph > 0) {
+            e[0] += fs.x;
+            e[1] += fs.y;
+            e[2] += fs.z;
+          }
+          for (int d = 0; d < 3; ++d)
+            a[d] = fma(-rp.gamma, v[d], fma((double)P.fq[i + d * P.n], T.inv_fscale, e[d]));
+        } else {
+          double noise[3];  // sigma * psi
+          if constexpr ((FL & F_EXTNOISE) != 0) {
+            for (int d = 0; d < 3; ++d) noise[d] = rp.sigma * P.ext_noise[3 * o + d];
+          } else {
+            langevin_noise(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
+          }
+          for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
+        }
         if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
           P.ax[i] = a[0];
           P.ay[i] = a[1];

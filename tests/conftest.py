@@ -48,4 +48,8 @@ def mpd_from_golden(g):
                    seed=int(g["seed"]), tension=float(g["tension"]), delta_lxy=float(g["delta_lxy"]),
                    initial_time=0.0, final_time=1.0,
                    sphere_index=g["sphere_index"].astype(np.int32) if len(g.get("sphere_index", [])) else None,
-                   sphere_consts=g["sphere_consts"] if len(g.get("sphere_index", [])) else None)
+                   sphere_consts=g["sphere_consts"] if len(g.get("sphere_index", [])) else None,
+                   bonds=g["bonds"].astype(np.int32) if len(g.get("bonds", [])) else None,
+                   bond_consts=g["bond_consts"] if len(g.get("bonds", [])) else None,
+                   bends=g["bends"].astype(np.int32) if len(g.get("bends", [])) else None,
+                   bend_consts=g["bend_consts"] if len(g.get("bends", [])) else None)

@@ -4,7 +4,9 @@ Run where the reference sources are present (it needs oracle/_ref, built by
 oracle/build_ref.sh):  python tests/golden/make_golden.py
 
 Fixtures
-  <case>.npz       state of a system relaxed by the reference MD, plus what the
+  <case>.npz       state of a system relaxed by the reference MD (ves300,
+                   bil400, net400 = bil400 plus BOND and BEND residues over the
+                   heads, sphere300 at its start), plus what the
                    reference's CellOpt / Blob code computes on it (ref_dump):
                    cell keys, visited pair list, pair and total forces, pair /
                    bonded / BEAD energies and their size-change differences for
@@ -12,6 +14,9 @@ Fixtures
   traj_bil/        a 48-step reference MD run on a 200-lipid bilayer with the
                    barostat on: input .mpd, sha256 of every file the run writes
                    (digests.json) and the small ones verbatim (out/).
+  net200/          a 200-lipid bilayer with BOND and BEND residues (input of
+                   the network trajectory and MD tests) and the sha256 of
+                   every file a 48-step reference MD run of it writes.
   generators.json  sha256 of the reference generators' .mpd for a few seeds.
 Inputs are seeded synthetic membranes built in the reference generators' terms
 (softmold_gb300 synth_*, byte-identical to generate/liposome and bilayer).
@@ -48,6 +53,52 @@ def set_run(path, final, store, measure):
     open(path, "w").write(t)
 
 
+def add_network(path, seed):
+    """Adds BOND and BEND residues over the head beads of a bilayer .mpd: two
+    BOND residues (nearest-neighbour heads, l0 0.8 k 50; next-nearest, l0 1.1
+    k 20) and one BEND residue (collinear head triplets, a 1 k 10), as the
+    molecule blocks `6 nBond / l0 k / i j ...` and `7 nBond / a k / i j l ...`."""
+    m = smd.read_mpd(path)
+    rng = np.random.default_rng(seed)
+    heads = np.flatnonzero(m.type == 2)
+    P = m.pos[heads]
+    d = P[:, None, :] - P[None, :, :]
+    d -= m.box * np.round(d / m.box)
+    r = np.sqrt((d ** 2).sum(-1))
+    near, nnear = [], []
+    for a in range(len(heads)):
+        for b in range(a + 1, len(heads)):
+            if abs(d[a, b, 2]) > 1.0:  # other leaflet
+                continue
+            if r[a, b] < 0.9:
+                near.append((heads[a], heads[b]))
+            elif r[a, b] < 1.2:
+                nnear.append((heads[a], heads[b]))
+    near = [near[k] for k in rng.permutation(len(near))[:max(1, len(near) // 3)]]
+    nnear = [nnear[k] for k in rng.permutation(len(nnear))[:max(1, len(nnear) // 4)]]
+    trip = []
+    for a in range(len(heads)):
+        for b in range(len(heads)):
+            if b == a or not (0.5 < r[a, b] < 0.9) or abs(d[a, b, 2]) > 1.0:
+                continue
+            for c in range(len(heads)):
+                if c in (a, b) or not (0.5 < r[b, c] < 0.9):
+                    continue
+                if np.dot(d[a, b], d[b, c]) / (r[a, b] * r[b, c]) > 0.95 and a < c:
+                    trip.append((heads[a], heads[b], heads[c]))
+    trip = [trip[k] for k in rng.permutation(len(trip))[:max(1, len(trip) // 6)]]
+    blocks = ["6\t%d\n0.8 50\n" % len(near) + "".join(f"{a} {b}\n" for a, b in near),
+              "6\t%d\n1.1 20\n" % len(nnear) + "".join(f"{a} {b}\n" for a, b in nnear),
+              "7\t%d\n1 10\n" % len(trip) + "".join(f"{a} {b} {c}\n" for a, b, c in trip)]
+    lines = open(path).read().split("\n")
+    k = next(i for i, ln in enumerate(lines) if ln.strip() == "molecule")
+    lines = lines[:k + 4] + "".join(blocks).rstrip("\n").split("\n") + lines[k + 4:]
+    text = "\n".join(lines)
+    text = re.sub(r"nMolecules (\d+)", lambda mm: f"nMolecules {int(mm.group(1)) + 3}", text)
+    open(path, "w").write(text)
+    return len(near), len(nnear), len(trip)
+
+
 def run_ref_md(workdir, name):
     env = dict(os.environ, OMP_NUM_THREADS="1")
     subprocess.run([os.path.join(REF, "MD"), name], cwd=workdir, env=env, check=True,
@@ -71,6 +122,10 @@ def dump_case(workdir, name, out_name):
         delta_lxy=m.delta_lxy,
         sphere_index=m.sphere_index if m.sphere_index is not None else np.zeros(0, np.int32),
         sphere_consts=m.sphere_consts if m.sphere_consts is not None else np.zeros(0),
+        bonds=m.bonds if m.bonds is not None else np.zeros((0, 2), np.int32),
+        bond_consts=m.bond_consts if m.bond_consts is not None else np.zeros((0, 2)),
+        bends=m.bends if m.bends is not None else np.zeros((0, 3), np.int32),
+        bend_consts=m.bend_consts if m.bend_consts is not None else np.zeros((0, 2)),
         keys=rd("keys.i32", np.int32), pairs=rd("pairs.i32", np.int32).reshape(-1, 2),
         pair_force=rd("pair_force.f64", np.float64).reshape(n, 3),
         force=rd("force.f64", np.float64).reshape(n, 3),
@@ -93,6 +148,25 @@ def main():
         set_run(os.path.join(tmp, "bil.mpd"), 4, 4, 4)
         run_ref_md(tmp, "bil")
         dump_case(tmp, "bil", "bil400")
+        # relaxed bilayer with a head network: BOND and BEND residues beside CHAIN
+        smd.synth_bilayer(os.path.join(tmp, "net.mpd"), 91, 400, 3.45, 20.0, 0.01, 0.0)
+        add_network(os.path.join(tmp, "net.mpd"), 91)
+        set_run(os.path.join(tmp, "net.mpd"), 4, 4, 4)
+        run_ref_md(tmp, "net")
+        dump_case(tmp, "net", "net400")
+        # unrelaxed 200-lipid network system: input of trajectory and MD tests
+        ndir = os.path.join(HERE, "net200")
+        os.makedirs(ndir, exist_ok=True)
+        smd.synth_bilayer(os.path.join(ndir, "net.mpd"), 5, 200, 3.45, 16.0, 0.01, 0.0)
+        add_network(os.path.join(ndir, "net.mpd"), 5)
+        set_run(os.path.join(ndir, "net.mpd"), 0.96, 0.48, 0.16)
+        run_dir = os.path.join(tmp, "netrun")
+        os.makedirs(run_dir)
+        shutil.copy(os.path.join(ndir, "net.mpd"), run_dir)
+        run_ref_md(run_dir, "net")
+        json.dump({os.path.basename(f): hashlib.sha256(open(f, "rb").read()).hexdigest()
+                   for f in sorted(glob.glob(os.path.join(run_dir, "*")))},
+                  open(os.path.join(ndir, "digests.json"), "w"), indent=1)
         # vesicle with a continuum sphere (BEAD residue, radius 5) whose surface
         # is 0.8 sigma outside the outer heads, inside its attractive well; the
         # reference's Umax=10 core is not repulsive enough for a stable run, so

@@ -46,6 +46,14 @@ class Oracle:
         L.orc_bead_potential.restype = C.c_double
         L.orc_bead_dpotential.argtypes = [C.c_int, D, I, D, C.c_int, C.c_int, I, D, D]
         L.orc_bead_dpotential.restype = C.c_double
+        for f in ("orc_bond_force", "orc_bend_force"):
+            getattr(L, f).argtypes = [D, D, C.c_int, I, D, D]
+        for f in ("orc_bond_potential", "orc_bend_potential"):
+            getattr(L, f).argtypes = [D, D, C.c_int, I, D]
+            getattr(L, f).restype = C.c_double
+        for f in ("orc_bond_dpotential", "orc_bend_dpotential"):
+            getattr(L, f).argtypes = [D, D, C.c_int, I, D, D]
+            getattr(L, f).restype = C.c_double
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_threads(1)
         L.orc_md_run.argtypes = [C.c_char_p, C.c_int]
@@ -85,11 +93,30 @@ class Oracle:
         for b, c in zip(g["chain_blocks"], g["chain_consts"]):
             self.L.orc_chain_force(pos.ctypes.data_as(D), _d(g["box"]), int(b[0]), int(b[1]), int(b[2]), _d(c),
                                    acc.ctypes.data_as(D))
+        for kind in ("bond", "bend"):
+            for lst, c in self._residues(g, kind):
+                getattr(self.L, f"orc_{kind}_force")(pos.ctypes.data_as(D), _d(g["box"]), len(lst), _i(lst), _d(c),
+                                                    acc.ctypes.data_as(D))
         si = g.get("sphere_index")
         if si is not None and len(si):
             self.L.orc_bead_force(len(pos), pos.ctypes.data_as(D), typ.ctypes.data_as(I), _d(g["box"]), nT,
                                   len(si), _i(si), _d(g["sphere_consts"]), acc.ctypes.data_as(D))
         return acc
+
+    @staticmethod
+    def _residues(g, kind):
+        """BOND / BEND terms grouped into residues (runs of equal constants),
+        in the order the .mpd lists them, as Blob::do*Force visits them."""
+        lst = g.get(kind + "s")
+        if lst is None or len(lst) == 0:
+            return []
+        cs = np.asarray(g[kind + "_consts"])
+        out, k0 = [], 0
+        for k in range(1, len(lst) + 1):
+            if k == len(lst) or not np.array_equal(cs[k], cs[k0]):
+                out.append((np.ascontiguousarray(lst[k0:k], np.int32), np.ascontiguousarray(cs[k0])))
+                k0 = k
+        return out
 
     def energies(self, g, scale=None):
         pos = np.ascontiguousarray(g["pos"], np.float64)
@@ -106,6 +133,11 @@ class Oracle:
             a = (pos.ctypes.data_as(D), _d(g["box"]), int(b[0]), int(b[1]), int(b[2]), _d(c))
             bonded += self.L.orc_chain_potential(*a) if scale is None else self.L.orc_chain_dpotential(*a,
                                                                                                      _d(scale))
+        for kind in ("bond", "bend"):
+            for lst, c in self._residues(g, kind):
+                a = (pos.ctypes.data_as(D), _d(g["box"]), len(lst), _i(lst), _d(c))
+                bonded += (getattr(self.L, f"orc_{kind}_potential")(*a) if scale is None else
+                           getattr(self.L, f"orc_{kind}_dpotential")(*a, _d(scale)))
         bead = 0.0
         si = g.get("sphere_index")
         if si is not None and len(si):

@@ -16,16 +16,20 @@ import pytest
 from conftest import GOLDEN
 
 TRAJ = os.path.join(GOLDEN, "traj_bil")
+NET = os.path.join(GOLDEN, "net200")
 
 
 @pytest.mark.skipif(platform.machine() != "x86_64", reason="digests are of x86-64 glibc number formatting")
-def test_md_oracle_matches_reference_outputs(oracle, tmp_path):
+@pytest.mark.parametrize("where,name", [(TRAJ, "bil"), (NET, "net")])
+def test_md_oracle_matches_reference_outputs(oracle, tmp_path, where, name):
+    """traj_bil: CHAIN lipids, barostat on; net200: the same with BOND and
+    BEND residues over the heads (tests/golden/net200)."""
     from oracle_binding import MD
-    shutil.copy(os.path.join(TRAJ, "bil.mpd"), tmp_path)
+    shutil.copy(os.path.join(where, name + ".mpd"), tmp_path)
     env = dict(os.environ, OMP_NUM_THREADS="1")
-    r = subprocess.run([MD, "bil", "1"], cwd=tmp_path, env=env, capture_output=True, text=True)
+    r = subprocess.run([MD, name, "1"], cwd=tmp_path, env=env, capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    want = json.load(open(os.path.join(TRAJ, "digests.json")))
+    want = json.load(open(os.path.join(where, "digests.json")))
     got = {f: hashlib.sha256(open(os.path.join(tmp_path, f), "rb").read()).hexdigest()
            for f in os.listdir(tmp_path)}
     assert sorted(got) == sorted(want)
