@@ -72,12 +72,13 @@ def workload(args, rank, tmpdir):
         paths = [path]
     elif args.workload == "sphere80k":
         path = os.path.join(tmpdir, f"bench{rank}.mpd")
-        # sphere radius 5, surface 2 sigma outside the outer heads; head well depth 10 with a
-        # repulsive core (Umax 100: the generator default of 10 lets heads collapse into the core)
-        smd.synth_vesicle_sphere(path, 1000 + rank, 80000, 3.45, 190.0, 5.0, -10.0, 100.0, 2.0)
+        # sphere radius 5, surface 2 sigma outside the outer heads; head well Umin -10.  The table's
+        # inner polynomial keeps beads out only while (Umax - Umin)/6 > ~2.3 |Umin|: heads Umax 300
+        # (barrier ~+530 at 1 sigma inside the surface), tails Umax 100 (soft repulsion, no well)
+        smd.synth_vesicle_sphere(path, 1000 + rank, 80000, 3.45, 190.0, 5.0, -10.0, 300.0, 2.0, 100.0)
         cfg = {"workload": "vesicle of 80,000 3-bead lipids (240,001 beads with the sphere), 190^3 box, one "
-                           "continuum sphere R 5 sigma 2 sigma outside the outer heads (head well depth 10, "
-                           "range 2), kT 3, gamma 1, dt 0.02"}
+                           "continuum sphere R 5 sigma 2 sigma outside the outer heads (head Umin -10 Umax 300, "
+                           "tail Umax 100, range 2), kT 3, gamma 1, dt 0.02"}
         paths = [path]
     elif args.workload == "adjoint10k":
         path = os.path.join(tmpdir, f"bench{rank}.mpd")
@@ -389,6 +390,11 @@ def main():
     # FP64 plain form on the same state, and the mixed form's force error
     pos, vel = s.state()
     boxes = [s.box(r) for r in range(len(ms))]  # the boxes of this state (the e2e run below moves them on)
+    offs = np.cumsum([0] + [len(x.type) for x in ms])
+    for r in range(len(ms)):
+        q = pos[offs[r]:offs[r + 1]]
+        if not (np.isfinite(q).all() and (q >= 0).all() and (q <= boxes[r]).all()):
+            raise RuntimeError(f"replica {r} left its box: the run blew up (bead-steps/s not reported)")
     p = smd.System(m, precision=smd.PLAIN_FP64, skin=args.skin)
     p.set_stream(stream.cuda_stream)
     for r in range(len(ms)):
@@ -453,7 +459,6 @@ def main():
         # equilibrated state of (a sample of) the replicas, timed one after another
         sample = range(len(ms)) if len(ms) == 1 else range(0, len(ms), 16)
         units, secs = 0, 0.0
-        offs = np.cumsum([0] + [len(x.type) for x in ms])
         for r in sample:
             ck = os.path.join(tmp, f"cpu{r}.mpd")
             a, b = offs[r], offs[r + 1]

@@ -159,8 +159,9 @@ int smd_advance(smd_system* h, int steps, int flags);
  * 256 threads per cell, octant-filtered) and the pair pass at 4, 8 and 16
  * lanes per bead on the handle's state, and keeps the fastest of each; every
  * choice gives bitwise the same trajectory.  smd_advance runs it once per
- * system shape before its first call of 64 steps or more (environment
- * SMD_AUTOTUNE=0 turns that off); force = 1 re-times.  Reports the choice
+ * system shape, at its first call after the handle has run 256 steps (the
+ * running membrane, not its start configuration; environment SMD_AUTOTUNE=0
+ * turns that off); force = 1 re-times.  Reports the choice
  * (lanes: 4/8/16; list_kernel: 0 flat-128, 1 flat-256, 2 octant) and, in
  * ms[6] if not NULL, the best times of the three list variants and of the
  * three lane counts.  The plain form keeps its fixed configuration. */
@@ -223,7 +224,7 @@ int smd_synth_bilayer(const char* path, int seed, int n_lipids, double areal_den
                       double delta_lxy, double tension);
 int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double areal_density,
                              double box, double sphere_radius, double head_umin, double head_umax,
-                             double gap);
+                             double gap, double other_umax);
 
 /* Non-bonded forces for callers that cannot allocate device memory (for
  * example code running while another framework owns the device memory

@@ -103,7 +103,7 @@ _SIGS = {
     "smd_synth_vesicle": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double]),
     "smd_synth_bilayer": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                     C.c_double]),
-    "smd_synth_vesicle_sphere": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+    "smd_synth_vesicle_sphere": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                            C.c_double, C.c_double, C.c_double]),
     "smd_md_main": (C.c_int, [C.c_char_p, C.c_int]),
     "smd_pair_forces_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_int,
@@ -488,6 +488,6 @@ def synth_bilayer(path, seed, n_lipids, density=3.45, zsize=40.0, delta_lxy=0.01
 
 
 def synth_vesicle_sphere(path, seed, n_lipids, density, box, radius=5.0, head_umin=-10.0, head_umax=10.0,
-                         gap=2.0):
+                         gap=2.0, other_umax=10.0):
     _check(lib().smd_synth_vesicle_sphere(path.encode(), seed, n_lipids, density, box, radius, head_umin,
-                                          head_umax, gap), "smd_synth_vesicle_sphere")
+                                          head_umax, gap, other_umax), "smd_synth_vesicle_sphere")

@@ -22,14 +22,15 @@ int smd_synth_bilayer(const char* path, int seed, int n_lipids, double density, 
 }
 
 int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double density, double box,
-                             double sphere_radius, double head_umin, double head_umax, double gap) {
+                             double sphere_radius, double head_umin, double head_umax, double gap,
+                             double other_umax) {
   if (!path || n_lipids <= 0 || !(density > 0) || !(box > 0) || !(sphere_radius > 1)) return 1;
   smd::MpdSystem s = smd::synth_vesicle(seed, n_lipids, density, box);
   // sphere centred on the +z axis, its surface `gap` outside the outer heads
   // (outer head shell: radius + 5 bond lengths, models/lipidModels.h:1428-1431)
   const double R = std::sqrt(((double)n_lipids / density) / (4.0 * M_PI));
   const double c[3] = {box / 2.0, box / 2.0, box / 2.0 + R + 0.7 * 5 + gap + sphere_radius};
-  smd::add_continuum_sphere(s, c, sphere_radius, head_umin, head_umax, 4);
+  smd::add_continuum_sphere(s, c, sphere_radius, head_umin, head_umax, other_umax, 4);
   std::string err;
   return smd::mpd_write_file(path, s, err);
 }

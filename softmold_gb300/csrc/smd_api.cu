@@ -173,9 +173,13 @@ int launch_rebuild(smd_system* h, cudaStream_t st, int cur, int in_graph) {
   auto& P = h->P;
   const int g = h->grid();
   SMD_LAUNCH(h, k_bin<<<g, kBlock, 0, st>>>(P, cur, h->mixed ? 1 : 0, in_graph));
-  SMD_LAUNCH(h, k_scan_tiles<<<h->n_tiles, kBlock, 0, st>>>(P));
-  SMD_LAUNCH(h, k_scan_sums<<<1, kBlock, 0, st>>>(P, h->n_tiles));
-  SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, st>>>(P));
+  if (h->n_cells <= kScanOneMax) {
+    SMD_LAUNCH(h, k_scan_one<<<1, kScanOneThreads, 0, st>>>(P));
+  } else {
+    SMD_LAUNCH(h, k_scan_tiles<<<h->n_tiles, kBlock, 0, st>>>(P));
+    SMD_LAUNCH(h, k_scan_sums<<<1, kBlock, 0, st>>>(P, h->n_tiles));
+    SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, st>>>(P));
+  }
   if (h->mixed) {
     SMD_LAUNCH(h, k_reorder<true><<<g, kBlock, 0, st>>>(P, cur));
     switch (h->tune.list) {
@@ -189,7 +193,8 @@ int launch_rebuild(smd_system* h, cudaStream_t st, int cur, int in_graph) {
   }
   return 0;
 }
-constexpr int kRebuildKernels = 6;
+// kernels of one list build
+int rebuild_kernels(const smd_system* h) { return h->n_cells <= kScanOneMax ? 4 : 6; }
 
 int rebuild_if_needed(smd_system* h, bool clear_after = false) {
   if (int rc = launch_rebuild(h, h->stream, h->cur, 0)) return rc;
@@ -527,8 +532,9 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
       maxF = std::max(maxF, std::fabs((c[4] - c[5] * m) * m) * 1.05);
     }
   }
-  // one pair force must fit in int32 after scaling
-  T.fscale = (float)std::ldexp(1.0, (int)std::floor(std::log2(1073741824.0 / maxF)));
+  // one pair force must stay below 2^26 after scaling, so that the pair pass
+  // can sum 32 of them per lane in int32 before widening to int64
+  T.fscale = (float)std::ldexp(1.0, (int)std::floor(std::log2(67108864.0 / maxF)));
   T.inv_fscale = 1.0 / (double)T.fscale;
   // chain constant sets
   std::vector<std::array<double, 4>> sets;
@@ -1101,7 +1107,7 @@ int capture_period(smd_system* h, int cur0) {
   cudaGraph_t done = nullptr;
   const cudaError_t e = cudaStreamEndCapture(st, &done);
   h->cur = saved_cur;
-  const long kernels = h->launches - saved_launches - (long)G * kRebuildKernels;
+  const long kernels = h->launches - saved_launches - (long)G * rebuild_kernels(h);
   h->launches = saved_launches;
   if (rc) {
     if (done) cudaGraphDestroy(done);
@@ -1239,7 +1245,10 @@ int smd_advance(smd_system* h, int steps, int flags) {
   const bool async = (flags & SMD_ASYNC) != 0;
   int rc = complete_pending(h);
   if (rc) return rc;
-  if (!h->tune.done && steps >= 64 && autotune_enabled() && (rc = autotune(h, false))) return rc;
+  // tune once the system has relaxed from its start (a lattice start is far
+  // sparser than the running membrane and favours other kernels)
+  if (!h->tune.done && h->it - h->first_step[0] >= 256 && autotune_enabled() && (rc = autotune(h, false)))
+    return rc;
   int done = 0;
   while (done < steps) {
     const int chunk = std::min(steps - done, kTrialChunk * std::max(1, h->resize_rate) / 2);
@@ -1387,7 +1396,7 @@ int smd_last_timing(smd_system* h, double* ms, long* step_launches, long* launch
   if (ms) *ms = h->step_ms;
   if (step_launches) *step_launches = h->step_launches;
   // list-build kernels that ran inside graph conditional bodies count too
-  if (launches) *launches = h->launches + (long)(h->graph_builds * kRebuildKernels);
+  if (launches) *launches = h->launches + (long)(h->graph_builds * rebuild_kernels(h));
   return 0;
 }
 

@@ -168,6 +168,56 @@ __global__ void __launch_bounds__(kBlock) k_scan_apply(DevPtrs P) {
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) P.cell_start[P.n_cells_total] = P.n;
 }
 
+// The same exclusive scan in one CTA for up to kScanOneMax cells (a single
+// system's grid): each of 1024 threads sums 8 consecutive counts, the block
+// scans the thread sums, and each thread writes its 8 starts.
+constexpr int kScanOneThreads = 1024;
+constexpr int kScanOneMax = 32768;
+__global__ void __launch_bounds__(kScanOneThreads) k_scan_one(DevPtrs P) {
+  if (!P.g->rebuild) return;
+  __shared__ int wsum[kScanOneThreads / 32];
+  const int n = P.n_cells_total;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int carry = 0;
+  for (int base = 0; base < n; base += kScanOneThreads * 8) {
+    const int c0 = base + threadIdx.x * 8;
+    int v[8];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      v[k] = (c0 + k < n) ? P.cell_count[c0 + k] : 0;
+      s += v[k];
+    }
+    int x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int t = wsum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      wsum[lane] = t;
+    }
+    __syncthreads();
+    int ex = carry + (w > 0 ? wsum[w - 1] : 0) + x - s;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (c0 + k < n) P.cell_start[c0 + k] = ex;
+      ex += v[k];
+    }
+    carry += wsum[kScanOneThreads / 32 - 1];
+    __syncthreads();  // wsum is rewritten by the next chunk
+  }
+  if (threadIdx.x == 0) P.cell_start[n] = P.n;
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_reorder(DevPtrs P, int cur) {
   if (!P.g->rebuild) return;
@@ -415,14 +465,13 @@ __global__ void __launch_bounds__(kNbrThreads) k_nbr_cells_plain(DevPtrs P, int 
 }
 
 // ---- Mixed form, octant-filtered.  Candidates are staged as FP32 offsets
-// from the cell centre (exact 32-bit fractional differences, scaled once).
-// While staging, each thread also tests its candidate against the boxes of
-// the eight octants of the cell and appends it to the list of every octant
-// it lies within list_cut of (about 45 % of the stencil per octant).  Each
-// bead of the cell then tests only its octant's list, 32 candidates per
-// round; beads go to warps round-robin, whatever their octant.  The list cut
-// carries a 1e-4 sigma margin over the FP32 rounding of the offsets, so the
-// list is a superset of the exact one.
+// from the cell centre (exact 32-bit fractional differences, scaled once),
+// segment by segment; while staging, each warp appends its 32 candidates to
+// the list of every octant of the cell whose box they lie within list_cut of
+// (about 45 % of the stencil per octant), with one ballot per octant.  Each
+// bead then scans only its octant's list, padded to rounds of 32 with a far
+// sentinel.  The list cut carries a 1e-4 sigma margin over the FP32
+// rounding of the offsets, so the list is a superset of the exact one.
 constexpr int kOctThreads = 256;
 constexpr int kOctChunk = 1024;  // staged candidates per pass (16 KB)
 
@@ -479,18 +528,14 @@ __device__ __forceinline__ void stencil_rows(const DevPtrs& P, const CellCtx& q,
 __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
   const int s0 = P.cell_start[c], e0 = P.cell_start[c + 1];
   if (s0 >= e0) return;
-  // per-cell constants, computed once and shared (the divisions are costly
-  // on every thread: FP64 runs at a small fraction of the FP32 rate here)
   __shared__ CellCtx qs;
   __shared__ unsigned int cr_s[3];
   __shared__ float h_s[3];
   __shared__ int seg_s[18], seg_len[18], seg_p[19];
-  __shared__ int oct_n[8], oct_s[9], oct_c[8];
-  __shared__ unsigned short ord[kNbrMaxCell];
-  __shared__ unsigned char octof[kNbrMaxCell];
+  __shared__ int oct_c[8];
   __shared__ int cnt[kNbrMaxCell];
-  __shared__ float4 stage[kOctChunk];
-  __shared__ unsigned short clist[8][kOctChunk];
+  __shared__ float4 stage[kOctChunk + 1];  // + one far sentinel
+  __shared__ unsigned short clist[8][kOctChunk + 32];
   __syncthreads();  // the previous cell of this CTA is done with the shared arrays
   if (threadIdx.x == 0) {
     const CellCtx q0 = cell_ctx(P, c, s0, e0);
@@ -504,7 +549,6 @@ __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
     h_s[1] = (float)(0.25 * r0.box[1] / q0.n1) + 1e-4f;
     h_s[2] = (float)(0.25 * r0.box[2] / q0.n2) + 1e-4f;
   }
-  if (threadIdx.x < 8) oct_n[threadIdx.x] = 0;
   __syncthreads();
   const CellCtx q = qs;
   const RepState& rs = P.rs[q.r];
@@ -515,9 +559,8 @@ __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
   }
   copy_back<true, kOctThreads>(P, cur, q, rs);
   stencil_rows(P, q, seg_s, seg_len);
-  const unsigned int crx = cr_s[0], cry = cr_s[1], crz = cr_s[2];
-  const float hx = h_s[0], hy = h_s[1], hz = h_s[2];
-  const float sx = rs.len_per_frac[0], sy = rs.len_per_frac[1], sz = rs.len_per_frac[2];
+  for (int b = threadIdx.x; b < nb; b += kOctThreads) cnt[b] = 0;
+  if (threadIdx.x == 0) stage[kOctChunk] = make_float4(1e30f, 1e30f, 1e30f, __int_as_float(-1));
   __syncthreads();
   if (threadIdx.x == 0) {  // prefix sums over the 18 slots, empty ones dropped
     int k = 0, acc = 0;
@@ -529,64 +572,51 @@ __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
       ++k;
     }
     seg_p[k] = acc;
-    seg_len[0] = k;  // number of segments
-  }
-  // bucket the cell's beads by octant
-  for (int b = threadIdx.x; b < nb; b += kOctThreads) {
-    const uint4 m = P.mt[q.s + b];
-    const int o = ((int)(m.x - crx) >= 0 ? 1 : 0) | ((int)(m.y - cry) >= 0 ? 2 : 0) | ((int)(m.z - crz) >= 0 ? 4 : 0);
-    octof[b] = (unsigned char)o;
-    cnt[b] = 0;
-    atomicAdd(&oct_n[o], 1);
+    seg_len[0] = k;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int a = 0;
-    for (int o = 0; o < 8; ++o) {
-      oct_s[o] = a;
-      a += oct_n[o];
-      oct_n[o] = 0;
-    }
-    oct_s[8] = a;
-  }
-  __syncthreads();
-  unsigned int busy = 0;  // octants holding beads
-  for (int o = 0; o < 8; ++o)
-    if (oct_s[o + 1] > oct_s[o]) busy |= 1u << o;
-  for (int b = threadIdx.x; b < nb; b += kOctThreads) {
-    const int o = octof[b];
-    ord[oct_s[o] + atomicAdd(&oct_n[o], 1)] = (unsigned short)b;
-  }
   const int nseg = seg_len[0];
   const int M = seg_p[nseg];
+  const unsigned int crx = cr_s[0], cry = cr_s[1], crz = cr_s[2];
+  const float hx = h_s[0], hy = h_s[1], hz = h_s[2];
+  const float sx = rs.len_per_frac[0], sy = rs.len_per_frac[1], sz = rs.len_per_frac[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned int below = (1u << lane) - 1u;
   const int kmax = P.kmax;
   const float lcut = P.tab->list_cut_f + 1e-4f;
   const float lc2 = lcut * lcut;
-  // thin boxes (fewer than 3 cells on an axis) keep every candidate and take
-  // the minimum image per pair
+  // thin boxes (fewer than 3 cells on an axis) take the flat scan with the
+  // minimum image per pair; the octant filter assumes a full stencil
   const bool thin = q.n0 < 3 || q.n1 < 3 || q.n2 < 3;
-  const float bx = rs.len_per_frac[0] * 4294967296.0f, by = rs.len_per_frac[1] * 4294967296.0f,
-              bz = rs.len_per_frac[2] * 4294967296.0f;
+  const float bx = sx * 4294967296.0f, by = sy * 4294967296.0f, bz = sz * 4294967296.0f;
   for (int base = 0; base < M; base += kOctChunk) {
     const int m = min(kOctChunk, M - base);
-    __syncthreads();
+    if (base > 0) __syncthreads();  // every warp is done with the previous chunk
     if (threadIdx.x < 8) oct_c[threadIdx.x] = 0;
+    __syncthreads();
+    // stage every segment with all threads, then let each warp append its
+    // 32 staged candidates to the list of every octant box they lie within
+    // list_cut of
+    for (int t = 0; t < nseg; ++t) {
+      const int ps = seg_p[t];
+      const int lo = max(ps, base), hi = min(seg_p[t + 1], base + m);
+      for (int g = lo + threadIdx.x; g < hi; g += kOctThreads) {
+        const int j = seg_s[t] + (g - ps);
+        const uint4 mj = P.mt[j];
+        stage[g - base] = make_float4((float)(int)(mj.x - crx) * sx, (float)(int)(mj.y - cry) * sy,
+                                      (float)(int)(mj.z - crz) * sz, __int_as_float(j));
+      }
+    }
     __syncthreads();
     for (int k0 = warp * 32; k0 < m; k0 += kOctThreads) {
       const int k = k0 + lane;
       unsigned int pass = 0;
       if (k < m) {
-        const int j = seg_bead(seg_s, seg_p, nseg, base + k);
-        const uint4 mj = P.mt[j];
-        const float x = (float)(int)(mj.x - crx) * sx, y = (float)(int)(mj.y - cry) * sy,
-                    z = (float)(int)(mj.z - crz) * sz;
-        stage[k] = make_float4(x, y, z, __int_as_float(j));
         if (thin) {
-          pass = busy;
+          pass = 0xffu;
         } else {
-          // squared distance to the lower / upper half of the cell per axis
+          const float4 cj = stage[k];
+          const float x = cj.x, y = cj.y, z = cj.z;
           const float xl = fmaxf(fabsf(x + hx) - hx, 0.f), xu = fmaxf(fabsf(x - hx) - hx, 0.f);
           const float yl = fmaxf(fabsf(y + hy) - hy, 0.f), yu = fmaxf(fabsf(y - hy) - hy, 0.f);
           const float zl = fmaxf(fabsf(z + hz) - hz, 0.f), zu = fmaxf(fabsf(z - hz) - hz, 0.f);
@@ -596,12 +626,10 @@ __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
           pass = (x0 + yz0 < lc2 ? 1u : 0u) | (x1 + yz0 < lc2 ? 2u : 0u) | (x0 + yz1 < lc2 ? 4u : 0u) |
                  (x1 + yz1 < lc2 ? 8u : 0u) | (x0 + yz2 < lc2 ? 16u : 0u) | (x1 + yz2 < lc2 ? 32u : 0u) |
                  (x0 + yz3 < lc2 ? 64u : 0u) | (x1 + yz3 < lc2 ? 128u : 0u);
-          pass &= busy;
         }
       }
 #pragma unroll
       for (int o = 0; o < 8; ++o) {
-        if (!(busy & (1u << o))) continue;
         const unsigned int bal = __ballot_sync(0xffffffffu, (pass >> o) & 1u);
         if (bal == 0) continue;
         int at = 0;
@@ -611,38 +639,40 @@ __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
       }
     }
     __syncthreads();
-    for (int t = warp; t < nb; t += kOctThreads / 32) {
-      const int b = ord[t];
-      const int o = octof[b];
-      const int nc = oct_c[o];
-      const unsigned short* cl = clist[o];
+    // pad every octant list to a multiple of 32 with the sentinel slot
+    for (int o = warp; o < 8; o += kOctThreads / 32) {
+      const int nc = oct_c[o], ncp = (nc + 31) & ~31;
+      if (nc + lane < ncp) clist[o][nc + lane] = (unsigned short)kOctChunk;
+    }
+    __syncthreads();
+    for (int b = warp; b < nb; b += kOctThreads / 32) {
       const int i = q.s + b;
       const uint4 mi = P.mt[i];
+      const int o = ((int)(mi.x - crx) >= 0 ? 1 : 0) | ((int)(mi.y - cry) >= 0 ? 2 : 0) |
+                    ((int)(mi.z - crz) >= 0 ? 4 : 0);
       const float xi = (float)(int)(mi.x - crx) * sx, yi = (float)(int)(mi.y - cry) * sy,
                   zi = (float)(int)(mi.z - crz) * sz;
+      const int ncp = (oct_c[o] + 31) & ~31;
+      const unsigned short* cl = clist[o];
       int count = cnt[b];
       int* out = P.nbr + (size_t)i * kmax;
-      for (int k0 = 0; k0 < nc; k0 += 32) {
-        const int k = k0 + lane;
-        bool hit = false;
-        int j = 0;
-        if (k < nc) {
-          const float4 cj = stage[cl[k]];
-          float dx = xi - cj.x, dy = yi - cj.y, dz = zi - cj.z;
-          if (thin) {
-            dx -= bx * rintf(dx / bx);
-            dy -= by * rintf(dy / by);
-            dz -= bz * rintf(dz / bz);
-          }
-          j = __float_as_int(cj.w);
-          hit = (dx * dx + dy * dy + dz * dz < lc2) && (j != i);
+#pragma unroll 4
+      for (int k0 = 0; k0 < ncp; k0 += 32) {
+        const float4 cj = stage[cl[k0 + lane]];
+        float dx = xi - cj.x, dy = yi - cj.y, dz = zi - cj.z;
+        if (thin) {
+          dx -= bx * rintf(dx / bx);
+          dy -= by * rintf(dy / by);
+          dz -= bz * rintf(dz / bz);
         }
+        const int j = __float_as_int(cj.w);
+        const bool hit = (dx * dx + dy * dy + dz * dz < lc2) & (j != i) & (j >= 0);
         const unsigned int hits = __ballot_sync(0xffffffffu, hit);
-        if (hit) {
+        if (hits) {
           const int slot = count + __popc(hits & below);
-          if (slot < kmax) out[slot] = j;
+          if (hit && slot < kmax) out[slot] = j;
+          count += __popc(hits);
         }
-        count += __popc(hits);
       }
       if (lane == 0) cnt[b] = count;
     }
@@ -1071,7 +1101,7 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
 // minimum image.  Writes the per-bead pair force (fixed point or FP64) and,
 // with F_DU / F_ENERGY, the replica's pair U(x)-U(s x) / pair energy.
 template <bool MIXED, int FL, int G>
-__global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
+__global__ void __launch_bounds__(kBlock, (MIXED && (FL & F_DU) == 0) ? 6 : 1) k_force(DevPtrs P, int cur) {
   using R = typename std::conditional<MIXED, float, double>::type;
   __shared__ R sF[6 * kMaxTypes * kMaxTypes];
   __shared__ R sU[6 * kMaxTypes * kMaxTypes];
@@ -1112,7 +1142,23 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
       const float* rowU = sU + 6 * ti * nT;
       const float rc2 = T.rc2f, fs = T.fscale;
       float eacc = 0.f;
+      // pair forces: branch-free (out-of-range entries add an exact 0), summed
+      // per lane in int32 and flushed to int64 every 32 entries: one pair is
+      // below 2^26 in fixed point, so 32 of them cannot overflow
+      int ax = 0, ay = 0, az = 0;
+      auto pair_force_q = [&](float dx, float dy, float dz, float r2, int tj) {
+        const float* c = rowF + 6 * tj;
+        const float rinv = rsqrtf(r2), r = r2 * rinv;
+        const int ci = (r >= c[0]) ? 3 : 0;
+        const float m = c[ci] - r;
+        float mag = ((c[ci + 1] - c[ci + 2] * m) * m) * rinv * fs;
+        mag = (r2 < rc2) ? mag : 0.f;
+        ax += __float2int_rn(dx * mag);
+        ay += __float2int_rn(dy * mag);
+        az += __float2int_rn(dz * mag);
+      };
       int k = sub;
+      int rounds = 0;
       // two independent gathers in flight per lane
       for (; k + G < nn; k += 2 * G) {
         const int j0 = __ldg(nb + k), j1 = __ldg(nb + k + G);
@@ -1131,17 +1177,18 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
                                   4294967296.0f);
             }
           }
-          if (r2 < rc2) {
-            const int tj = o.w & 0xff;
-            if constexpr ((FL & F_ENERGY) == 0) {
-              const float mag = pair_mag_rsqrt(rowF + 6 * tj, r2) * fs;
-              qx += (long long)__float2int_rn(dx * mag);
-              qy += (long long)__float2int_rn(dy * mag);
-              qz += (long long)__float2int_rn(dz * mag);
-            } else {
-              eacc += pair_pot<float>(rowU + 6 * tj, sqrtf(r2));
-            }
+          if constexpr ((FL & F_ENERGY) == 0) {
+            pair_force_q(dx, dy, dz, r2, o.w & 0xff);
+          } else {
+            if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
           }
+        }
+        if (++rounds == 16) {
+          qx += ax;
+          qy += ay;
+          qz += az;
+          ax = ay = az = 0;
+          rounds = 0;
         }
       }
       for (; k < nn; k += G) {
@@ -1158,18 +1205,15 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
                                 4294967296.0f);
           }
         }
-        if (r2 < rc2) {
-          const int tj = o.w & 0xff;
-          if constexpr ((FL & F_ENERGY) == 0) {
-            const float mag = pair_mag_rsqrt(rowF + 6 * tj, r2) * fs;
-            qx += (long long)__float2int_rn(dx * mag);
-            qy += (long long)__float2int_rn(dy * mag);
-            qz += (long long)__float2int_rn(dz * mag);
-          } else {
-            eacc += pair_pot<float>(rowU + 6 * tj, sqrtf(r2));
-          }
+        if constexpr ((FL & F_ENERGY) == 0) {
+          pair_force_q(dx, dy, dz, r2, o.w & 0xff);
+        } else {
+          if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
         }
       }
+      qx += ax;
+      qy += ay;
+      qz += az;
       ep = 0.5 * (double)eacc;
     } else {
       const double4 me = P.d4[cur][i];

@@ -249,15 +249,19 @@ MpdSystem synth_bilayer(int seed, int nLipids, double density, double zsize, dou
 }
 
 void add_continuum_sphere(MpdSystem& s, const double pos[3], double R, double uminHead, double umaxHead,
+                          double umaxOther,
                           int beadType) {
   const int nT = s.nTypes;
   std::vector<double> C;
-  // laradjiSpanglerFC with Umax 10 / Umin 0 except the head-sphere entries,
-  // rc 2, rm 1, radius R-1, density 5.88 (continuumSphereAndLiposome.cpp:159-169)
+  // laradjiSpanglerFC with Umax umaxOther / Umin 0 except the head-sphere
+  // entries, rc 2, rm 1, radius R-1, density 5.88 (the generator default
+  // Umax is 10, continuumSphereAndLiposome.cpp:159-169).  The table's inner
+  // polynomial is a barrier only while (Umax - Umin) / 6 exceeds ~2.3 |Umin|
+  // (within ~1.3 sigma of the surface); deeper it is attractive and singular.
   for (int i = 0; i < nT; ++i)
     for (int j = 0; j < nT; ++j) {
       const int g = i + j * nT;
-      double umax = 10.0, umin = 0.0;
+      double umax = umaxOther, umin = 0.0;
       if (g == kHead + beadType * nT || g == beadType + kHead * nT) {
         umax = umaxHead;
         umin = uminHead;

@@ -38,6 +38,7 @@ MpdSystem synth_bilayer(int seed, int nLipids, double density, double zsize, dou
 // Adds one continuum sphere (BEAD residue) of radius R at pos with the
 // continuumSphereAndLiposome tables (head well depth uminHead).
 void add_continuum_sphere(MpdSystem& s, const double pos[3], double R, double uminHead, double umaxHead,
+                          double umaxOther,
                           int beadType);
 
 }  // namespace smd

@@ -15,7 +15,7 @@ sensitivity grows by ~e^(4.6 t / tau), so beyond ~50 steps no difference step
 converges, and the segment-local form (the adjoint restarted at every
 checkpoint) is the bounded estimate; it is checked against the sum of its
 segments' exact adjoints.  Gradient tolerance at the 1e-3 relative
-difference step: 1e-3 per component.
+difference step: 1e-3 per component, 3e-3 for kbend (FD_1E3_TOL).
 """
 import dataclasses
 
@@ -29,6 +29,12 @@ pytestmark = pytest.mark.gpu
 
 PREC = [smd.PLAIN_FP64, smd.MIXED]
 TAIL = 3
+# against differences at the 1e-3 step: 1e-3 for Umin and kbond; 3e-3 for
+# kbend, whose gradient is ~1e4 times smaller than Umin's.  At that step J is
+# only piecewise smooth (pairs cross rm and rc within it), and the quotient's
+# own error reaches ~1.5e-3 on kbend for some states; the exact check at 1e-7
+# resolves kbend to 1e-7.
+FD_1E3_TOL = np.array([1e-3, 1e-3, 3e-3])
 
 
 def with_params(m, umin=None, kbond=None, kbend=None, types=(TAIL, TAIL)):
@@ -83,11 +89,12 @@ def mean_potential(m, start, it0, steps, precision, theta=None):
 
 @pytest.fixture(scope="module")
 def bilayer500(tmp_path_factory):
-    """500-lipid flat bilayer, barostat off, after 200 steps from the lattice."""
+    """500-lipid flat bilayer, barostat off, after 200 steps from the lattice
+    (mixed form: bitwise reproducible, so every run starts from the same state)."""
     p = str(tmp_path_factory.mktemp("adj") / "b.mpd")
     smd.synth_bilayer(p, 4242, 500, 3.45, 15.0, 0.0, 0.0)
     m = smd.read_mpd(p)
-    s = smd.System(m, precision=smd.PLAIN_FP64)
+    s = smd.System(m, precision=smd.MIXED)
     s.prepare()
     s.advance(200)
     start = s.state()
@@ -170,7 +177,7 @@ def test_adjoint_against_differences_at_1e3(built, bilayer500, fd_fp64_10, preci
     fd = fd_fp64_10
     rel = np.abs(res["grad"] - fd) / np.abs(fd)
     print(f"precision {precision}: adjoint {res['grad']}, FD {fd}, rel err {rel}")
-    assert (rel < 1e-3).all()
+    assert (rel < FD_1E3_TOL).all()
 
 
 def test_mixed_gradient_against_fp64_reference_gradient(built, bilayer500):
@@ -252,7 +259,7 @@ def test_autograd_function_wrapper(built, bilayer500, fd_fp64_10):
     J = MeanPotential.apply(theta)
     (2.0 * J).backward()
     rel = np.abs(theta.grad.numpy() - 2.0 * fd_fp64_10) / np.abs(2.0 * fd_fp64_10)
-    assert (rel < 1e-3).all(), (theta.grad, fd_fp64_10)
+    assert (rel < FD_1E3_TOL).all(), (theta.grad, fd_fp64_10)
 
 
 def test_adjoint_rejects_barostat(built, tmp_path):

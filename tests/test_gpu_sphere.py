@@ -64,8 +64,9 @@ def test_sphere_energy_and_size_change(built, precision):
 
 def _sphere_mpd(tmp_path, final):
     p = str(tmp_path / "sph.mpd")
-    # a repulsive head core (Umax 100) keeps the run stable; well depth 10
-    smd.synth_vesicle_sphere(p, 99, 300, 3.45, 40.0, 5.0, -10.0, 100.0, 0.8)
+    # head well Umin -10 with Umax 300 and tails Umax 100: the table's inner
+    # polynomial is then a barrier that keeps beads out of the singular core
+    smd.synth_vesicle_sphere(p, 99, 300, 3.45, 40.0, 5.0, -10.0, 300.0, 0.8, 100.0)
     t = open(p).read()
     for key in ("finalTime", "storeInterval", "measureInterval"):
         t = re.sub(key + r" \S+", f"{key} {final}", t)
