@@ -725,6 +725,44 @@ __device__ __forceinline__ int flat_scan(const float4* stage, int mpad, float xi
   return count;
 }
 
+// Two beads (one warp) against the same staged candidates: one shared load
+// and one loop step serve both.  Appends as flat_scan does, per bead.
+template <bool THIN>
+__device__ __forceinline__ void flat_scan2(const float4* stage, int mpad, float xa, float ya, float za, int ia,
+                                           float xb, float yb, float zb, int ib, float lc2, float bx, float by,
+                                           float bz, int* outa, int* outb, int& ca, int& cb, int kmax, int lane) {
+  const unsigned int below = (1u << lane) - 1u;
+#pragma unroll 2
+  for (int k0 = 0; k0 < mpad; k0 += 32) {
+    const float4 cj = stage[k0 + lane];
+    const int j = __float_as_int(cj.w);
+    float dx = xa - cj.x, dy = ya - cj.y, dz = za - cj.z;
+    float ex = xb - cj.x, ey = yb - cj.y, ez = zb - cj.z;
+    if constexpr (THIN) {
+      dx -= bx * rintf(dx / bx);
+      dy -= by * rintf(dy / by);
+      dz -= bz * rintf(dz / bz);
+      ex -= bx * rintf(ex / bx);
+      ey -= by * rintf(ey / by);
+      ez -= bz * rintf(ez / bz);
+    }
+    bool ha = (dx * dx + dy * dy + dz * dz < lc2) & (j != ia);
+    bool hb = (ex * ex + ey * ey + ez * ez < lc2) & (j != ib);
+    if constexpr (THIN) {
+      ha = ha & (j >= 0);
+      hb = hb & (j >= 0);
+    }
+    const unsigned int hitsa = __ballot_sync(0xffffffffu, ha), hitsb = __ballot_sync(0xffffffffu, hb);
+    if (hitsa | hitsb) {
+      const int sa = ca + __popc(hitsa & below), sb = cb + __popc(hitsb & below);
+      if (ha && sa < kmax) outa[sa] = j;
+      if (hb && sb < kmax) outb[sb] = j;
+      ca += __popc(hitsa);
+      cb += __popc(hitsb);
+    }
+  }
+}
+
 template <int NT>
 __device__ __forceinline__ void nbr_cell_flat(const DevPtrs& P, int cur, int c) {
   const int s0 = P.cell_start[c], e0 = P.cell_start[c + 1];
@@ -794,15 +832,34 @@ __device__ __forceinline__ void nbr_cell_flat(const DevPtrs& P, int cur, int c) 
     // far sentinels complete the last round of 32 (index -1 matches no bead)
     for (int k = m + threadIdx.x; k < mpad; k += NT) stage[k] = make_float4(1e30f, 1e30f, 1e30f, __int_as_float(-1));
     __syncthreads();
-    for (int b = warp; b < nb; b += NT / 32) {
+    // beads in pairs (b, b + NT/32): warp w takes 2w, 2w+1 of every 2*NT/32
+    for (int b = 2 * warp; b < nb; b += 2 * (NT / 32)) {
       const int i = q.s + b;
       const uint4 mi = P.mt[i];
       const float xi = (float)(int)(mi.x - crx) * sx, yi = (float)(int)(mi.y - cry) * sy,
                   zi = (float)(int)(mi.z - crz) * sz;
       int* out = P.nbr + (size_t)i * kmax;
-      const int count = thin ? flat_scan<true>(stage, mpad, xi, yi, zi, i, lc2, bx, by, bz, out, cnt[b], kmax, lane)
-                             : flat_scan<false>(stage, mpad, xi, yi, zi, i, lc2, bx, by, bz, out, cnt[b], kmax, lane);
-      if (lane == 0) cnt[b] = count;
+      if (b + 1 < nb) {
+        const int i2 = i + 1;
+        const uint4 m2 = P.mt[i2];
+        const float x2 = (float)(int)(m2.x - crx) * sx, y2 = (float)(int)(m2.y - cry) * sy,
+                    z2 = (float)(int)(m2.z - crz) * sz;
+        int ca = cnt[b], cb = cnt[b + 1];
+        if (thin)
+          flat_scan2<true>(stage, mpad, xi, yi, zi, i, x2, y2, z2, i2, lc2, bx, by, bz, out, out + kmax, ca, cb, kmax,
+                           lane);
+        else
+          flat_scan2<false>(stage, mpad, xi, yi, zi, i, x2, y2, z2, i2, lc2, bx, by, bz, out, out + kmax, ca, cb, kmax,
+                            lane);
+        if (lane == 0) {
+          cnt[b] = ca;
+          cnt[b + 1] = cb;
+        }
+      } else {
+        const int count = thin ? flat_scan<true>(stage, mpad, xi, yi, zi, i, lc2, bx, by, bz, out, cnt[b], kmax, lane)
+                               : flat_scan<false>(stage, mpad, xi, yi, zi, i, lc2, bx, by, bz, out, cnt[b], kmax, lane);
+        if (lane == 0) cnt[b] = count;
+      }
     }
   }
   __syncthreads();
@@ -810,7 +867,7 @@ __device__ __forceinline__ void nbr_cell_flat(const DevPtrs& P, int cur, int c) 
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_nbr_cells_flat(DevPtrs P, int cur) {
+__global__ void __launch_bounds__(NT, 768 / NT) k_nbr_cells_flat(DevPtrs P, int cur) {
   if (!P.g->rebuild) return;
   list_build_begin(P);
   for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) nbr_cell_flat<NT>(P, cur, c);
@@ -1093,6 +1150,48 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
   }
 }
 
+// Bonded force on bead i: its share of the CHAIN bonds and bends (the bead
+// at chain position p takes bonds (p-1,p), (p,p+1) and bends (p-2..p),
+// (p-1..p+1), (p..p+2)), then its BOND / BEND residue terms in entry order.
+// FP32 in the mixed form (vectors exact from the fractional mirror), FP64 in
+// the plain form.  Every step variant takes its bonded force from here.
+template <bool MIXED>
+__device__ __forceinline__ Vec3<typename std::conditional<MIXED, float, double>::type> bonded_force(
+    const DevPtrs& P, int cur, int i, int ci, const double box[3], const RepState& rs) {
+  using R = typename std::conditional<MIXED, float, double>::type;
+  const Tables& T = *P.tab;
+  Vec3<R> fb{0, 0, 0};
+  if (ci < 0 && !(ci & 0x40000000)) {
+    const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
+    Vec3<R> er[4];
+    bool valid[4];
+    chain_vectors<MIXED, R>(P, cur, i, p, len, box, er, valid);
+    const R* cf;
+    if constexpr (MIXED) cf = T.chainF[set]; else cf = T.chainD[set];
+    if (valid[1]) bond_term<R>(er[1], cf, (R)-1, fb);  // bond (p-1,p): second
+    if (valid[2]) bond_term<R>(er[2], cf, (R)1, fb);   // bond (p,p+1): first
+    if (valid[0] && valid[1]) bend_term<R>(er[0], er[1], cf + 2, 2, fb);
+    if (valid[1] && valid[2]) bend_term<R>(er[1], er[2], cf + 2, 1, fb);
+    if (valid[2] && valid[3]) bend_term<R>(er[2], er[3], cf + 2, 0, fb);
+  }
+  if (P.n_terms > 0) {
+    const int o = P.orig[i];
+    const int e1 = P.term_off[o + 1];
+    for (int e = P.term_off[o]; e < e1; ++e) {
+      const int4 t = P.terms[e];
+      const int role = (t.x >> 1) & 3, set = t.x >> 3;
+      const R* cf;
+      if constexpr (MIXED) cf = T.termF[set]; else cf = T.termD[set];
+      if ((t.x & 1) == 0)  // bond (first, second): the bead's force is mag (x_self - x_other)
+        bond_term<R>(term_vec<MIXED, R>(P, cur, o, role == 0 ? t.z : t.y, box, rs), cf, (R)1, fb);
+      else  // bend (first, second, third): da = x1 - x2, db = x2 - x3
+        bend_term<R>(term_vec<MIXED, R>(P, cur, t.y, t.z, box, rs), term_vec<MIXED, R>(P, cur, t.z, t.w, box, rs),
+                     cf, role, fb);
+    }
+  }
+  return fb;
+}
+
 // Non-bonded pass: G lanes per bead walk the bead's Verlet-list entries
 // (bead-major, so a group reads G consecutive indices per round) and reduce
 // with shuffles.  MIXED: FP32 pair arithmetic, each pair force rounded to a
@@ -1100,8 +1199,9 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
 // on the order of the pairs; PLAIN: FP64 with the reference's neighbour-shift
 // minimum image.  Writes the per-bead pair force (fixed point or FP64) and,
 // with F_DU / F_ENERGY, the replica's pair U(x)-U(s x) / pair energy.
+constexpr int kGather = 4;  // neighbour gathers in flight per lane (mixed pair pass)
 template <bool MIXED, int FL, int G>
-__global__ void __launch_bounds__(kBlock, (MIXED && (FL & F_DU) == 0) ? 6 : 1) k_force(DevPtrs P, int cur) {
+__global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
   using R = typename std::conditional<MIXED, float, double>::type;
   __shared__ R sF[6 * kMaxTypes * kMaxTypes];
   __shared__ R sU[6 * kMaxTypes * kMaxTypes];
@@ -1159,13 +1259,14 @@ __global__ void __launch_bounds__(kBlock, (MIXED && (FL & F_DU) == 0) ? 6 : 1) k
       };
       int k = sub;
       int rounds = 0;
-      // two independent gathers in flight per lane
-      for (; k + G < nn; k += 2 * G) {
-        const int j0 = __ldg(nb + k), j1 = __ldg(nb + k + G);
-        const uint4 o0 = P.m4[cur][j0], o1 = P.m4[cur][j1];
+      // kGather independent gathers in flight per lane
+      for (; k + (kGather - 1) * G < nn; k += kGather * G) {
+        uint4 og[kGather];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const uint4 o = u ? o1 : o0;
+        for (int u = 0; u < kGather; ++u) og[u] = P.m4[cur][__ldg(nb + k + u * G)];
+#pragma unroll
+        for (int u = 0; u < kGather; ++u) {
+          const uint4 o = og[u];
           const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
           const float r2 = dx * dx + dy * dy + dz * dz;
           if constexpr ((FL & F_DU) != 0) {
@@ -1183,7 +1284,7 @@ __global__ void __launch_bounds__(kBlock, (MIXED && (FL & F_DU) == 0) ? 6 : 1) k
             if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
           }
         }
-        if (++rounds == 16) {
+        if (++rounds == 32 / kGather) {  // at most 32 pair terms per int32 sum
           qx += ax;
           qy += ay;
           qz += az;
@@ -1322,7 +1423,10 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
     Vec3<R> fb{0, 0, 0};
     const int ci = P.cinfo[i];
     const bool sphere = (ci < 0) && (ci & 0x40000000);  // integrated by k_sphere
-    if ((FL & F_PAIRONLY) == 0 && ci < 0 && !(ci & 0x40000000)) {
+    // bonded forces: one function for every step variant, so stopped and
+    // running steps round them alike
+    if constexpr ((FL & (F_PAIRONLY | F_ENERGY)) == 0) fb = bonded_force<MIXED>(P, cur, i, ci, box, rs);
+    if ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0 && ci < 0 && !(ci & 0x40000000)) {
       const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
       // forces in R from the same vectors in every variant; energies and
       // size-change differences in FP64
@@ -1337,15 +1441,6 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
 #pragma unroll
           for (int k = 0; k < 4; ++k) e[k] = Vec3<double>{er[k].x, er[k].y, er[k].z};
         }
-      }
-      if constexpr ((FL & F_ENERGY) == 0) {
-        const R* cf;
-        if constexpr (MIXED) cf = T.chainF[set]; else cf = T.chainD[set];
-        if (valid[1]) bond_term<R>(er[1], cf, (R)-1, fb);  // bond (p-1,p): second
-        if (valid[2]) bond_term<R>(er[2], cf, (R)1, fb);   // bond (p,p+1): first
-        if (valid[0] && valid[1]) bend_term<R>(er[0], er[1], cf + 2, 2, fb);
-        if (valid[1] && valid[2]) bend_term<R>(er[1], er[2], cf + 2, 1, fb);
-        if (valid[2] && valid[3]) bend_term<R>(er[2], er[3], cf + 2, 0, fb);
       }
       if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
         // energy terms owned by the first bead of each bond / bend, in FP64
@@ -1362,20 +1457,17 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
         }
       }
     }
-    // ---- BOND / BEND residue terms of this bead, in entry order
-    if constexpr ((FL & F_PAIRONLY) == 0) {
+    // ---- BOND / BEND residue terms of this bead: energies and differences
+    // (their forces are in bonded_force)
+    if constexpr ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0) {
       if (P.n_terms > 0) {
         const int o = P.orig[i];
         const int e1 = P.term_off[o + 1];
         for (int e = P.term_off[o]; e < e1; ++e) {
           const int4 t = P.terms[e];
           const int role = (t.x >> 1) & 3, set = t.x >> 3;
-          const R* cf;
-          if constexpr (MIXED) cf = T.termF[set]; else cf = T.termD[set];
           const double* cd = T.termD[set];
           if ((t.x & 1) == 0) {  // bond (first, second): the bead's force is mag (x_self - x_other)
-            if constexpr ((FL & F_ENERGY) == 0)
-              bond_term<R>(term_vec<MIXED, R>(P, cur, o, role == 0 ? t.z : t.y, box, rs), cf, (R)1, fb);
             if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
               if (role == 0) {  // energy terms owned by the first bead
                 const Vec3<double> d = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
@@ -1387,9 +1479,6 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
               }
             }
           } else {  // bend (first, second, third): da = x1 - x2, db = x2 - x3
-            if constexpr ((FL & F_ENERGY) == 0)
-              bend_term<R>(term_vec<MIXED, R>(P, cur, t.y, t.z, box, rs), term_vec<MIXED, R>(P, cur, t.z, t.w, box, rs),
-                           cf, role, fb);
             if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
               if (role == 0) {
                 const Vec3<double> da = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);

@@ -1,7 +1,7 @@
 """Autotuned launch configurations (smd_autotune / smd_set_tuning): every
-list-build kernel and lane count gives bitwise the same mixed-form trajectory,
-because pair forces are summed in int64 and the list content beyond rc never
-reaches the forces."""
+list-build kernel and lane count gives bitwise the same mixed-form
+trajectory: pair forces are summed in int64 and the list content beyond rc
+never reaches the forces."""
 import numpy as np
 import pytest
 
@@ -9,6 +9,7 @@ import softmold_gb300 as smd
 
 pytestmark = pytest.mark.gpu
 
+# (pair-pass lanes, list kernel)
 CONFIGS = [(8, 0), (4, 1), (16, 2), (8, 2), (16, 0)]
 
 
