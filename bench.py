@@ -425,8 +425,7 @@ def main():
         s.set_state(hp, hv)
         s.advance(E2E_INTERVAL)
         e = s.energy()
-        pp, vv = s.state()
-        hp[:], hv[:] = pp, vv
+        s.state(hp, hv)
         t1 = time.perf_counter()
         if k >= 2:
             e2e_t.append(t1 - t0)

@@ -100,8 +100,12 @@ void smd_destroy(smd_system* h);
 /* Runs later work on this CUDA stream (cudaStream_t; NULL = library stream). */
 int smd_set_stream(smd_system* h, void* cuda_stream);
 
-/* Copies all beads' state, replicas concatenated (Blob::getPositions /
- * getVelocities). */
+/* Copies all beads' state, replicas concatenated, in input order, xyz per
+ * bead (Blob::getPositions / getVelocities).  Either pointer may be NULL.
+ * The permutation to the device's cell order runs on the device, so each
+ * array is one contiguous host copy (fastest from pinned memory).  Setting
+ * positions rebuilds the Verlet list, growing it if the new configuration
+ * is denser. */
 int smd_get_state(smd_system* h, double* pos, double* vel);
 int smd_set_state(smd_system* h, const double* pos, const double* vel);
 int smd_get_box(smd_system* h, int replica, double box[3]);

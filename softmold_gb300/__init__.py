@@ -342,9 +342,15 @@ class System:
         except Exception:
             pass
 
-    def state(self):
-        p = np.zeros((self.n, 3))
-        v = np.zeros((self.n, 3))
+    def state(self, pos=None, vel=None):
+        """Positions and velocities in input order, (n, 3) FP64.  `pos` / `vel`
+        may be given as C-contiguous (n, 3) float64 arrays (pinned host memory
+        for the fastest copy) to be filled in place."""
+        p = np.empty((self.n, 3)) if pos is None else pos
+        v = np.empty((self.n, 3)) if vel is None else vel
+        for a in (p, v):
+            if a.dtype != np.float64 or a.shape != (self.n, 3) or not a.flags.c_contiguous:
+                raise ValueError("state buffers must be C-contiguous (n, 3) float64")
         _check(lib().smd_get_state(self.h, p.ctypes.data, v.ctypes.data), "smd_get_state")
         return p, v
 

@@ -105,21 +105,6 @@ __global__ void __launch_bounds__(kBlock) k_adj_load(DevPtrs P, int cur, const d
   finalize_step(P, bm, StepEnd{0, 0, 0, 0, 0});
 }
 
-// The state in file order: positions (and velocities if vs is not null).
-__global__ void __launch_bounds__(kBlock) k_adj_save(DevPtrs P, double* xs, double* vs) {
-  const int i = blockIdx.x * kBlock + threadIdx.x;
-  if (i >= P.n) return;
-  const int o = P.orig[i];
-  xs[3 * o] = P.x[i];
-  xs[3 * o + 1] = P.y[i];
-  xs[3 * o + 2] = P.z[i];
-  if (vs) {
-    vs[3 * o] = P.vx[i];
-    vs[3 * o + 1] = P.vy[i];
-    vs[3 * o + 2] = P.vz[i];
-  }
-}
-
 // Sorted-order copy of the adjoint direction w (file order) for the pair
 // gathers.
 template <typename V>

@@ -108,6 +108,7 @@ struct smd_system {
   } tune;
   cudaStream_t side = nullptr;  // captures the conditional bodies
   long long graph_builds = 0;   // device count of list builds run inside graphs
+  double* xfer = nullptr;       // 6n doubles: file-order positions and velocities for host copies
 
   template <typename T>
   int alloc(T** p, size_t count) {
@@ -381,6 +382,13 @@ int grow_list(smd_system* h, int need) {
     }
   SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(h->P.g, 1));
   return rebuild_if_needed(h, true);
+}
+
+// Device staging for the state copies: the host side moves one contiguous
+// file-order block per array and the permutation runs on the device.
+int xfer_buffer(smd_system* h) {
+  if (h->xfer) return 0;
+  return h->alloc(&h->xfer, (size_t)h->n * 6);
 }
 
 int read_error(smd_system* h) {
@@ -821,87 +829,49 @@ int smd_set_stream(smd_system* h, void* s) {
 
 int smd_get_state(smd_system* h, double* pos, double* vel) {
   if (!h) return fail(1, "null handle");
-  const int n = h->n;
-  std::vector<double> a(n), b(n), c(n), va(n), vb(n), vc(n);
-  std::vector<int> orig(n);
-  auto& P = h->P;
-  SMD_CUDA(cudaMemcpyAsync(a.data(), P.x, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaMemcpyAsync(b.data(), P.y, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaMemcpyAsync(c.data(), P.z, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaMemcpyAsync(va.data(), P.vx, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaMemcpyAsync(vb.data(), P.vy, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaMemcpyAsync(vc.data(), P.vz, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaMemcpyAsync(orig.data(), P.orig, n * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  if (!pos && !vel) return 0;
+  if (int rc = xfer_buffer(h)) return rc;
+  const size_t n3 = (size_t)h->n * 3;
+  double* xs = h->xfer;
+  double* vs = h->xfer + n3;
+  SMD_LAUNCH(h, k_state_save<<<h->grid(), kBlock, 0, h->stream>>>(h->P, pos ? xs : nullptr, vel ? vs : nullptr));
+  if (pos) SMD_CUDA(cudaMemcpyAsync(pos, xs, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (vel) SMD_CUDA(cudaMemcpyAsync(vel, vs, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
-  for (int i = 0; i < n; ++i) {
-    const int o = orig[i];
-    if (pos) {
-      pos[3 * o] = a[i];
-      pos[3 * o + 1] = b[i];
-      pos[3 * o + 2] = c[i];
-    }
-    if (vel) {
-      vel[3 * o] = va[i];
-      vel[3 * o + 1] = vb[i];
-      vel[3 * o + 2] = vc[i];
-    }
-  }
   return 0;
 }
 
 int smd_set_state(smd_system* h, const double* pos, const double* vel) {
   if (!h) return fail(1, "null handle");
-  const int n = h->n;
+  if (!pos && !vel) return 0;
+  if (int rc = xfer_buffer(h)) return rc;
   auto& P = h->P;
-  std::vector<int> orig(n);
-  SMD_CUDA(cudaMemcpyAsync(orig.data(), P.orig, n * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaStreamSynchronize(h->stream));
-  std::vector<double> a(n), b(n), c(n), va(n), vb(n), vc(n);
-  for (int i = 0; i < n; ++i) {
-    const int o = orig[i];
-    if (pos) {
-      a[i] = pos[3 * o];
-      b[i] = pos[3 * o + 1];
-      c[i] = pos[3 * o + 2];
-    }
-    if (vel) {
-      va[i] = vel[3 * o];
-      vb[i] = vel[3 * o + 1];
-      vc[i] = vel[3 * o + 2];
-    }
-  }
+  const size_t n3 = (size_t)h->n * 3;
+  double* xs = h->xfer;
+  double* vs = h->xfer + n3;
+  if (pos) SMD_CUDA(cudaMemcpyAsync(xs, pos, n3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (vel) SMD_CUDA(cudaMemcpyAsync(vs, vel, n3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SMD_LAUNCH(h, k_state_load<<<h->grid(), kBlock, 0, h->stream>>>(P, pos ? xs : nullptr, vel ? vs : nullptr));
   if (pos) {
-    SMD_CUDA(cudaMemcpy(P.x, a.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    SMD_CUDA(cudaMemcpy(P.y, b.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    SMD_CUDA(cudaMemcpy(P.z, c.data(), n * sizeof(double), cudaMemcpyHostToDevice));
     if (h->mixed)
       SMD_LAUNCH(h, k_mirror<true><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur));
     else
       SMD_LAUNCH(h, k_mirror<false><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur));
     SMD_LAUNCH(h, k_set_rebuild<<<1, 1, 0, h->stream>>>(P.g, 1));
   }
-  if (vel) {
-    SMD_CUDA(cudaMemcpy(P.vx, va.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    SMD_CUDA(cudaMemcpy(P.vy, vb.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    SMD_CUDA(cudaMemcpy(P.vz, vc.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-  }
   if (pos) {
-    // a new configuration may be denser than the list was sized for: count
-    // with zero capacity, then size and build
-    P.kmax = 0;
+    // a new configuration may be denser than the list was sized for: build,
+    // and if a bead overflowed, grow the list to its count and build again
     if (int rc = force_rebuild(h)) return rc;
     Global g;
     SMD_CUDA(cudaMemcpyAsync(&g, P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
     SMD_CUDA(cudaStreamSynchronize(h->stream));
-    P.kmax = h->kmax;
-    const int need = std::max(g.need_nbr, g.max_nbr);
-    g.error &= ~1;
-    g.need_nbr = 0;
-    SMD_CUDA(cudaMemcpy(P.g, &g, sizeof(Global), cudaMemcpyHostToDevice));
-    if (need > h->kmax * 4 / 5) {
+    if (g.error & 1) {
+      const int need = std::max(g.need_nbr, g.max_nbr);
+      g.error &= ~1;
+      g.need_nbr = 0;
+      SMD_CUDA(cudaMemcpy(P.g, &g, sizeof(Global), cudaMemcpyHostToDevice));
       if (int rc = grow_list(h, need)) return rc;
-    } else if (int rc = force_rebuild(h)) {
-      return rc;
     }
   }
   SMD_CUDA(cudaStreamSynchronize(h->stream));
@@ -1551,12 +1521,12 @@ int smd_adjoint(smd_system* h, const smd_adjoint_spec* spec, smd_adjoint_result*
     // ---- forward: the state at the start of every segment
     for (int c = 0; c < ncp; ++c) {
       double* x = cp + (size_t)c * 2 * n3;
-      SMD_LAUNCH(h, k_adj_save<<<h->grid(), kBlock, 0, h->stream>>>(P, x, x + n3));
+      SMD_LAUNCH(h, k_state_save<<<h->grid(), kBlock, 0, h->stream>>>(P, x, x + n3));
       cp_it[c] = h->it;
       const int len = std::min(K, T - c * K);
       if (int r = smd_advance(h, len, SMD_ASYNC)) return r;
     }
-    SMD_LAUNCH(h, k_adj_save<<<h->grid(), kBlock, 0, h->stream>>>(P, fin, fin + n3));
+    SMD_LAUNCH(h, k_state_save<<<h->grid(), kBlock, 0, h->stream>>>(P, fin, fin + n3));
     const long long it_end = h->it;
     SMD_CUDA(cudaMemsetAsync(A.w0, 0, n3 * sizeof(double), h->stream));
     SMD_CUDA(cudaMemsetAsync(A.xbar, 0, n3 * sizeof(double), h->stream));
@@ -1577,7 +1547,7 @@ int smd_adjoint(smd_system* h, const smd_adjoint_spec* spec, smd_adjoint_result*
       h->it = cp_it[c];
       SMD_LAUNCH(h, k_set_counters<<<1, 1, 0, h->stream>>>(P.g, h->it, 1, 0, 0));
       for (int m = 0; m < len; ++m) {  // recompute x_n of the segment
-        SMD_LAUNCH(h, k_adj_save<<<h->grid(), kBlock, 0, h->stream>>>(P, seg + (size_t)m * n3, nullptr));
+        SMD_LAUNCH(h, k_state_save<<<h->grid(), kBlock, 0, h->stream>>>(P, seg + (size_t)m * n3, nullptr));
         if (m + 1 < len)
           if (int r = smd_advance(h, 1, SMD_ASYNC)) return r;
       }

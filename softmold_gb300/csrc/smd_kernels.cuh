@@ -937,6 +937,41 @@ __device__ __forceinline__ double bend_pot(Vec3<double> da, Vec3<double> db, con
   return c[1] * p * p * 0.5;
 }
 
+// Size-change differences U(d) - U(s d) of the bonded terms in FP32 for the
+// mixed form, with sq[k] = s_k^2 - 1.  Both are factored through the exact
+// small quantities q = sum sq_k d_k^2 (= r'^2 - r^2) and its bend analogues,
+// so a scale near 1 cancels nothing:
+//   bond  1/2 k (r - l)^2:  (r - l)^2 - (r' - l)^2 = (r - r')(r + r' - 2l),
+//                           r - r' = -q / (r + r');
+//   bend  1/2 k (a - c)^2:  (a - c)^2 - (a - c')^2 = (c' - c)(2a - c - c'),
+//         c = p / (|da||db|), c' - c = (dp |da||db| + p (|da||db| - |da'||db'|)) / (|da||db||da'||db'|),
+//         |da||db| - |da'||db'| = -(da^2 qb + db^2 qa + qa qb) / (|da||db| + |da'||db'|).
+__device__ __forceinline__ float bond_dpot_f(Vec3<float> d, const float sq[3], const float* c) {
+  const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+  const float q = sq[0] * d.x * d.x + sq[1] * d.y * d.y + sq[2] * d.z * d.z;
+  const float r = sqrtf(r2), rn = sqrtf(r2 + q);
+  const float dr = -q / (r + rn);
+  return 0.5f * c[1] * dr * (r + rn - 2.f * c[0]);
+}
+__device__ __forceinline__ float bend_dpot_f(Vec3<float> da, Vec3<float> db, const float sq[3], const float* c) {
+  const float a2 = da.x * da.x + da.y * da.y + da.z * da.z, b2 = db.x * db.x + db.y * db.y + db.z * db.z;
+  const float p = da.x * db.x + da.y * db.y + da.z * db.z;
+  const float qa = sq[0] * da.x * da.x + sq[1] * da.y * da.y + sq[2] * da.z * da.z;
+  const float qb = sq[0] * db.x * db.x + sq[1] * db.y * db.y + sq[2] * db.z * db.z;
+  const float dp = sq[0] * da.x * db.x + sq[1] * da.y * db.y + sq[2] * da.z * db.z;
+  const float ab = sqrtf(a2 * b2), abn = sqrtf((a2 + qa) * (b2 + qb));
+  const float dab = -(a2 * qb + b2 * qa + qa * qb) / (ab + abn);
+  const float cs = p / ab;
+  const float dc = (dp * ab + p * dab) / (ab * abn);
+  return 0.5f * c[1] * dc * (2.f * (c[0] - cs) - dc);
+}
+
+// float -> int64 rounded to nearest, the same value as __float2ll_rn: values
+// below 2^31 in magnitude (nearly every pair term) take the 32-bit conversion.
+__device__ __forceinline__ long long f2ll_rn(float y) {
+  return (fabsf(y) < 2147483648.f) ? (long long)__float2int_rn(y) : __float2ll_rn(y);
+}
+
 // Difference vectors e[k] = x(p-2+k) - x(p-1+k), k = 0..3, of the chain
 // around bead i; valid[k] marks existing ones.  MIXED: exact from the 32-bit
 // fractional mirror (in FP64); PLAIN: FP64 with the bonded minimum image.
@@ -1274,8 +1309,8 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
             const float rn2 = r2 + q;
             if (r2 < rc2 || rn2 < rc2) {
               const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
-              dq += __float2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
-                                  4294967296.0f);
+              dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
+                            4294967296.0f);
             }
           }
           if constexpr ((FL & F_ENERGY) == 0) {
@@ -1302,8 +1337,8 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
           const float rn2 = r2 + q;
           if (r2 < rc2 || rn2 < rc2) {
             const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
-            dq += __float2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
-                                4294967296.0f);
+            dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
+                          4294967296.0f);
           }
         }
         if constexpr ((FL & F_ENERGY) == 0) {
@@ -1428,28 +1463,36 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
     if constexpr ((FL & (F_PAIRONLY | F_ENERGY)) == 0) fb = bonded_force<MIXED>(P, cur, i, ci, box, rs);
     if ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0 && ci < 0 && !(ci & 0x40000000)) {
       const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
-      // forces in R from the same vectors in every variant; energies and
-      // size-change differences in FP64
+      // the chain's difference vectors in R (exact from the fractional
+      // mirror in the mixed form)
       Vec3<R> er[4];
       bool valid[4];
       chain_vectors<MIXED, R>(P, cur, i, p, len, box, er, valid);
-      Vec3<double> e[4];
-      if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
+      // terms owned by the first bead of each bond / bend: energies in FP64;
+      // size-change differences in FP64 (plain) or factored FP32 (mixed)
+      if constexpr (MIXED && (FL & F_DU) != 0) {
+        const float* cf = T.chainF[set];
+        const float sq[3] = {(float)(rs.scale[0] * rs.scale[0] - 1.0), (float)(rs.scale[1] * rs.scale[1] - 1.0),
+                             (float)(rs.scale[2] * rs.scale[2] - 1.0)};
+        float du = 0.f;
+        if (valid[2]) du += bond_dpot_f(er[2], sq, cf);
+        if (valid[2] && valid[3]) du += bend_dpot_f(er[2], er[3], sq, cf + 2);
+        dU_bond += (double)du;
+      }
+      if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
+        Vec3<double> e[4];
         if constexpr (MIXED) {
           chain_vectors<MIXED, double>(P, cur, i, p, len, box, e, valid);
         } else {
 #pragma unroll
           for (int k = 0; k < 4; ++k) e[k] = Vec3<double>{er[k].x, er[k].y, er[k].z};
         }
-      }
-      if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
-        // energy terms owned by the first bead of each bond / bend, in FP64
         const double* cd = T.chainD[set];
         if constexpr ((FL & F_ENERGY) != 0) {
           if (valid[2]) e_bond += bond_pot(e[2], cd);
           if (valid[2] && valid[3]) e_bond += bend_pot(e[2], e[3], cd + 2);
         }
-        if constexpr ((FL & F_DU) != 0) {
+        if constexpr (!MIXED && (FL & F_DU) != 0) {
           const Vec3<double> s2{e[2].x * rs.scale[0], e[2].y * rs.scale[1], e[2].z * rs.scale[2]};
           const Vec3<double> s3{e[3].x * rs.scale[0], e[3].y * rs.scale[1], e[3].z * rs.scale[2]};
           if (valid[2]) dU_bond += bond_pot(e[2], cd) - bond_pot(s2, cd);
@@ -1463,6 +1506,8 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
       if (P.n_terms > 0) {
         const int o = P.orig[i];
         const int e1 = P.term_off[o + 1];
+        const float sq_f[3] = {(float)(rs.scale[0] * rs.scale[0] - 1.0), (float)(rs.scale[1] * rs.scale[1] - 1.0),
+                               (float)(rs.scale[2] * rs.scale[2] - 1.0)};
         for (int e = P.term_off[o]; e < e1; ++e) {
           const int4 t = P.terms[e];
           const int role = (t.x >> 1) & 3, set = t.x >> 3;
@@ -1470,24 +1515,35 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
           if ((t.x & 1) == 0) {  // bond (first, second): the bead's force is mag (x_self - x_other)
             if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
               if (role == 0) {  // energy terms owned by the first bead
-                const Vec3<double> d = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
-                if constexpr ((FL & F_ENERGY) != 0) e_bond += bond_pot(d, cd);
-                if constexpr ((FL & F_DU) != 0) {
-                  const Vec3<double> sd{d.x * rs.scale[0], d.y * rs.scale[1], d.z * rs.scale[2]};
-                  dU_bond += bond_pot(d, cd) - bond_pot(sd, cd);
+                if constexpr (MIXED && (FL & F_DU) != 0)
+                  dU_bond += (double)bond_dpot_f(term_vec<MIXED, float>(P, cur, t.y, t.z, box, rs), sq_f,
+                                                 T.termF[set]);
+                if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
+                  const Vec3<double> d = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
+                  if constexpr ((FL & F_ENERGY) != 0) e_bond += bond_pot(d, cd);
+                  if constexpr (!MIXED && (FL & F_DU) != 0) {
+                    const Vec3<double> sd{d.x * rs.scale[0], d.y * rs.scale[1], d.z * rs.scale[2]};
+                    dU_bond += bond_pot(d, cd) - bond_pot(sd, cd);
+                  }
                 }
               }
             }
           } else {  // bend (first, second, third): da = x1 - x2, db = x2 - x3
             if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
               if (role == 0) {
-                const Vec3<double> da = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
-                const Vec3<double> db = term_vec<MIXED, double>(P, cur, t.z, t.w, box, rs);
-                if constexpr ((FL & F_ENERGY) != 0) e_bond += bend_pot(da, db, cd);
-                if constexpr ((FL & F_DU) != 0) {
-                  const Vec3<double> sa{da.x * rs.scale[0], da.y * rs.scale[1], da.z * rs.scale[2]};
-                  const Vec3<double> sb{db.x * rs.scale[0], db.y * rs.scale[1], db.z * rs.scale[2]};
-                  dU_bond += bend_pot(da, db, cd) - bend_pot(sa, sb, cd);
+                if constexpr (MIXED && (FL & F_DU) != 0)
+                  dU_bond += (double)bend_dpot_f(term_vec<MIXED, float>(P, cur, t.y, t.z, box, rs),
+                                                 term_vec<MIXED, float>(P, cur, t.z, t.w, box, rs), sq_f,
+                                                 T.termF[set]);
+                if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
+                  const Vec3<double> da = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
+                  const Vec3<double> db = term_vec<MIXED, double>(P, cur, t.z, t.w, box, rs);
+                  if constexpr ((FL & F_ENERGY) != 0) e_bond += bend_pot(da, db, cd);
+                  if constexpr (!MIXED && (FL & F_DU) != 0) {
+                    const Vec3<double> sa{da.x * rs.scale[0], da.y * rs.scale[1], da.z * rs.scale[2]};
+                    const Vec3<double> sb{db.x * rs.scale[0], db.y * rs.scale[1], db.z * rs.scale[2]};
+                    dU_bond += bend_pot(da, db, cd) - bend_pot(sa, sb, cd);
+                  }
                 }
               }
             }
@@ -1936,6 +1992,43 @@ __global__ void __launch_bounds__(kBlock) k_mirror(DevPtrs P, int cur) {
   } else {
     const double4 me = P.d4[cur][i];
     P.d4[cur][i] = make_double4(P.x[i], P.y[i], P.z[i], me.w);
+  }
+}
+
+// State in file order (x0 y0 z0 x1 ..., the order of the input's beads) from
+// the sorted device arrays: a gather through orig, so the host copy is one
+// contiguous block per array.  Either output may be null.
+__global__ void __launch_bounds__(kBlock) k_state_save(DevPtrs P, double* xs, double* vs) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= P.n) return;
+  const int o = P.orig[i];
+  if (xs) {
+    xs[3 * o] = P.x[i];
+    xs[3 * o + 1] = P.y[i];
+    xs[3 * o + 2] = P.z[i];
+  }
+  if (vs) {
+    vs[3 * o] = P.vx[i];
+    vs[3 * o + 1] = P.vy[i];
+    vs[3 * o + 2] = P.vz[i];
+  }
+}
+
+// The inverse scatter: file-order positions and / or velocities into the
+// sorted device arrays (the caller refreshes the mirror after positions).
+__global__ void __launch_bounds__(kBlock) k_state_load(DevPtrs P, const double* xs, const double* vs) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= P.n) return;
+  const int o = P.orig[i];
+  if (xs) {
+    P.x[i] = xs[3 * o];
+    P.y[i] = xs[3 * o + 1];
+    P.z[i] = xs[3 * o + 2];
+  }
+  if (vs) {
+    P.vx[i] = vs[3 * o];
+    P.vy[i] = vs[3 * o + 1];
+    P.vz[i] = vs[3 * o + 2];
   }
 }
 
