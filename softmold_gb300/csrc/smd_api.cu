@@ -132,11 +132,13 @@ struct smd_system {
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
   int grid() const { return (n + kBlock - 1) / kBlock; }
+  int bead_grid() const { return (n + kBeadBlock - 1) / kBeadBlock; }
   int grid_lanes(int g = kLanes) const { return (int)(((long long)n * g + kBlock - 1) / kBlock); }
   int sms = 152;
-  // list build: one CTA per cell; the hardware scheduler balances the very
-  // uneven cell occupancy of a membrane better than a fixed stride does
-  int nbr_grid() const { return n_cells; }
+  // list build: CTA b builds occupied cell b; beyond 32 CTAs per SM the rest
+  // come from a device work queue (sparse boxes have far more cells than
+  // occupied ones, and an idle CTA per empty cell costs launch time)
+  int nbr_grid() const { return std::min(n_cells, sms * 32); }
 };
 
 namespace {
@@ -172,8 +174,8 @@ __global__ void k_graph_cond(const Global* g, unsigned long long cond) {
 // last block recomputes it from the displacement bound.
 int launch_rebuild(smd_system* h, cudaStream_t st, int cur, int in_graph) {
   auto& P = h->P;
-  const int g = h->grid();
-  SMD_LAUNCH(h, k_bin<<<g, kBlock, 0, st>>>(P, cur, h->mixed ? 1 : 0, in_graph));
+  const int gb = h->bead_grid();
+  SMD_LAUNCH(h, k_bin<<<gb, kBeadBlock, 0, st>>>(P, cur, h->mixed ? 1 : 0, in_graph));
   if (h->n_cells <= kScanOneMax) {
     SMD_LAUNCH(h, k_scan_one<<<1, kScanOneThreads, 0, st>>>(P));
   } else {
@@ -182,14 +184,14 @@ int launch_rebuild(smd_system* h, cudaStream_t st, int cur, int in_graph) {
     SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, st>>>(P));
   }
   if (h->mixed) {
-    SMD_LAUNCH(h, k_reorder<true><<<g, kBlock, 0, st>>>(P, cur));
+    SMD_LAUNCH(h, k_reorder<true><<<gb, kBeadBlock, 0, st>>>(P, cur));
     switch (h->tune.list) {
       case 1: SMD_LAUNCH(h, (k_nbr_cells_flat<256><<<h->nbr_grid(), 256, 0, st>>>(P, cur))); break;
       case 2: SMD_LAUNCH(h, (k_nbr_cells_oct<<<h->nbr_grid(), kOctThreads, 0, st>>>(P, cur))); break;
       default: SMD_LAUNCH(h, (k_nbr_cells_flat<128><<<h->nbr_grid(), 128, 0, st>>>(P, cur))); break;
     }
   } else {
-    SMD_LAUNCH(h, k_reorder<false><<<g, kBlock, 0, st>>>(P, cur));
+    SMD_LAUNCH(h, k_reorder<false><<<gb, kBeadBlock, 0, st>>>(P, cur));
     SMD_LAUNCH(h, (k_nbr_cells_plain<<<h->nbr_grid(), kNbrThreads, 0, st>>>(P, cur)));
   }
   return 0;
@@ -238,7 +240,6 @@ int prof_mark(smd_system* h) {
 template <int FL>
 int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   auto& P = h->P;
-  const int g = h->grid();
   constexpr bool kLoopStep = (FL & (F_FORCES | F_ENERGY | F_INIT)) == 0;
   if (kLoopStep && h->profile) {
     if (int rc = prof_mark(h)) return rc;
@@ -259,11 +260,11 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
     } else {
       SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
     }
-    SMD_LAUNCH(h, (k_integ<true, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, se)));
+    SMD_LAUNCH(h, (k_integ<true, FL><<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur, se)));
     if (h->n_sph) SMD_LAUNCH(h, (k_sphere<true, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   } else {
     SMD_LAUNCH(h, (k_force<false, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
-    SMD_LAUNCH(h, (k_integ<false, FL><<<g, kBlock, 0, h->stream>>>(P, h->cur, se)));
+    SMD_LAUNCH(h, (k_integ<false, FL><<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur, se)));
     if (h->n_sph) SMD_LAUNCH(h, (k_sphere<false, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   }
   if (kLoopStep && h->profile) {
@@ -286,11 +287,10 @@ int launch_force_only(smd_system* h) {
 // mode bit 0: restart half-kick; bit 1: completes a stopped loop step.
 int launch_finish(smd_system* h, int mode, int apply_mc, StepEnd se) {
   auto& P = h->P;
-  const int g = h->grid();
   if (h->mixed)
-    SMD_LAUNCH(h, k_finish<true><<<g, kBlock, 0, h->stream>>>(P, h->cur, mode, apply_mc, se));
+    SMD_LAUNCH(h, k_finish<true><<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur, mode, apply_mc, se));
   else
-    SMD_LAUNCH(h, k_finish<false><<<g, kBlock, 0, h->stream>>>(P, h->cur, mode, apply_mc, se));
+    SMD_LAUNCH(h, k_finish<false><<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur, mode, apply_mc, se));
   h->cur ^= 1;
   return 0;
 }
@@ -677,7 +677,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     if ((rc = h->alloc(&P.fp, 3 * (size_t)total))) return rc;
   }
   if ((rc = h->alloc(&P.cell_count, cells)) || (rc = h->alloc(&P.cell_start, cells + 1)) ||
-      (rc = h->alloc(&P.block_sums, h->n_tiles)))
+      (rc = h->alloc(&P.block_sums, h->n_tiles)) || (rc = h->alloc(&P.occ, cells)))
     return rc;
   if ((rc = h->alloc(&P.rp, n_rep)) || (rc = h->alloc(&P.rs, n_rep)) || (rc = h->alloc(&P.g, 1))) return rc;
   Tables* tdev = nullptr;

@@ -25,6 +25,9 @@ constexpr int kMaxTypes = 8;
 constexpr int kMaxChainSets = 32;
 constexpr int kMaxTermSets = 64;  // distinct constant pairs of BOND / BEND residues
 constexpr int kBlock = 256;
+// threads per CTA of the per-bead step kernels (bin, reorder, integrator):
+// small CTAs spread a small system over every SM
+constexpr int kBeadBlock = 128;
 constexpr int kScanTile = 2048;  // cells per scan block (256 threads x 8)
 constexpr int kLanes = 8;        // lanes per bead in the list build and the pair pass
 constexpr int kMaxSpheres = 16;  // BEAD beads of one handle (the reference's brute-force branch takes <= 20)
@@ -102,6 +105,8 @@ struct Global {  // single instance
   int trial_slot;              // staged barostat trial used by the next MC step
   long long it;                // loop step (the Langevin noise key); advanced by the step's last kernel
   long long graph_builds;      // list builds run inside graph conditional bodies
+  int n_occ;                   // occupied list cells of the current build
+  int next_cell;               // work queue of the list kernels over occ[]
 };
 
 // Bookkeeping of the kernel that completes a step (its last block): advance
@@ -151,6 +156,7 @@ struct DevPtrs {
   int *torig, *tcinfo;
   int *key, *slot, *tkey;
   int *cell_count, *cell_start, *block_sums;
+  int* occ;          // occupied list cells of the last build (count in Global::n_occ)
   int *nbr, *nnbr;
   long long* fq;     // MIXED pair force, fixed point, 3*n (x | y | z)
   double* fp;        // PLAIN pair force, 3*n

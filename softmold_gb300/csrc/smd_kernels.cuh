@@ -66,9 +66,9 @@ __device__ __forceinline__ float displacement(uint4 ref, unsigned int fx, unsign
 // ------------------------------------------------------------ list build
 // Verlet-list cell of bead i from its 32-bit fractional coordinates: the
 // cell index along an axis is floor(f * n / 2^32), always in [0, n).
-__global__ void __launch_bounds__(kBlock) k_bin(DevPtrs P, int cur, int mixed, int in_graph) {
+__global__ void __launch_bounds__(kBeadBlock) k_bin(DevPtrs P, int cur, int mixed, int in_graph) {
   if (!P.g->rebuild) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * kBeadBlock + threadIdx.x;
   if (in_graph && i == 0) P.g->graph_builds++;
   if (i >= P.n) return;
   const int r = rep_of(P, i);
@@ -142,6 +142,10 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
 
 __global__ void __launch_bounds__(kBlock) k_scan_sums(DevPtrs P, int n_tiles) {
   if (!P.g->rebuild) return;
+  if (threadIdx.x == 0) {  // k_scan_apply appends the occupied cells
+    P.g->n_occ = 0;
+    P.g->next_cell = 0;
+  }
   int carry = 0;
   for (int base = 0; base < n_tiles; base += kBlock) {
     const int t = base + threadIdx.x;
@@ -164,6 +168,16 @@ __global__ void __launch_bounds__(kBlock) k_scan_apply(DevPtrs P) {
     const int ex = block_exclusive_scan(v, &total);
     if (c < P.n_cells_total) P.cell_start[c] = carry + ex;
     carry += total;
+    // occupied cells, appended one warp at a time (their order is free: each
+    // cell's list does not depend on when it is built)
+    const unsigned int occ = __ballot_sync(0xffffffffu, v > 0);
+    if (occ) {
+      const int lane = threadIdx.x & 31;
+      int at = 0;
+      if (lane == 0) at = atomicAdd(&P.g->n_occ, __popc(occ));
+      at = __shfl_sync(0xffffffffu, at, 0);
+      if (v > 0) P.occ[at + __popc(occ & ((1u << lane) - 1u))] = c;
+    }
   }
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) P.cell_start[P.n_cells_total] = P.n;
 }
@@ -175,54 +189,81 @@ constexpr int kScanOneThreads = 1024;
 constexpr int kScanOneMax = 32768;
 __global__ void __launch_bounds__(kScanOneThreads) k_scan_one(DevPtrs P) {
   if (!P.g->rebuild) return;
-  __shared__ int wsum[kScanOneThreads / 32];
+  __shared__ int wsum[kScanOneThreads / 32], osum[kScanOneThreads / 32];
   const int n = P.n_cells_total;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int carry = 0;
+  int carry = 0, ocarry = 0;  // beads and occupied cells before the chunk
   for (int base = 0; base < n; base += kScanOneThreads * 8) {
     const int c0 = base + threadIdx.x * 8;
     int v[8];
-    int s = 0;
+    int s = 0, f = 0;
+    if (c0 + 8 <= n) {  // two 16-byte loads (the arrays are 16-byte aligned and c0 % 8 == 0)
+      const int4 a = *reinterpret_cast<const int4*>(P.cell_count + c0);
+      const int4 b = *reinterpret_cast<const int4*>(P.cell_count + c0 + 4);
+      v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = (c0 + k < n) ? P.cell_count[c0 + k] : 0;
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      v[k] = (c0 + k < n) ? P.cell_count[c0 + k] : 0;
       s += v[k];
+      f += v[k] > 0;
     }
-    int x = s;
+    int x = s, xo = f;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
+      const int y = __shfl_up_sync(0xffffffffu, x, o), yo = __shfl_up_sync(0xffffffffu, xo, o);
+      if (lane >= o) {
+        x += y;
+        xo += yo;
+      }
     }
-    if (lane == 31) wsum[w] = x;
+    if (lane == 31) {
+      wsum[w] = x;
+      osum[w] = xo;
+    }
     __syncthreads();
     if (w == 0) {
-      int t = wsum[lane];
+      int t = wsum[lane], to = osum[lane];
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, t, o);
-        if (lane >= o) t += y;
+        const int y = __shfl_up_sync(0xffffffffu, t, o), yo = __shfl_up_sync(0xffffffffu, to, o);
+        if (lane >= o) {
+          t += y;
+          to += yo;
+        }
       }
       wsum[lane] = t;
+      osum[lane] = to;
     }
     __syncthreads();
     int ex = carry + (w > 0 ? wsum[w - 1] : 0) + x - s;
+    int eo = ocarry + (w > 0 ? osum[w - 1] : 0) + xo - f;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      if (c0 + k < n) P.cell_start[c0 + k] = ex;
+      if (c0 + k < n) {
+        P.cell_start[c0 + k] = ex;
+        if (v[k] > 0) P.occ[eo++] = c0 + k;
+      }
       ex += v[k];
     }
     carry += wsum[kScanOneThreads / 32 - 1];
-    __syncthreads();  // wsum is rewritten by the next chunk
+    ocarry += osum[kScanOneThreads / 32 - 1];
+    __syncthreads();  // wsum, osum are rewritten by the next chunk
   }
-  if (threadIdx.x == 0) P.cell_start[n] = P.n;
+  if (threadIdx.x == 0) {
+    P.cell_start[n] = P.n;
+    P.g->n_occ = ocarry;
+    P.g->next_cell = 0;
+  }
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(kBlock) k_reorder(DevPtrs P, int cur) {
+__global__ void __launch_bounds__(kBeadBlock) k_reorder(DevPtrs P, int cur) {
   if (!P.g->rebuild) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
-  for (int c = i; c < P.n_cells_total; c += gridDim.x * kBlock) P.cell_count[c] = 0;
+  const int i = blockIdx.x * kBeadBlock + threadIdx.x;
+  for (int c = i; c < P.n_cells_total; c += gridDim.x * kBeadBlock) P.cell_count[c] = 0;
   if (i >= P.n) return;
   const int nw = P.cell_start[P.key[i]] + P.slot[i];
   const double x = P.x[i], y = P.y[i], z = P.z[i];
@@ -381,6 +422,25 @@ __device__ __forceinline__ void list_counts(const DevPtrs& P, const CellCtx& q, 
   }
 }
 
+// Occupied cells of this CTA for the list kernels: round 0 takes
+// occ[blockIdx.x] without a claim; when the occupied cells outnumber the CTAs,
+// later rounds take the rest from a device work queue, one at a time, which
+// balances the very uneven cell occupancy.  -1 when none is left.  Every
+// thread of the CTA gets the same cell.
+__device__ __forceinline__ int list_cell(const DevPtrs& P, int round) {
+  __shared__ int cell;
+  const int n_occ = P.g->n_occ;
+  if (round == 0) return (int)blockIdx.x < n_occ ? P.occ[blockIdx.x] : -1;
+  if ((int)gridDim.x >= n_occ) return -1;
+  __syncthreads();  // every thread has read the previous cell
+  if (threadIdx.x == 0) {
+    const int k = (int)gridDim.x + atomicAdd(&P.g->next_cell, 1);
+    cell = k < n_occ ? P.occ[k] : -1;
+  }
+  __syncthreads();
+  return cell;
+}
+
 __device__ __forceinline__ void list_build_begin(const DevPtrs& P) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     P.g->slack = 0.0;
@@ -461,7 +521,7 @@ __device__ __forceinline__ void nbr_cell_plain(const DevPtrs& P, int cur, int c)
 __global__ void __launch_bounds__(kNbrThreads) k_nbr_cells_plain(DevPtrs P, int cur) {
   if (!P.g->rebuild) return;
   list_build_begin(P);
-  for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) nbr_cell_plain(P, cur, c);
+  for (int r = 0, c = list_cell(P, 0); c >= 0; c = list_cell(P, ++r)) nbr_cell_plain(P, cur, c);
 }
 
 // ---- Mixed form, octant-filtered.  Candidates are staged as FP32 offsets
@@ -684,7 +744,7 @@ __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
 __global__ void __launch_bounds__(kOctThreads) k_nbr_cells_oct(DevPtrs P, int cur) {
   if (!P.g->rebuild) return;
   list_build_begin(P);
-  for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) nbr_cell_oct(P, cur, c);
+  for (int r = 0, c = list_cell(P, 0); c >= 0; c = list_cell(P, ++r)) nbr_cell_oct(P, cur, c);
 }
 
 // ---- Mixed form, flat stencil.  The CTA stages the stencil's beads as FP32
@@ -870,7 +930,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT, 768 / NT) k_nbr_cells_flat(DevPtrs P, int cur) {
   if (!P.g->rebuild) return;
   list_build_begin(P);
-  for (int c = blockIdx.x; c < P.n_cells_total; c += gridDim.x) nbr_cell_flat<NT>(P, cur, c);
+  for (int r = 0, c = list_cell(P, 0); c >= 0; c = list_cell(P, ++r)) nbr_cell_flat<NT>(P, cur, c);
 }
 
 // ------------------------------------------------------------ the step
@@ -1432,10 +1492,10 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
 // position mirror for the next force pass.  Flags select the stopped,
 // start-up, force-only and energy-only variants.
 template <bool MIXED, int FL>
-__global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se) {
+__global__ void __launch_bounds__(kBeadBlock) k_integ(DevPtrs P, int cur, StepEnd se) {
   const long long it = P.g->it;
   const Tables& T = *P.tab;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * kBeadBlock + threadIdx.x;
   const bool active = i < P.n;
   const int r = active ? rep_of(P, i) : 0;
   double dU_bond = 0.0, e_bond = 0.0, e_kin = 0.0;
@@ -1672,12 +1732,12 @@ __global__ void __launch_bounds__(kBlock) k_integ(DevPtrs P, int cur, StepEnd se
   }
   if constexpr ((FL & (F_STOP | F_INIT | F_FORCES | F_ENERGY)) == 0) {
     vmax = warp_max(vmax);
-    __shared__ float smax[kBlock / 32];
+    __shared__ float smax[kBeadBlock / 32];
     if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = vmax;
     __syncthreads();
     float bm = 0.f;
     if (threadIdx.x == 0)
-      for (int w = 0; w < kBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
+      for (int w = 0; w < kBeadBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
     if (P.n_sph > 0) {
       // k_sphere completes the step once the spheres have moved
       if (threadIdx.x == 0 && bm > 0.f) atomicMax(&P.g->dmax_bits, __float_as_uint(bm));
@@ -1754,8 +1814,8 @@ __global__ void k_mc(DevPtrs P) {
 // before first() (MD.cpp:340-355, 480-509), so a first half-kick that follows
 // a second one uses a / m^2, the one of a fresh start a / m.
 template <bool MIXED>
-__global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int mode, int apply_mc, StepEnd se) {
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+__global__ void __launch_bounds__(kBeadBlock) k_finish(DevPtrs P, int cur, int mode, int apply_mc, StepEnd se) {
+  const int i = blockIdx.x * kBeadBlock + threadIdx.x;
   const int do_second = mode & 1;
   float vmax = 0.f;
   if (i < P.n) {
@@ -1807,12 +1867,12 @@ __global__ void __launch_bounds__(kBlock) k_finish(DevPtrs P, int cur, int mode,
     }
   }
   vmax = warp_max(vmax);
-  __shared__ float smax[kBlock / 32];
+  __shared__ float smax[kBeadBlock / 32];
   if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = vmax;
   __syncthreads();
   float bm = 0.f;
   if (threadIdx.x == 0)
-    for (int w = 0; w < kBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
+    for (int w = 0; w < kBeadBlock / 32; ++w) bm = fmaxf(bm, smax[w]);
   finalize_step(P, bm, se);
 }
 
