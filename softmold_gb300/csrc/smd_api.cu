@@ -150,11 +150,38 @@ int check_launch(smd_system* h) {
   return 0;
 }
 
+// Launch with programmatic stream serialization: the kernel may start while
+// the previous kernel in the stream drains (it waits for that kernel's
+// results on the device).  Kernel nodes captured this way keep the
+// programmatic edge in the graph.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 #define SMD_LAUNCH(h, ...)               \
   do {                                   \
     __VA_ARGS__;                         \
     int rc_ = check_launch(h);           \
     if (rc_) return rc_;                 \
+  } while (0)
+
+#define SMD_PDL(h, ...)                                                                          \
+  do {                                                                                           \
+    const cudaError_t e_ = launch_pdl(__VA_ARGS__);                                              \
+    if (e_ != cudaSuccess) return fail(200 + (int)e_, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    int rc_ = check_launch(h);                                                                   \
+    if (rc_) return rc_;                                                                         \
   } while (0)
 
 __global__ void k_set_rebuild(Global* g, int v) { g->rebuild = v; }
@@ -177,22 +204,22 @@ int launch_rebuild(smd_system* h, cudaStream_t st, int cur, int in_graph) {
   const int gb = h->bead_grid();
   SMD_LAUNCH(h, k_bin<<<gb, kBeadBlock, 0, st>>>(P, cur, h->mixed ? 1 : 0, in_graph));
   if (h->n_cells <= kScanOneMax) {
-    SMD_LAUNCH(h, k_scan_one<<<1, kScanOneThreads, 0, st>>>(P));
+    SMD_PDL(h, k_scan_one, 1, kScanOneThreads, st, P);
   } else {
     SMD_LAUNCH(h, k_scan_tiles<<<h->n_tiles, kBlock, 0, st>>>(P));
     SMD_LAUNCH(h, k_scan_sums<<<1, kBlock, 0, st>>>(P, h->n_tiles));
     SMD_LAUNCH(h, k_scan_apply<<<h->n_tiles, kBlock, 0, st>>>(P));
   }
   if (h->mixed) {
-    SMD_LAUNCH(h, k_reorder<true><<<gb, kBeadBlock, 0, st>>>(P, cur));
+    SMD_PDL(h, k_reorder<true>, gb, kBeadBlock, st, P, cur);
     switch (h->tune.list) {
-      case 1: SMD_LAUNCH(h, (k_nbr_cells_flat<256><<<h->nbr_grid(), 256, 0, st>>>(P, cur))); break;
-      case 2: SMD_LAUNCH(h, (k_nbr_cells_oct<<<h->nbr_grid(), kOctThreads, 0, st>>>(P, cur))); break;
-      default: SMD_LAUNCH(h, (k_nbr_cells_flat<128><<<h->nbr_grid(), 128, 0, st>>>(P, cur))); break;
+      case 1: SMD_PDL(h, k_nbr_cells_flat<256>, h->nbr_grid(), 256, st, P, cur); break;
+      case 2: SMD_PDL(h, k_nbr_cells_oct, h->nbr_grid(), kOctThreads, st, P, cur); break;
+      default: SMD_PDL(h, k_nbr_cells_flat<128>, h->nbr_grid(), 128, st, P, cur); break;
     }
   } else {
-    SMD_LAUNCH(h, k_reorder<false><<<gb, kBeadBlock, 0, st>>>(P, cur));
-    SMD_LAUNCH(h, (k_nbr_cells_plain<<<h->nbr_grid(), kNbrThreads, 0, st>>>(P, cur)));
+    SMD_PDL(h, k_reorder<false>, gb, kBeadBlock, st, P, cur);
+    SMD_PDL(h, k_nbr_cells_plain, h->nbr_grid(), kNbrThreads, st, P, cur);
   }
   return 0;
 }
@@ -260,11 +287,11 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
     } else {
       SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
     }
-    SMD_LAUNCH(h, (k_integ<true, FL><<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur, se)));
+    SMD_PDL(h, k_integ<true, FL>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
     if (h->n_sph) SMD_LAUNCH(h, (k_sphere<true, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   } else {
     SMD_LAUNCH(h, (k_force<false, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
-    SMD_LAUNCH(h, (k_integ<false, FL><<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur, se)));
+    SMD_PDL(h, k_integ<false, FL>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
     if (h->n_sph) SMD_LAUNCH(h, (k_sphere<false, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   }
   if (kLoopStep && h->profile) {

@@ -183,6 +183,15 @@ struct DevPtrs {
 };
 
 // ------------------------------------------------------------------ helpers
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start while the kernel before it drains: it calls
+// pdl_wait() before reading anything that kernel wrote (the wait returns once
+// that grid has completed and its writes are visible).  The kernel before it
+// calls pdl_trigger() to let it launch early.  Both are no-ops in an ordinary
+// launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ int rep_of(const DevPtrs& P, int i) {
   // replicas are contiguous ranges; linear scan is fine for the few replicas
   // of a batch, binary search for many.

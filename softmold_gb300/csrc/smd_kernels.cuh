@@ -67,6 +67,7 @@ __device__ __forceinline__ float displacement(uint4 ref, unsigned int fx, unsign
 // Verlet-list cell of bead i from its 32-bit fractional coordinates: the
 // cell index along an axis is floor(f * n / 2^32), always in [0, n).
 __global__ void __launch_bounds__(kBeadBlock) k_bin(DevPtrs P, int cur, int mixed, int in_graph) {
+  pdl_trigger();
   if (!P.g->rebuild) return;
   const int i = blockIdx.x * kBeadBlock + threadIdx.x;
   if (in_graph && i == 0) P.g->graph_builds++;
@@ -158,6 +159,7 @@ __global__ void __launch_bounds__(kBlock) k_scan_sums(DevPtrs P, int n_tiles) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_scan_apply(DevPtrs P) {
+  pdl_trigger();
   if (!P.g->rebuild) return;
   const int base = blockIdx.x * kScanTile;
   int carry = P.block_sums[blockIdx.x];
@@ -188,6 +190,8 @@ __global__ void __launch_bounds__(kBlock) k_scan_apply(DevPtrs P) {
 constexpr int kScanOneThreads = 1024;
 constexpr int kScanOneMax = 32768;
 __global__ void __launch_bounds__(kScanOneThreads) k_scan_one(DevPtrs P) {
+  pdl_trigger();
+  pdl_wait();  // k_bin's counts
   if (!P.g->rebuild) return;
   __shared__ int wsum[kScanOneThreads / 32], osum[kScanOneThreads / 32];
   const int n = P.n_cells_total;
@@ -261,6 +265,8 @@ __global__ void __launch_bounds__(kScanOneThreads) k_scan_one(DevPtrs P) {
 
 template <bool MIXED>
 __global__ void __launch_bounds__(kBeadBlock) k_reorder(DevPtrs P, int cur) {
+  pdl_trigger();
+  pdl_wait();  // the scan's cell starts
   if (!P.g->rebuild) return;
   const int i = blockIdx.x * kBeadBlock + threadIdx.x;
   for (int c = i; c < P.n_cells_total; c += gridDim.x * kBeadBlock) P.cell_count[c] = 0;
@@ -519,6 +525,7 @@ __device__ __forceinline__ void nbr_cell_plain(const DevPtrs& P, int cur, int c)
 }
 
 __global__ void __launch_bounds__(kNbrThreads) k_nbr_cells_plain(DevPtrs P, int cur) {
+  pdl_wait();  // the reordered state
   if (!P.g->rebuild) return;
   list_build_begin(P);
   for (int r = 0, c = list_cell(P, 0); c >= 0; c = list_cell(P, ++r)) nbr_cell_plain(P, cur, c);
@@ -742,6 +749,7 @@ __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
 }
 
 __global__ void __launch_bounds__(kOctThreads) k_nbr_cells_oct(DevPtrs P, int cur) {
+  pdl_wait();  // the reordered state
   if (!P.g->rebuild) return;
   list_build_begin(P);
   for (int r = 0, c = list_cell(P, 0); c >= 0; c = list_cell(P, ++r)) nbr_cell_oct(P, cur, c);
@@ -928,6 +936,7 @@ __device__ __forceinline__ void nbr_cell_flat(const DevPtrs& P, int cur, int c) 
 
 template <int NT>
 __global__ void __launch_bounds__(NT, 768 / NT) k_nbr_cells_flat(DevPtrs P, int cur) {
+  pdl_wait();  // the reordered state
   if (!P.g->rebuild) return;
   list_build_begin(P);
   for (int r = 0, c = list_cell(P, 0); c >= 0; c = list_cell(P, ++r)) nbr_cell_flat<NT>(P, cur, c);
@@ -1297,6 +1306,7 @@ __device__ __forceinline__ Vec3<typename std::conditional<MIXED, float, double>:
 constexpr int kGather = 4;  // neighbour gathers in flight per lane (mixed pair pass)
 template <bool MIXED, int FL, int G>
 __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
+  pdl_trigger();
   using R = typename std::conditional<MIXED, float, double>::type;
   __shared__ R sF[6 * kMaxTypes * kMaxTypes];
   __shared__ R sU[6 * kMaxTypes * kMaxTypes];
@@ -1493,6 +1503,7 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
 // start-up, force-only and energy-only variants.
 template <bool MIXED, int FL>
 __global__ void __launch_bounds__(kBeadBlock) k_integ(DevPtrs P, int cur, StepEnd se) {
+  pdl_wait();  // the pair pass's forces
   const long long it = P.g->it;
   const Tables& T = *P.tab;
   const int i = blockIdx.x * kBeadBlock + threadIdx.x;
