@@ -1304,6 +1304,105 @@ __device__ __forceinline__ Vec3<typename std::conditional<MIXED, float, double>:
 // minimum image.  Writes the per-bead pair force (fixed point or FP64) and,
 // with F_DU / F_ENERGY, the replica's pair U(x)-U(s x) / pair energy.
 constexpr int kGather = 4;  // neighbour gathers in flight per lane (mixed pair pass)
+// Mixed-form pair sums of bead i over its Verlet list, lane `sub` of its G
+// lanes: each pair force rounded to fixed point and summed in int32 per lane
+// (flushed to int64 every 32 terms), with F_DU the size-change difference
+// (fixed point) and with F_ENERGY the pair energy.  sF, sU: the FP32 tables
+// in shared memory.
+template <int FL, int G>
+__device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int sub, const RepState& rs,
+                                           const float* sF, const float* sU, int nT, long long& qx, long long& qy,
+                                           long long& qz, long long& dq, float& eacc) {
+  const Tables& T = *P.tab;
+  const int nn = P.nnbr[i];
+  const int* nb = P.nbr + (size_t)i * P.kmax;
+  const uint4 me = P.m4[cur][i];
+  const int ti = me.w & 0xff;
+  const float s0 = rs.len_per_frac[0], s1 = rs.len_per_frac[1], s2 = rs.len_per_frac[2];
+  float sq0 = 0.f, sq1 = 0.f, sq2 = 0.f;
+  if constexpr ((FL & F_DU) != 0) {
+    sq0 = (float)(rs.scale[0] * rs.scale[0] - 1.0);
+    sq1 = (float)(rs.scale[1] * rs.scale[1] - 1.0);
+    sq2 = (float)(rs.scale[2] * rs.scale[2] - 1.0);
+  }
+  const float* rowF = sF + 6 * ti * nT;
+  const float* rowU = sU + 6 * ti * nT;
+  const float rc2 = T.rc2f, fs = T.fscale;
+  // pair forces: branch-free (out-of-range entries add an exact 0), summed
+  // per lane in int32 and flushed to int64 every 32 entries: one pair is
+  // below 2^26 in fixed point, so 32 of them cannot overflow
+  int ax = 0, ay = 0, az = 0;
+  auto pair_force_q = [&](float dx, float dy, float dz, float r2, int tj) {
+    const float* c = rowF + 6 * tj;
+    const float rinv = rsqrtf(r2), r = r2 * rinv;
+    const int ci = (r >= c[0]) ? 3 : 0;
+    const float m = c[ci] - r;
+    float mag = ((c[ci + 1] - c[ci + 2] * m) * m) * rinv * fs;
+    mag = (r2 < rc2) ? mag : 0.f;
+    ax += __float2int_rn(dx * mag);
+    ay += __float2int_rn(dy * mag);
+    az += __float2int_rn(dz * mag);
+  };
+  int k = sub;
+  int rounds = 0;
+  // kGather independent gathers in flight per lane
+  for (; k + (kGather - 1) * G < nn; k += kGather * G) {
+    uint4 og[kGather];
+#pragma unroll
+    for (int u = 0; u < kGather; ++u) og[u] = P.m4[cur][__ldg(nb + k + u * G)];
+#pragma unroll
+    for (int u = 0; u < kGather; ++u) {
+      const uint4 o = og[u];
+      const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if constexpr ((FL & F_DU) != 0) {
+        const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
+        const float rn2 = r2 + q;
+        if (r2 < rc2 || rn2 < rc2) {
+          const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
+          dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
+                        4294967296.0f);
+        }
+      }
+      if constexpr ((FL & F_ENERGY) == 0) {
+        pair_force_q(dx, dy, dz, r2, o.w & 0xff);
+      } else {
+        if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
+      }
+    }
+    if (++rounds == 32 / kGather) {  // at most 32 pair terms per int32 sum
+      qx += ax;
+      qy += ay;
+      qz += az;
+      ax = ay = az = 0;
+      rounds = 0;
+    }
+  }
+  for (; k < nn; k += G) {
+    const int j = __ldg(nb + k);
+    const uint4 o = P.m4[cur][j];
+    const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if constexpr ((FL & F_DU) != 0) {
+      const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
+      const float rn2 = r2 + q;
+      if (r2 < rc2 || rn2 < rc2) {
+        const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
+        dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
+                      4294967296.0f);
+      }
+    }
+    if constexpr ((FL & F_ENERGY) == 0) {
+      pair_force_q(dx, dy, dz, r2, o.w & 0xff);
+    } else {
+      if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
+    }
+  }
+  qx += ax;
+  qy += ay;
+  qz += az;
+}
+
 template <bool MIXED, int FL, int G>
 __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
   pdl_trigger();
@@ -1334,92 +1433,8 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
     const int nn = P.nnbr[i];
     const int* nb = P.nbr + (size_t)i * P.kmax;
     if constexpr (MIXED) {
-      const uint4 me = P.m4[cur][i];
-      const int ti = me.w & 0xff;
-      const float s0 = rs.len_per_frac[0], s1 = rs.len_per_frac[1], s2 = rs.len_per_frac[2];
-      float sq0 = 0.f, sq1 = 0.f, sq2 = 0.f;
-      if constexpr ((FL & F_DU) != 0) {
-        sq0 = (float)(rs.scale[0] * rs.scale[0] - 1.0);
-        sq1 = (float)(rs.scale[1] * rs.scale[1] - 1.0);
-        sq2 = (float)(rs.scale[2] * rs.scale[2] - 1.0);
-      }
-      const float* rowF = sF + 6 * ti * nT;
-      const float* rowU = sU + 6 * ti * nT;
-      const float rc2 = T.rc2f, fs = T.fscale;
       float eacc = 0.f;
-      // pair forces: branch-free (out-of-range entries add an exact 0), summed
-      // per lane in int32 and flushed to int64 every 32 entries: one pair is
-      // below 2^26 in fixed point, so 32 of them cannot overflow
-      int ax = 0, ay = 0, az = 0;
-      auto pair_force_q = [&](float dx, float dy, float dz, float r2, int tj) {
-        const float* c = rowF + 6 * tj;
-        const float rinv = rsqrtf(r2), r = r2 * rinv;
-        const int ci = (r >= c[0]) ? 3 : 0;
-        const float m = c[ci] - r;
-        float mag = ((c[ci + 1] - c[ci + 2] * m) * m) * rinv * fs;
-        mag = (r2 < rc2) ? mag : 0.f;
-        ax += __float2int_rn(dx * mag);
-        ay += __float2int_rn(dy * mag);
-        az += __float2int_rn(dz * mag);
-      };
-      int k = sub;
-      int rounds = 0;
-      // kGather independent gathers in flight per lane
-      for (; k + (kGather - 1) * G < nn; k += kGather * G) {
-        uint4 og[kGather];
-#pragma unroll
-        for (int u = 0; u < kGather; ++u) og[u] = P.m4[cur][__ldg(nb + k + u * G)];
-#pragma unroll
-        for (int u = 0; u < kGather; ++u) {
-          const uint4 o = og[u];
-          const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          if constexpr ((FL & F_DU) != 0) {
-            const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
-            const float rn2 = r2 + q;
-            if (r2 < rc2 || rn2 < rc2) {
-              const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
-              dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
-                            4294967296.0f);
-            }
-          }
-          if constexpr ((FL & F_ENERGY) == 0) {
-            pair_force_q(dx, dy, dz, r2, o.w & 0xff);
-          } else {
-            if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
-          }
-        }
-        if (++rounds == 32 / kGather) {  // at most 32 pair terms per int32 sum
-          qx += ax;
-          qy += ay;
-          qz += az;
-          ax = ay = az = 0;
-          rounds = 0;
-        }
-      }
-      for (; k < nn; k += G) {
-        const int j = __ldg(nb + k);
-        const uint4 o = P.m4[cur][j];
-        const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if constexpr ((FL & F_DU) != 0) {
-          const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
-          const float rn2 = r2 + q;
-          if (r2 < rc2 || rn2 < rc2) {
-            const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
-            dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
-                          4294967296.0f);
-          }
-        }
-        if constexpr ((FL & F_ENERGY) == 0) {
-          pair_force_q(dx, dy, dz, r2, o.w & 0xff);
-        } else {
-          if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
-        }
-      }
-      qx += ax;
-      qy += ay;
-      qz += az;
+      pair_sum_q<FL, G>(P, cur, i, sub, rs, sF, sU, nT, qx, qy, qz, dq, eacc);
       ep = 0.5 * (double)eacc;
     } else {
       const double4 me = P.d4[cur][i];
@@ -1501,11 +1516,235 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
 // this step, first half-kick and drift of the next, periodic wrap, and the
 // position mirror for the next force pass.  Flags select the stopped,
 // start-up, force-only and energy-only variants.
+// One bead's part of the per-bead pass: bonded terms, the total force, the
+// Langevin term and the velocity-Verlet updates, the next mirror and the
+// displacement from the list build.  q is the bead's pair force in fixed
+// point (mixed form; the plain form reads P.fp), fs its sphere force; the
+// energy and size-change sums and the displacement accumulate into the
+// caller's variables.
+template <bool MIXED, int FL>
+__device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int r, long long it, const long long q[3],
+                                           const Vec3<double>& fs, double& dU_bond, double& e_bond, double& e_kin,
+                                           float& vmax) {
+  const Tables& T = *P.tab;
+  const RepParams& rp = P.rp[r];
+  const RepState& rs = P.rs[r];
+  const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
+  int ti;
+  if constexpr (MIXED) ti = P.m4[cur][i].w & 0xff; else ti = __double_as_longlong(P.d4[cur][i].w) & 0xff;
+  // ---- CHAIN terms (FP32 in the mixed form, from exact FP64 differences)
+  using R = typename std::conditional<MIXED, float, double>::type;
+  Vec3<R> fb{0, 0, 0};
+  const int ci = P.cinfo[i];
+  const bool sphere = (ci < 0) && (ci & 0x40000000);  // integrated by k_sphere
+  // bonded forces: one function for every step variant, so stopped and
+  // running steps round them alike
+  if constexpr ((FL & (F_PAIRONLY | F_ENERGY)) == 0) fb = bonded_force<MIXED>(P, cur, i, ci, box, rs);
+  if ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0 && ci < 0 && !(ci & 0x40000000)) {
+    const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
+    // the chain's difference vectors in R (exact from the fractional
+    // mirror in the mixed form)
+    Vec3<R> er[4];
+    bool valid[4];
+    chain_vectors<MIXED, R>(P, cur, i, p, len, box, er, valid);
+    // terms owned by the first bead of each bond / bend: energies in FP64;
+    // size-change differences in FP64 (plain) or factored FP32 (mixed)
+    if constexpr (MIXED && (FL & F_DU) != 0) {
+      const float* cf = T.chainF[set];
+      const float sq[3] = {(float)(rs.scale[0] * rs.scale[0] - 1.0), (float)(rs.scale[1] * rs.scale[1] - 1.0),
+                           (float)(rs.scale[2] * rs.scale[2] - 1.0)};
+      float du = 0.f;
+      if (valid[2]) du += bond_dpot_f(er[2], sq, cf);
+      if (valid[2] && valid[3]) du += bend_dpot_f(er[2], er[3], sq, cf + 2);
+      dU_bond += (double)du;
+    }
+    if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
+      Vec3<double> e[4];
+      if constexpr (MIXED) {
+        chain_vectors<MIXED, double>(P, cur, i, p, len, box, e, valid);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) e[k] = Vec3<double>{er[k].x, er[k].y, er[k].z};
+      }
+      const double* cd = T.chainD[set];
+      if constexpr ((FL & F_ENERGY) != 0) {
+        if (valid[2]) e_bond += bond_pot(e[2], cd);
+        if (valid[2] && valid[3]) e_bond += bend_pot(e[2], e[3], cd + 2);
+      }
+      if constexpr (!MIXED && (FL & F_DU) != 0) {
+        const Vec3<double> s2{e[2].x * rs.scale[0], e[2].y * rs.scale[1], e[2].z * rs.scale[2]};
+        const Vec3<double> s3{e[3].x * rs.scale[0], e[3].y * rs.scale[1], e[3].z * rs.scale[2]};
+        if (valid[2]) dU_bond += bond_pot(e[2], cd) - bond_pot(s2, cd);
+        if (valid[2] && valid[3]) dU_bond += bend_pot(e[2], e[3], cd + 2) - bend_pot(s2, s3, cd + 2);
+      }
+    }
+  }
+  // ---- BOND / BEND residue terms of this bead: energies and differences
+  // (their forces are in bonded_force)
+  if constexpr ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0) {
+    if (P.n_terms > 0) {
+      const int o = P.orig[i];
+      const int e1 = P.term_off[o + 1];
+      const float sq_f[3] = {(float)(rs.scale[0] * rs.scale[0] - 1.0), (float)(rs.scale[1] * rs.scale[1] - 1.0),
+                             (float)(rs.scale[2] * rs.scale[2] - 1.0)};
+      for (int e = P.term_off[o]; e < e1; ++e) {
+        const int4 t = P.terms[e];
+        const int role = (t.x >> 1) & 3, set = t.x >> 3;
+        const double* cd = T.termD[set];
+        if ((t.x & 1) == 0) {  // bond (first, second): the bead's force is mag (x_self - x_other)
+          if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
+            if (role == 0) {  // energy terms owned by the first bead
+              if constexpr (MIXED && (FL & F_DU) != 0)
+                dU_bond += (double)bond_dpot_f(term_vec<MIXED, float>(P, cur, t.y, t.z, box, rs), sq_f,
+                                               T.termF[set]);
+              if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
+                const Vec3<double> d = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
+                if constexpr ((FL & F_ENERGY) != 0) e_bond += bond_pot(d, cd);
+                if constexpr (!MIXED && (FL & F_DU) != 0) {
+                  const Vec3<double> sd{d.x * rs.scale[0], d.y * rs.scale[1], d.z * rs.scale[2]};
+                  dU_bond += bond_pot(d, cd) - bond_pot(sd, cd);
+                }
+              }
+            }
+          }
+        } else {  // bend (first, second, third): da = x1 - x2, db = x2 - x3
+          if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
+            if (role == 0) {
+              if constexpr (MIXED && (FL & F_DU) != 0)
+                dU_bond += (double)bend_dpot_f(term_vec<MIXED, float>(P, cur, t.y, t.z, box, rs),
+                                               term_vec<MIXED, float>(P, cur, t.z, t.w, box, rs), sq_f,
+                                               T.termF[set]);
+              if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
+                const Vec3<double> da = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
+                const Vec3<double> db = term_vec<MIXED, double>(P, cur, t.z, t.w, box, rs);
+                if constexpr ((FL & F_ENERGY) != 0) e_bond += bend_pot(da, db, cd);
+                if constexpr (!MIXED && (FL & F_DU) != 0) {
+                  const Vec3<double> sa{da.x * rs.scale[0], da.y * rs.scale[1], da.z * rs.scale[2]};
+                  const Vec3<double> sb{db.x * rs.scale[0], db.y * rs.scale[1], db.z * rs.scale[2]};
+                  dU_bond += bend_pot(da, db, cd) - bend_pot(sa, sb, cd);
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  if constexpr ((FL & F_ENERGY) != 0) {
+    const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
+    e_kin = (vx * vx + vy * vy + vz * vz) / 2.0;
+  } else {
+    double F[3];
+    if constexpr (MIXED) {
+      F[0] = (double)q[0] * T.inv_fscale + (double)fb.x;
+      F[1] = (double)q[1] * T.inv_fscale + (double)fb.y;
+      F[2] = (double)q[2] * T.inv_fscale + (double)fb.z;
+    } else {
+      F[0] = P.fp[i] + fb.x;
+      F[1] = P.fp[i + P.n] + fb.y;
+      F[2] = P.fp[i + 2 * P.n] + fb.z;
+    }
+    if (P.n_sph > 0) {
+      F[0] += fs.x;
+      F[1] += fs.y;
+      F[2] += fs.z;
+    }
+    if constexpr ((FL & F_FORCES) != 0) {
+      if (!sphere) {
+        const int o = P.orig[i];
+        P.force_out[3 * o] = F[0];
+        P.force_out[3 * o + 1] = F[1];
+        P.force_out[3 * o + 2] = F[2];
+      }
+    } else if (!sphere) {
+      const int o = P.orig[i];
+      double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+      double a[3];
+      if constexpr (MIXED && (FL & F_EXTNOISE) == 0) {
+        // CHAIN force and noise summed in FP32 (both force terms of the
+        // mixed form), the pair force exact from its fixed-point sum:
+        // a = -gamma v + (q 2^-k + (f_chain + sigma psi))
+        float nf[3];
+        langevin_noise_f(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31f, nf);
+        double e[3] = {(double)(fb.x + nf[0]), (double)(fb.y + nf[1]), (double)(fb.z + nf[2])};
+        if (P.n_sph > 0) {
+          e[0] += fs.x;
+          e[1] += fs.y;
+          e[2] += fs.z;
+        }
+        for (int d = 0; d < 3; ++d)
+          a[d] = fma(-rp.gamma, v[d], fma((double)q[d], T.inv_fscale, e[d]));
+      } else {
+        double noise[3];  // sigma * psi
+        if constexpr ((FL & F_EXTNOISE) != 0) {
+          for (int d = 0; d < 3; ++d) noise[d] = rp.sigma * P.ext_noise[3 * o + d];
+        } else {
+          langevin_noise(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
+        }
+        for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
+      }
+      if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
+        P.ax[i] = a[0];
+        P.ay[i] = a[1];
+        P.az[i] = a[2];
+        if constexpr ((FL & F_STOP) != 0) {
+          if (ti != 0) {
+            const double h = rp.dt * 0.5;
+            P.vx[i] = fma(a[0], h, v[0]);
+            P.vy[i] = fma(a[1], h, v[1]);
+            P.vz[i] = fma(a[2], h, v[2]);
+          }
+        }
+      } else {
+        double x[3] = {P.x[i], P.y[i], P.z[i]};
+        if (ti != 0) {
+          if constexpr (MIXED) {
+            // second() of this step and first() of the next, rounded as the
+            // stopped step and k_finish round them, so that a replica's
+            // trajectory does not depend on where other replicas stop
+            const double h = rp.dt * 0.5;
+            for (int d = 0; d < 3; ++d) {
+              v[d] = fma(a[d], h, fma(a[d], h, v[d]));
+              x[d] = fma(v[d], rp.dt, x[d]);
+              if (x[d] > box[d]) x[d] -= box[d];
+              if (x[d] < 0) x[d] += box[d];
+            }
+          } else {
+            const double h = rp.dt * 0.5;
+            for (int d = 0; d < 3; ++d) {
+              v[d] += (a[d] * h);  // second() of this step
+              v[d] += (a[d] * h);  // first() of the next step
+              x[d] += v[d] * rp.dt;
+              if (x[d] > box[d]) x[d] -= box[d];
+              if (x[d] < 0) x[d] += box[d];
+            }
+          }
+          P.vx[i] = v[0];
+          P.vy[i] = v[1];
+          P.vz[i] = v[2];
+          P.x[i] = x[0];
+          P.y[i] = x[1];
+          P.z[i] = x[2];
+        }
+        const unsigned int fx = to_frac(x[0], rs.frac_per_len[0]), fy = to_frac(x[1], rs.frac_per_len[1]),
+                           fz = to_frac(x[2], rs.frac_per_len[2]);
+        vmax = displacement(P.ref[i], fx, fy, fz, rs);
+        if constexpr (MIXED) {
+          const uint4 me = P.m4[cur][i];
+          P.m4[cur ^ 1][i] = make_uint4(fx, fy, fz, me.w);
+        } else {
+          const double4 me = P.d4[cur][i];
+          P.d4[cur ^ 1][i] = make_double4(x[0], x[1], x[2], me.w);
+        }
+      }
+    }
+  }
+}
+
 template <bool MIXED, int FL>
 __global__ void __launch_bounds__(kBeadBlock) k_integ(DevPtrs P, int cur, StepEnd se) {
   pdl_wait();  // the pair pass's forces
   const long long it = P.g->it;
-  const Tables& T = *P.tab;
   const int i = blockIdx.x * kBeadBlock + threadIdx.x;
   const bool active = i < P.n;
   const int r = active ? rep_of(P, i) : 0;
@@ -1519,218 +1758,13 @@ __global__ void __launch_bounds__(kBeadBlock) k_integ(DevPtrs P, int cur, StepEn
   }
   dU_bond += du_sph;
   if (active) {
-    const RepParams& rp = P.rp[r];
-    const RepState& rs = P.rs[r];
-    const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
-    int ti;
-    if constexpr (MIXED) ti = P.m4[cur][i].w & 0xff; else ti = __double_as_longlong(P.d4[cur][i].w) & 0xff;
-    // ---- CHAIN terms (FP32 in the mixed form, from exact FP64 differences)
-    using R = typename std::conditional<MIXED, float, double>::type;
-    Vec3<R> fb{0, 0, 0};
-    const int ci = P.cinfo[i];
-    const bool sphere = (ci < 0) && (ci & 0x40000000);  // integrated by k_sphere
-    // bonded forces: one function for every step variant, so stopped and
-    // running steps round them alike
-    if constexpr ((FL & (F_PAIRONLY | F_ENERGY)) == 0) fb = bonded_force<MIXED>(P, cur, i, ci, box, rs);
-    if ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0 && ci < 0 && !(ci & 0x40000000)) {
-      const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
-      // the chain's difference vectors in R (exact from the fractional
-      // mirror in the mixed form)
-      Vec3<R> er[4];
-      bool valid[4];
-      chain_vectors<MIXED, R>(P, cur, i, p, len, box, er, valid);
-      // terms owned by the first bead of each bond / bend: energies in FP64;
-      // size-change differences in FP64 (plain) or factored FP32 (mixed)
-      if constexpr (MIXED && (FL & F_DU) != 0) {
-        const float* cf = T.chainF[set];
-        const float sq[3] = {(float)(rs.scale[0] * rs.scale[0] - 1.0), (float)(rs.scale[1] * rs.scale[1] - 1.0),
-                             (float)(rs.scale[2] * rs.scale[2] - 1.0)};
-        float du = 0.f;
-        if (valid[2]) du += bond_dpot_f(er[2], sq, cf);
-        if (valid[2] && valid[3]) du += bend_dpot_f(er[2], er[3], sq, cf + 2);
-        dU_bond += (double)du;
-      }
-      if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
-        Vec3<double> e[4];
-        if constexpr (MIXED) {
-          chain_vectors<MIXED, double>(P, cur, i, p, len, box, e, valid);
-        } else {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) e[k] = Vec3<double>{er[k].x, er[k].y, er[k].z};
-        }
-        const double* cd = T.chainD[set];
-        if constexpr ((FL & F_ENERGY) != 0) {
-          if (valid[2]) e_bond += bond_pot(e[2], cd);
-          if (valid[2] && valid[3]) e_bond += bend_pot(e[2], e[3], cd + 2);
-        }
-        if constexpr (!MIXED && (FL & F_DU) != 0) {
-          const Vec3<double> s2{e[2].x * rs.scale[0], e[2].y * rs.scale[1], e[2].z * rs.scale[2]};
-          const Vec3<double> s3{e[3].x * rs.scale[0], e[3].y * rs.scale[1], e[3].z * rs.scale[2]};
-          if (valid[2]) dU_bond += bond_pot(e[2], cd) - bond_pot(s2, cd);
-          if (valid[2] && valid[3]) dU_bond += bend_pot(e[2], e[3], cd + 2) - bend_pot(s2, s3, cd + 2);
-        }
-      }
+    long long q[3] = {0, 0, 0};
+    if constexpr (MIXED && (FL & F_ENERGY) == 0) {
+      q[0] = P.fq[i];
+      q[1] = P.fq[i + P.n];
+      q[2] = P.fq[i + 2 * P.n];
     }
-    // ---- BOND / BEND residue terms of this bead: energies and differences
-    // (their forces are in bonded_force)
-    if constexpr ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0) {
-      if (P.n_terms > 0) {
-        const int o = P.orig[i];
-        const int e1 = P.term_off[o + 1];
-        const float sq_f[3] = {(float)(rs.scale[0] * rs.scale[0] - 1.0), (float)(rs.scale[1] * rs.scale[1] - 1.0),
-                               (float)(rs.scale[2] * rs.scale[2] - 1.0)};
-        for (int e = P.term_off[o]; e < e1; ++e) {
-          const int4 t = P.terms[e];
-          const int role = (t.x >> 1) & 3, set = t.x >> 3;
-          const double* cd = T.termD[set];
-          if ((t.x & 1) == 0) {  // bond (first, second): the bead's force is mag (x_self - x_other)
-            if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
-              if (role == 0) {  // energy terms owned by the first bead
-                if constexpr (MIXED && (FL & F_DU) != 0)
-                  dU_bond += (double)bond_dpot_f(term_vec<MIXED, float>(P, cur, t.y, t.z, box, rs), sq_f,
-                                                 T.termF[set]);
-                if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
-                  const Vec3<double> d = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
-                  if constexpr ((FL & F_ENERGY) != 0) e_bond += bond_pot(d, cd);
-                  if constexpr (!MIXED && (FL & F_DU) != 0) {
-                    const Vec3<double> sd{d.x * rs.scale[0], d.y * rs.scale[1], d.z * rs.scale[2]};
-                    dU_bond += bond_pot(d, cd) - bond_pot(sd, cd);
-                  }
-                }
-              }
-            }
-          } else {  // bend (first, second, third): da = x1 - x2, db = x2 - x3
-            if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
-              if (role == 0) {
-                if constexpr (MIXED && (FL & F_DU) != 0)
-                  dU_bond += (double)bend_dpot_f(term_vec<MIXED, float>(P, cur, t.y, t.z, box, rs),
-                                                 term_vec<MIXED, float>(P, cur, t.z, t.w, box, rs), sq_f,
-                                                 T.termF[set]);
-                if constexpr ((FL & F_ENERGY) != 0 || (!MIXED && (FL & F_DU) != 0)) {
-                  const Vec3<double> da = term_vec<MIXED, double>(P, cur, t.y, t.z, box, rs);
-                  const Vec3<double> db = term_vec<MIXED, double>(P, cur, t.z, t.w, box, rs);
-                  if constexpr ((FL & F_ENERGY) != 0) e_bond += bend_pot(da, db, cd);
-                  if constexpr (!MIXED && (FL & F_DU) != 0) {
-                    const Vec3<double> sa{da.x * rs.scale[0], da.y * rs.scale[1], da.z * rs.scale[2]};
-                    const Vec3<double> sb{db.x * rs.scale[0], db.y * rs.scale[1], db.z * rs.scale[2]};
-                    dU_bond += bend_pot(da, db, cd) - bend_pot(sa, sb, cd);
-                  }
-                }
-              }
-            }
-          }
-        }
-      }
-    }
-    if constexpr ((FL & F_ENERGY) != 0) {
-      const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
-      e_kin = (vx * vx + vy * vy + vz * vz) / 2.0;
-    } else {
-      double F[3];
-      if constexpr (MIXED) {
-        F[0] = (double)P.fq[i] * T.inv_fscale + (double)fb.x;
-        F[1] = (double)P.fq[i + P.n] * T.inv_fscale + (double)fb.y;
-        F[2] = (double)P.fq[i + 2 * P.n] * T.inv_fscale + (double)fb.z;
-      } else {
-        F[0] = P.fp[i] + fb.x;
-        F[1] = P.fp[i + P.n] + fb.y;
-        F[2] = P.fp[i + 2 * P.n] + fb.z;
-      }
-      if (P.n_sph > 0) {
-        F[0] += fs.x;
-        F[1] += fs.y;
-        F[2] += fs.z;
-      }
-      if constexpr ((FL & F_FORCES) != 0) {
-        if (!sphere) {
-          const int o = P.orig[i];
-          P.force_out[3 * o] = F[0];
-          P.force_out[3 * o + 1] = F[1];
-          P.force_out[3 * o + 2] = F[2];
-        }
-      } else if (!sphere) {
-        const int o = P.orig[i];
-        double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
-        double a[3];
-        if constexpr (MIXED && (FL & F_EXTNOISE) == 0) {
-          // CHAIN force and noise summed in FP32 (both force terms of the
-          // mixed form), the pair force exact from its fixed-point sum:
-          // a = -gamma v + (q 2^-k + (f_chain + sigma psi))
-          float nf[3];
-          langevin_noise_f(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31f, nf);
-          double e[3] = {(double)(fb.x + nf[0]), (double)(fb.y + nf[1]), (double)(fb.z + nf[2])};
-          if (P.n_sph > 0) {
-            e[0] += fs.x;
-            e[1] += fs.y;
-            e[2] += fs.z;
-          }
-          for (int d = 0; d < 3; ++d)
-            a[d] = fma(-rp.gamma, v[d], fma((double)P.fq[i + d * P.n], T.inv_fscale, e[d]));
-        } else {
-          double noise[3];  // sigma * psi
-          if constexpr ((FL & F_EXTNOISE) != 0) {
-            for (int d = 0; d < 3; ++d) noise[d] = rp.sigma * P.ext_noise[3 * o + d];
-          } else {
-            langevin_noise(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
-          }
-          for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
-        }
-        if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
-          P.ax[i] = a[0];
-          P.ay[i] = a[1];
-          P.az[i] = a[2];
-          if constexpr ((FL & F_STOP) != 0) {
-            if (ti != 0) {
-              const double h = rp.dt * 0.5;
-              P.vx[i] = fma(a[0], h, v[0]);
-              P.vy[i] = fma(a[1], h, v[1]);
-              P.vz[i] = fma(a[2], h, v[2]);
-            }
-          }
-        } else {
-          double x[3] = {P.x[i], P.y[i], P.z[i]};
-          if (ti != 0) {
-            if constexpr (MIXED) {
-              // second() of this step and first() of the next, rounded as the
-              // stopped step and k_finish round them, so that a replica's
-              // trajectory does not depend on where other replicas stop
-              const double h = rp.dt * 0.5;
-              for (int d = 0; d < 3; ++d) {
-                v[d] = fma(a[d], h, fma(a[d], h, v[d]));
-                x[d] = fma(v[d], rp.dt, x[d]);
-                if (x[d] > box[d]) x[d] -= box[d];
-                if (x[d] < 0) x[d] += box[d];
-              }
-            } else {
-              const double h = rp.dt * 0.5;
-              for (int d = 0; d < 3; ++d) {
-                v[d] += (a[d] * h);  // second() of this step
-                v[d] += (a[d] * h);  // first() of the next step
-                x[d] += v[d] * rp.dt;
-                if (x[d] > box[d]) x[d] -= box[d];
-                if (x[d] < 0) x[d] += box[d];
-              }
-            }
-            P.vx[i] = v[0];
-            P.vy[i] = v[1];
-            P.vz[i] = v[2];
-            P.x[i] = x[0];
-            P.y[i] = x[1];
-            P.z[i] = x[2];
-          }
-          const unsigned int fx = to_frac(x[0], rs.frac_per_len[0]), fy = to_frac(x[1], rs.frac_per_len[1]),
-                             fz = to_frac(x[2], rs.frac_per_len[2]);
-          vmax = displacement(P.ref[i], fx, fy, fz, rs);
-          if constexpr (MIXED) {
-            const uint4 me = P.m4[cur][i];
-            P.m4[cur ^ 1][i] = make_uint4(fx, fy, fz, me.w);
-          } else {
-            const double4 me = P.d4[cur][i];
-            P.d4[cur ^ 1][i] = make_double4(x[0], x[1], x[2], me.w);
-          }
-        }
-      }
-    }
+    integ_bead<MIXED, FL>(P, cur, i, r, it, q, fs, dU_bond, e_bond, e_kin, vmax);
   }
   if constexpr ((FL & F_DU) != 0) {
     if constexpr (MIXED) warp_atomic_add_q(__double2ll_rn(dU_bond * 4294967296.0), &P.rs[r].dUq_bond, r);
