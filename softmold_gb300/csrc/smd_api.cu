@@ -135,10 +135,15 @@ struct smd_system {
   int bead_grid() const { return (n + kBeadBlock - 1) / kBeadBlock; }
   int grid_lanes(int g = kLanes) const { return (int)(((long long)n * g + kBlock - 1) / kBlock); }
   int sms = 152;
-  // list build: CTA b builds occupied cell b; beyond 32 CTAs per SM the rest
-  // come from a device work queue (sparse boxes have far more cells than
-  // occupied ones, and an idle CTA per empty cell costs launch time)
-  int nbr_grid() const { return std::min(n_cells, sms * 32); }
+  // list build: CTA b builds occupied cell b, and cells beyond the grid come
+  // from a device work queue.  The grid follows the occupied-cell count of
+  // the last build read back (+25 %): sparse boxes have far more cells than
+  // occupied ones, and every idle CTA costs launch time.
+  int occ_est = 0;
+  int nbr_grid() const {
+    const int want = occ_est > 0 ? occ_est + occ_est / 4 + 64 : sms * 32;
+    return std::max(1, std::min(n_cells, want));
+  }
 };
 
 namespace {
@@ -423,6 +428,7 @@ int read_error(smd_system* h) {
   SMD_CUDA(cudaMemcpyAsync(&g, h->P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
   h->graph_builds = g.graph_builds;
+  if (g.n_occ > 0) h->occ_est = g.n_occ;
   if (g.error & 2) return fail(8, "a Verlet-list cell holds more than 1024 beads (collapsed system)");
   if (g.error & 1) {
     char buf[256];

@@ -244,13 +244,20 @@ __global__ void __launch_bounds__(kScanOneThreads) k_scan_one(DevPtrs P) {
     __syncthreads();
     int ex = carry + (w > 0 ? wsum[w - 1] : 0) + x - s;
     int eo = ocarry + (w > 0 ? osum[w - 1] : 0) + xo - f;
+    int st[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      if (c0 + k < n) {
-        P.cell_start[c0 + k] = ex;
-        if (v[k] > 0) P.occ[eo++] = c0 + k;
-      }
+      st[k] = ex;
       ex += v[k];
+      if (c0 + k < n && v[k] > 0) P.occ[eo++] = c0 + k;
+    }
+    if (c0 + 8 <= n) {  // two 16-byte stores
+      *reinterpret_cast<int4*>(P.cell_start + c0) = make_int4(st[0], st[1], st[2], st[3]);
+      *reinterpret_cast<int4*>(P.cell_start + c0 + 4) = make_int4(st[4], st[5], st[6], st[7]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (c0 + k < n) P.cell_start[c0 + k] = st[k];
     }
     carry += wsum[kScanOneThreads / 32 - 1];
     ocarry += osum[kScanOneThreads / 32 - 1];
@@ -592,6 +599,67 @@ __device__ __forceinline__ void stencil_rows(const DevPtrs& P, const CellCtx& q,
   }
 }
 
+// The same row segments formed by one warp: lane l < 18 takes half-row l
+// (row t = l / 2; the second half is empty unless the row wraps in x), and
+// the non-empty halves are compacted in lane order with their stencil-slot
+// prefix sums (ballot and shuffles), the count going to seg_len[0].
+__device__ __forceinline__ void stencil_warp(const DevPtrs& P, const CellCtx& q, int* seg_s, int* seg_p,
+                                             int* seg_len) {
+  const int lane = threadIdx.x & 31;
+  int start = 0, len = 0;
+  if (lane < 18) {
+    const int t = lane >> 1, half = lane & 1;
+    const int oy = t % 3 - 1, oz = t / 3 - 1;
+    const int lo1 = q.n1 >= 3 ? -1 : 0, hi1 = q.n1 >= 2 ? 1 : 0;
+    const int lo2 = q.n2 >= 3 ? -1 : 0, hi2 = q.n2 >= 2 ? 1 : 0;
+    if (oy >= lo1 && oy <= hi1 && oz >= lo2 && oz <= hi2) {
+      int xa = q.cx - 1, xb = q.cx + 1;
+      if (q.n0 < 3) {
+        xa = 0;
+        xb = q.n0 - 1;
+      }
+      const int zz = (q.cz + oz + q.n2) % q.n2, yy = (q.cy + oy + q.n1) % q.n1;
+      const int row = q.cb + q.n0 * (yy + q.n1 * zz);
+      int a0, a1, b0 = 0, b1 = 0;
+      if (xa >= 0 && xb < q.n0) {
+        a0 = row + xa;
+        a1 = row + xb + 1;
+      } else if (xa < 0) {
+        a0 = row + q.n0 - 1;
+        a1 = row + q.n0;
+        b0 = row;
+        b1 = row + xb + 1;
+      } else {
+        a0 = row + xa;
+        a1 = row + q.n0;
+        b0 = row;
+        b1 = row + 1;
+      }
+      const int u0 = half ? b0 : a0, u1 = half ? b1 : a1;
+      if (u1 > u0) {
+        start = P.cell_start[u0];
+        len = P.cell_start[u1] - start;
+      }
+    }
+  }
+  const unsigned int full = __ballot_sync(0xffffffffu, len > 0);
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (len > 0) {
+    const int k = __popc(full & ((1u << lane) - 1u));
+    seg_s[k] = start;
+    seg_p[k] = incl - len;
+  }
+  if (lane == 31) {
+    seg_p[__popc(full)] = incl;
+    seg_len[0] = __popc(full);
+  }
+}
+
 __device__ __forceinline__ void nbr_cell_oct(const DevPtrs& P, int cur, int c) {
   const int s0 = P.cell_start[c], e0 = P.cell_start[c + 1];
   if (s0 >= e0) return;
@@ -835,47 +903,26 @@ template <int NT>
 __device__ __forceinline__ void nbr_cell_flat(const DevPtrs& P, int cur, int c) {
   const int s0 = P.cell_start[c], e0 = P.cell_start[c + 1];
   if (s0 >= e0) return;
-  __shared__ CellCtx qs;
-  __shared__ unsigned int cr_s[3];
   __shared__ int seg_s[18], seg_len[18], seg_p[19];
   __shared__ int cnt[kNbrMaxCell];
   __shared__ float4 stage[kFlatChunk];
-  __syncthreads();  // the previous cell of this CTA is done with the shared arrays
-  if (threadIdx.x == 0) {
-    const CellCtx q0 = cell_ctx(P, c, s0, e0);
-    qs = q0;
-    cr_s[0] = cell_centre_frac(q0.cx, q0.n0);
-    cr_s[1] = cell_centre_frac(q0.cy, q0.n1);
-    cr_s[2] = cell_centre_frac(q0.cz, q0.n2);
-  }
-  __syncthreads();
-  const CellCtx q = qs;
+  // every thread derives the cell's context itself (the same few loads)
+  const CellCtx q = cell_ctx(P, c, s0, e0);
   const RepState& rs = P.rs[q.r];
   const int nb = q.e - q.s;
   if (nb > kNbrMaxCell) {
     if (threadIdx.x == 0) atomicOr(&P.g->error, 2);
     return;
   }
+  const unsigned int crx = cell_centre_frac(q.cx, q.n0), cry = cell_centre_frac(q.cy, q.n1),
+                     crz = cell_centre_frac(q.cz, q.n2);
+  __syncthreads();  // the previous cell of this CTA is done with the shared arrays
   copy_back<true, NT>(P, cur, q, rs);
-  stencil_rows(P, q, seg_s, seg_len);
+  if (threadIdx.x < 32) stencil_warp(P, q, seg_s, seg_p, seg_len);
   for (int b = threadIdx.x; b < nb; b += NT) cnt[b] = 0;
-  __syncthreads();
-  if (threadIdx.x == 0) {  // prefix sums over the 18 slots, empty ones dropped
-    int k = 0, acc = 0;
-    for (int t = 0; t < 18; ++t) {
-      if (seg_len[t] == 0) continue;
-      seg_s[k] = seg_s[t];
-      seg_p[k] = acc;
-      acc += seg_len[t];
-      ++k;
-    }
-    seg_p[k] = acc;
-    seg_len[0] = k;
-  }
   __syncthreads();
   const int nseg = seg_len[0];
   const int M = seg_p[nseg];
-  const unsigned int crx = cr_s[0], cry = cr_s[1], crz = cr_s[2];
   const float sx = rs.len_per_frac[0], sy = rs.len_per_frac[1], sz = rs.len_per_frac[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int kmax = P.kmax;
@@ -887,14 +934,33 @@ __device__ __forceinline__ void nbr_cell_flat(const DevPtrs& P, int cur, int c) 
     const int m = min(kFlatChunk, M - base);
     const int mpad = (m + 31) & ~31;
     if (base > 0) __syncthreads();  // every warp is done with the previous chunk
-    for (int t = 0; t < nseg; ++t) {
-      const int ps = seg_p[t];
-      const int lo = max(ps, base), hi = min(seg_p[t + 1], base + m);
-      for (int g = lo + threadIdx.x; g < hi; g += NT) {
-        const int j = seg_s[t] + (g - ps);
-        const uint4 mj = P.mt[j];
-        stage[g - base] = make_float4((float)(int)(mj.x - crx) * sx, (float)(int)(mj.y - cry) * sy,
-                                      (float)(int)(mj.z - crz) * sz, __int_as_float(j));
+    // stage the chunk: thread t takes slots base + t, + NT, ...; the bead of a
+    // slot comes from the segment table, and four loads are issued together
+    // (a small system has few cells per SM, so their latency is not hidden
+    // by other CTAs)
+    {
+      constexpr int kBatch = 4;
+      int t = 0;  // segment of this thread's next slot (slots only increase)
+      for (int k0 = threadIdx.x; k0 < m; k0 += kBatch * NT) {
+        int jj[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const int g = base + k0 + u * NT;
+          jj[u] = -1;
+          if (k0 + u * NT < m) {
+            while (seg_p[t + 1] <= g) ++t;
+            jj[u] = seg_s[t] + (g - seg_p[t]);
+          }
+        }
+        uint4 mj[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u)
+          if (jj[u] >= 0) mj[u] = P.mt[jj[u]];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u)
+          if (jj[u] >= 0)
+            stage[k0 + u * NT] = make_float4((float)(int)(mj[u].x - crx) * sx, (float)(int)(mj[u].y - cry) * sy,
+                                             (float)(int)(mj[u].z - crz) * sz, __int_as_float(jj[u]));
       }
     }
     // far sentinels complete the last round of 32 (index -1 matches no bead)
