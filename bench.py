@@ -221,6 +221,27 @@ def cpu_baseline(path, threads, target_s=12.0):
     return steps, t
 
 
+def melt_on_host(path, threads, steps):
+    """Runs the oracle's MD loop (the reference `MD` restated) on the host for
+    `steps` untimed steps from the workload's lattice start and leaves the
+    final state in the .mpd, so that the reference arm samples the same kind
+    of state as the GPU arm (which equilibrates on the device)."""
+    import re
+    import subprocess
+    d, base = os.path.split(path)
+    txt = open(path).read()
+    dt = float(re.search(r"^deltaT\s+(\S+)", txt, re.M).group(1))
+    t_end = repr(steps * dt)
+    for key in ("finalTime", "storeInterval", "measureInterval"):
+        txt = re.sub(rf"^{key}\s+\S+", f"{key} {t_end}", txt, flags=re.M)
+    open(path, "w").write(txt)
+    exe = os.path.join(ROOT, "oracle", "_build", "md_oracle")
+    r = subprocess.run([exe, base[:-4], str(threads)], cwd=d, capture_output=True, text=True,
+                       env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
+    if r.returncode != 0:
+        raise RuntimeError(f"the oracle could not run {path}: {r.stdout[-300:]} {r.stderr[-300:]}")
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference's CPU algorithm (the oracle port of
     MD.cpp, built here) on all host threads, same workload and metric."""
@@ -232,6 +253,12 @@ def run_reference(args, rank, world):
     with tempfile.TemporaryDirectory() as tmp:
         paths, ms, cfg = workload(args, 0, tmp)
         threads = os.cpu_count() or 1
+        # melt the lattice start on the host, as the GPU arm does on the device
+        # (up to 1,000 steps, at most 2.5e8 bead-steps for the whole workload)
+        n_all = sum(len(m.type) for m in ms)
+        melt = max(100, min(1000, int(2.5e8 / n_all)))
+        for p_ in paths:
+            melt_on_host(p_, threads, melt)
         import ctypes as C
         lib = C.CDLL(os.path.join(ROOT, "oracle", "_build", "libsmd_oracle.so"))
         lib.orc_md_time.argtypes = [C.c_char_p, C.c_int, C.c_int]
@@ -250,7 +277,7 @@ def run_reference(args, rank, world):
         value = units / total
         n = sum(len(m.type) for m in ms)
         what = f"the {n}-bead workload" if len(ms) == 1 else f"replicas of the {len(ms)}-replica batch in turn"
-        sample = f"{args.steps} samples of {per_step} MD steps of {what}"
+        sample = f"{args.steps} samples of {per_step} MD steps of {what}, after {melt} untimed steps from the lattice start"
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
