@@ -83,11 +83,11 @@ struct RepState {  // per replica, updated on the device
 };
 
 // Size-change energy of a replica's current trial.  The mixed form rounds
-// each pair term (twice counted) and each bead's bonded term to 2^-32 before
+// each pair term (once per pair) and each bead's bonded term to 2^-32 before
 // summing, so the total, and with it every Metropolis decision, is the same
 // whatever the pair order or the replicas sharing a launch.
 __host__ __device__ inline double rep_dU(const RepState& rs) {
-  const double q = 0.5 * (double)rs.dUq_pair + (double)rs.dUq_bond;
+  const double q = (double)rs.dUq_pair + (double)rs.dUq_bond;
   return rs.dU_pair + rs.dU_bond + q * (1.0 / 4294967296.0);
 }
 

@@ -1414,17 +1414,22 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
   // kGather independent gathers in flight per lane
   for (; k + (kGather - 1) * G < nn; k += kGather * G) {
     uint4 og[kGather];
+    int jg[kGather];
 #pragma unroll
-    for (int u = 0; u < kGather; ++u) og[u] = P.m4[cur][__ldg(nb + k + u * G)];
+    for (int u = 0; u < kGather; ++u) {
+      jg[u] = __ldg(nb + k + u * G);
+      og[u] = P.m4[cur][jg[u]];
+    }
 #pragma unroll
     for (int u = 0; u < kGather; ++u) {
       const uint4 o = og[u];
       const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
       const float r2 = dx * dx + dy * dy + dz * dz;
       if constexpr ((FL & F_DU) != 0) {
+        // each pair once, from its lower-index bead (the term is even in d)
         const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
         const float rn2 = r2 + q;
-        if (r2 < rc2 || rn2 < rc2) {
+        if (jg[u] > i && (r2 < rc2 || rn2 < rc2)) {
           const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
           dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
                         4294967296.0f);
@@ -1452,7 +1457,7 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
     if constexpr ((FL & F_DU) != 0) {
       const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
       const float rn2 = r2 + q;
-      if (r2 < rc2 || rn2 < rc2) {
+      if (j > i && (r2 < rc2 || rn2 < rc2)) {
         const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
         dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
                       4294967296.0f);
