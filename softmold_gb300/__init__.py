@@ -322,7 +322,7 @@ class System:
             d.seed = m.seed & 0xffffffff
             d.tension, d.delta_lxy = m.tension, m.delta_lxy
             d.resize_rate = 8
-            d.first_step = int(m.initial_time / m.dt + 1e-7)
+            d.first_step = int(m.initial_time / m.dt + 1e-7) if m.dt > 0 else 0  # the library refuses dt <= 0
             d.skin = skin
         h = C.c_void_p()
         _check(lib().smd_create_batch(descs, len(systems), precision, C.byref(h)), "smd_create_batch")

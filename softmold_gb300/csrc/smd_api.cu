@@ -516,9 +516,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   if (!descs || n_rep <= 0 || !out) return fail(1, "smd_create_batch: bad arguments");
   if (precision != SMD_PLAIN_FP64 && precision != SMD_MIXED) return fail(1, "unknown precision");
   *out = nullptr;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
-    return fail(2, "no CUDA device: the GB300 step has no CPU fallback");
+  // descriptors first (host checks only), then the device
   std::string why;
   for (int r = 0; r < n_rep; ++r)
     if (validate(descs[r], why)) return fail(1, "replica " + std::to_string(r) + ": " + why);
@@ -534,6 +532,9 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
       if (d.fconst[k] != d0.fconst[k] || d.uconst[k] != d0.uconst[k])
         return fail(1, "replicas of a batch must share the pair tables");
   }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(2, "no CUDA device: the GB300 step has no CPU fallback");
   std::unique_ptr<smd_system> h(new smd_system());
   h->mixed = (precision == SMD_MIXED);
   h->n_rep = n_rep;

@@ -63,3 +63,57 @@ def test_create_without_device_fails_loudly(built):
 def test_md_executable_usage(built):
     r = subprocess.run([smd.MD_EXE], capture_output=True, text=True)
     assert r.returncode == 0 and "usage" in r.stderr
+
+
+def _bad(**kw):
+    import dataclasses
+    from conftest import load_golden, mpd_from_golden
+    m = mpd_from_golden(load_golden("bil400"))
+    return dataclasses.replace(m, **kw)
+
+
+@pytest.mark.parametrize("change,message", [
+    ("empty", "n must be positive"),
+    ("short box", "shorter than 3 cutoffs"),
+    ("type", "bead type out of range"),
+    ("outside", "position out of the box"),
+    ("chain", "CHAIN block out of range"),
+    ("bond", "BOND bead index out of range"),
+    ("dt", "dt must be positive"),
+])
+def test_invalid_descriptors_are_refused_before_any_device_work(built, change, message):
+    """The descriptor checks run on the host before the device is touched,
+    so they hold with or without a GPU: an error code and a message, as the
+    reference's `throw 0` with a message on stdout."""
+    from conftest import load_golden
+    g = load_golden("bil400")
+    pos, typ = np.array(g["pos"]), np.array(g["type"], np.int32)
+    if change == "empty":
+        m = _bad(pos=np.zeros((0, 3)), vel=np.zeros((0, 3)), type=np.zeros(0, np.int32),
+                 chain_blocks=np.zeros((0, 3), np.int32), chain_consts=np.zeros((0, 4)))
+    elif change == "short box":
+        box = np.array(g["box"], np.float64)
+        box[2] = 5.9
+        m = _bad(box=box, pos=np.mod(pos, box))
+    elif change == "type":
+        typ[0] = int(g["n_types"])
+        m = _bad(type=typ)
+    elif change == "outside":
+        pos[0, 0] = -0.5
+        m = _bad(pos=pos)
+    elif change == "chain":
+        m = _bad(chain_blocks=np.array([[len(pos) - 2, 1, 3]], np.int32), chain_consts=np.array([[0.7, 100, 1, 100]]))
+    elif change == "bond":
+        m = _bad(bonds=np.array([[0, len(pos)]], np.int32), bond_consts=np.array([[0.7, 100.0]]))
+    else:
+        m = _bad(dt=0.0)
+    with pytest.raises(smd.SmdError, match=message):
+        smd.System(m)
+
+
+def test_batch_replicas_must_share_the_pair_tables(built):
+    a = _bad()
+    f = np.array(a.fconst, np.float64).copy()
+    f[0] += 1.0
+    with pytest.raises(smd.SmdError, match="share the pair tables"):
+        smd.System([a, _bad(fconst=f)])
