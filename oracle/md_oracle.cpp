@@ -114,6 +114,19 @@ struct OracleMD {
           orc_bond_force(pos(), sys.size, (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
         else
           orc_bend_force(pos(), sys.size, (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
+      } else if (m.type == smd::MOL_BOUNDARY) {
+        const std::vector<int> L = column(m, 1);
+        orc_boundary_force(pos(), sys.size, (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
+      } else if (m.type == smd::MOL_FLOATING_BASE) {
+        const std::vector<int> L = column(m, 1);
+        orc_floating_base_force(pos(), sys.type.data(), (int)m.bonds.size(), L.data(), m.constants.data(),
+                                acc.data());
+      } else if (m.type == smd::MOL_ZTORQUE) {
+        const std::vector<int> L = column(m, 3);
+        orc_ztorque_force(pos(), sys.size, (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
+      } else if (m.type == smd::MOL_ZPOWERPOTENTIAL) {
+        const std::vector<int> L = column(m, 2);
+        orc_zpower_force(pos(), (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
       } else if (m.type == smd::MOL_SOLID) {
       } else {
         err = "molecule type " + std::to_string(m.type) + " is not supported";
@@ -134,6 +147,13 @@ struct OracleMD {
   void pair_forces() {
     orc_pair_force(N, pos(), sys.type.data(), sys.size, sys.cutoff, sys.nTypes,
                    sys.twoBodyFconst.data(), acc.data());
+  }
+  // The first w indices of every entry of a residue, flattened.
+  static std::vector<int> column(const smd::Molecule& m, int w) {
+    std::vector<int> L;
+    for (const auto& b : m.bonds)
+      for (int q = 0; q < w; ++q) L.push_back(b[q]);
+    return L;
   }
   // Index list of a BOND (pairs) or BEND (triplets) residue.
   static std::vector<int> flat_list(const smd::Molecule& m) {
@@ -164,6 +184,15 @@ struct OracleMD {
         *beadPot += bp;
         pot += bp;
         ++*nBeadRes;
+      } else if (m.type == smd::MOL_BOUNDARY) {
+        pot += orc_boundary_potential(pos(), sys.size, (int)m.bonds.size(), column(m, 1).data(), m.constants.data());
+      } else if (m.type == smd::MOL_FLOATING_BASE) {
+        pot += orc_floating_base_potential(pos(), sys.type.data(), (int)m.bonds.size(), column(m, 1).data(),
+                                           m.constants.data());
+      } else if (m.type == smd::MOL_ZTORQUE) {
+        pot += orc_ztorque_potential(pos(), sys.size, (int)m.bonds.size(), column(m, 3).data(), m.constants.data());
+      } else if (m.type == smd::MOL_ZPOWERPOTENTIAL) {
+        pot += orc_zpower_potential(pos(), (int)m.bonds.size(), column(m, 2).data(), m.constants.data());
       }
     }
     return pot;

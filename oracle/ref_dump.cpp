@@ -8,7 +8,8 @@
 //   pairs.i32        (i,j) pairs visited by CellOpt::computeForce with r<rc
 //   pair_force.f64   N*3 accelerations from CellOpt::computeForce alone
 //   force.f64        N*3 from computeForce + every residue's do*Force
-//   energy.f64       [pair U, bonded U, bead U, then for each scale s_k:
+//   energy.f64       [pair U, bonded U (CHAIN, BOND, BEND and the external-field
+//                     residues), bead U, then for each scale s_k:
 //                     pair dU(s_k), bonded dU(s_k), bead dU(s_k)]
 //   rand53.f64       first 4096 MTRand(seed).rand53() draws
 // Run with OMP_NUM_THREADS=1 so traversal and summation orders are serial.
@@ -121,6 +122,10 @@ int main(int argc, char** argv) {
       case BOND: System.doBondForce(k); break;
       case BEND: System.doBendForce(k); break;
       case BEAD: System.doBeadForce(k); break;
+      case BOUNDARY: System.doBoundaryForce(k); break;
+      case FLOATING_BASE: System.doFloatingBaseForce(k); break;
+      case ZTORQUE: System.doZTorqueForce(k); break;
+      case ZPOWERPOTENTIAL: System.doZPowerForce(k); break;
       default: break;
     }
   }
@@ -139,6 +144,12 @@ int main(int argc, char** argv) {
       case BOND: bonded += System.doBondPotential(k); break;
       case BEND: bonded += System.doBendPotential(k); break;
       case BEAD: bead += System.doBeadPotential(k); break;
+      // external-field residues count with the bonded terms (the reference's
+      // potential_ output sums every residue); they have no size-change term
+      case BOUNDARY: bonded += System.doBoundaryPotential(k); break;
+      case FLOATING_BASE: bonded += System.doFloatingBasePotential(k); break;
+      case ZTORQUE: bonded += System.doZTorquePotential(k); break;
+      case ZPOWERPOTENTIAL: bonded += System.doZPowerPotential(k); break;
       default: break;
     }
   }

@@ -529,6 +529,34 @@ double beadbead_potential_fn(V3 d, const double* C, double cut2) {
 }  // namespace
 
 // ================================================================ C API
+namespace {
+// Bonds (l, l+1) of each chain except its last (the reference's loop stops at
+// length-2); d = x_l - x_{l+1} with the minimum image, z at the bond's middle
+// folded into [0, Lz).
+template <typename F>
+void ztorque_bonds(const double* pos, const double box[3], int nb, const int* blocks, F&& f) {
+  for (int j = 0; j < nb; ++j) {
+    const int start = blocks[3 * j], nChains = blocks[3 * j + 1], length = blocks[3 * j + 2];
+    for (int k = start; k < start + length * nChains; k += length)
+      for (int l = k; l < k + length - 2; ++l) {
+        const V3 d = diff(pos, l, l + 1, box);
+        double zHeight = pos[3 * l + 2] + d.z / 2.0;
+        while (zHeight >= box[2]) zHeight -= box[2];
+        while (zHeight < 0) zHeight += box[2];
+        f(l, d, zHeight);
+      }
+  }
+}
+// magnitude (include/algorithms/functions.h:250-257)
+inline double magnitude3(const V3& d) {
+  double sum = 0;
+  sum += d.x * d.x;
+  sum += d.y * d.y;
+  sum += d.z * d.z;
+  return std::sqrt(sum);
+}
+}  // namespace
+
 extern "C" {
 
 void orc_set_threads(int n) {
@@ -831,6 +859,125 @@ double orc_bead_potential(int n, const double* pos, const int* type, const doubl
 double orc_bead_dpotential(int n, const double* pos, const int* type, const double box[3], int nT,
                            int nb, const int* idx, const double* C, const double scale[3]) {
   return bead_energy(n, pos, type, box, nT, nb, idx, C, scale);
+}
+
+
+// ---------------------------------------------------------------- field residues
+// Expressions keep the reference's evaluation order (the oracle is built
+// without FMA contraction), so a one-thread run matches it bit for bit.
+
+void orc_boundary_force(const double* pos, const double box[3], int nb, const int* beads, const double* c,
+                        double* acc) {
+  const int dim = static_cast<int>(c[0]);
+  for (int j = 0; j < nb; ++j) {
+    const int i = beads[j];
+    double d = pos[3 * i + dim] - c[1];
+    d -= (d > box[dim] / 2.0) ? box[dim] : 0;
+    d += (d < -box[dim] / 2.0) ? box[dim] : 0;
+    const double dir = (d < 0) ? -1.0 : 1.0;
+    d = std::fabs(d);
+    const double d2 = d * d;
+    double magnitude = 0;
+    if (d2 <= 2.0) magnitude = c[3] * (4.0 / (d2 * d2 * d) - 2.0 / (d2 * d));
+    acc[3 * i + dim] += magnitude * dir;
+  }
+}
+
+double orc_boundary_potential(const double* pos, const double box[3], int nb, const int* beads, const double* c) {
+  const int dim = static_cast<int>(c[0]);
+  double total = 0;
+  for (int j = 0; j < nb; ++j) {
+    const int i = beads[j];
+    double d = pos[3 * i + dim] - c[1];
+    d -= (d > box[dim] / 2.0) ? box[dim] : 0;
+    d += (d < -box[dim] / 2.0) ? box[dim] : 0;
+    d = std::fabs(d);
+    double potential = 0;
+    d = d * d;
+    if (d <= 2.0) potential = c[3] * (1.0 / (d * d) - 1.0 / d);
+    total += potential;
+  }
+  return total;
+}
+
+// The force reads the absolute z; the potential reads z minus the residue's
+// first constant (both as in the reference).
+void orc_floating_base_force(const double* pos, const int* type, int nb, const int* beads, const double* c,
+                             double* acc) {
+  for (int j = 0; j < nb; ++j) {
+    const int i = beads[j];
+    const double z = pos[3 * i + 2];
+    const double* C = c + 6 * type[i];
+    if (z <= C[0]) {
+      acc[3 * i + 2] += C[3] * z * z * z - 2 * C[3] * C[0] * z * z + (2 * C[2] + C[3] * C[0] * C[0]) * z;
+    } else if (z < C[1]) {
+      const double rcz = z - C[1];
+      acc[3 * i + 2] += C[5] * (rcz * rcz) *
+                        (2 * z * z - (4 * C[1] - 7 * C[0]) * z + 2 * C[1] * C[1] + C[0] * (-7 * C[1] + 6 * C[0]));
+    }
+  }
+}
+
+double orc_floating_base_potential(const double* pos, const int* type, int nb, const int* beads, const double* c) {
+  double total = 0;
+  for (int j = 0; j < nb; ++j) {
+    const int i = beads[j];
+    const double z = pos[3 * i + 2] - c[0];
+    const double* C = c + 6 * type[i];
+    double potential = 0;
+    if (z <= C[0]) {
+      const double rmz = C[0] - z;
+      potential = C[2] * (C[0] * C[0] - z * z) + C[3] * rmz * rmz * rmz * ((C[0] / 3.0) - (1.0 / 4.0) * rmz) + C[4];
+    } else if (z < C[1]) {
+      const double rcz = C[1] - z;
+      potential = C[5] * rcz * rcz * rcz * (rcz * ((2.0 / 5.0) * rcz - (7.0 / 4.0) * C[0]) + (2.0) * C[0] * C[0]);
+    }
+    total += potential;
+  }
+  return total;
+}
+
+void orc_zpower_force(const double* pos, int nb, const int* blocks, const double* c, double* acc) {
+  for (int j = 0; j < nb; ++j)
+    for (int k = blocks[2 * j]; k < blocks[2 * j] + blocks[2 * j + 1]; ++k)
+      acc[3 * k + 2] += c[0] * std::pow(pos[3 * k + 2], c[1]);
+}
+
+double orc_zpower_potential(const double* pos, int nb, const int* blocks, const double* c) {
+  double total = 0;
+  for (int j = 0; j < nb; ++j)
+    for (int k = blocks[2 * j]; k < blocks[2 * j] + blocks[2 * j + 1]; ++k)
+      total += -c[0] * std::pow(pos[3 * k + 2], c[1] + 1) / (c[1] + 1);
+  return total;
+}
+
+
+void orc_ztorque_force(const double* pos, const double box[3], int nb, const int* blocks, const double* c,
+                       double* acc) {
+  ztorque_bonds(pos, box, nb, blocks, [&](int l, const V3& d, double z) {
+    const double mag = magnitude3(d);
+    double epsilon = c[0] - c[1] * std::tanh(c[2] * (z - c[3]));
+    if (z > c[3]) epsilon = 0;
+    const double m = -epsilon * (d.z / (mag * mag * mag * mag));
+    double* a1 = acc + 3 * l;
+    double* a2 = acc + 3 * (l + 1);
+    a1[0] += d.z * m * d.x;
+    a1[1] += d.z * m * d.y;
+    a1[2] += -m * (d.x * d.x + d.y * d.y);
+    a2[0] += -d.z * m * d.x;
+    a2[1] += -d.z * m * d.y;
+    a2[2] += m * (d.x * d.x + d.y * d.y);
+  });
+}
+
+double orc_ztorque_potential(const double* pos, const double box[3], int nb, const int* blocks, const double* c) {
+  double total = 0;
+  ztorque_bonds(pos, box, nb, blocks, [&](int, const V3& d, double z) {
+    const double cosTheta = std::abs(d.z) / magnitude3(d);
+    const double epsilon = c[0] - c[1] * std::tanh(c[2] * (z - c[3]));
+    total += epsilon * (1.0 - cosTheta * cosTheta) / 2.0;
+  });
+  return total;
 }
 
 }  // extern "C"

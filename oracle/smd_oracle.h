@@ -89,6 +89,32 @@ double orc_bead_potential(int n, const double* pos, const int* type, const doubl
 double orc_bead_dpotential(int n, const double* pos, const int* type, const double box[3], int nTypes,
                            int nb, const int* idx, const double* C, const double scale[3]);
 
+// External-field residues.  Forces and potentials, no size-change
+// difference: the reference's barostat adds none for them (MD.cpp:640-656).
+// BOUNDARY: beads[nb], constants {dim, centre, -, k} (Blob::doBoundaryForce /
+// doBoundaryPotential, include/system.h:2335-2349, 3138-3151; boundaryF /
+// boundaryP, include/MD.h:546-617).
+void orc_boundary_force(const double* pos, const double box[3], int nb, const int* beads, const double* c,
+                        double* acc);
+double orc_boundary_potential(const double* pos, const double box[3], int nb, const int* beads, const double* c);
+// FLOATING_BASE: beads[nb], constants 6 per bead type (Blob::doFloatingBaseForce
+// / doFloatingBasePotential, include/system.h:2403-2447; floatingBaseForce /
+// floatingBasePotential, include/MD.h:458-497).
+void orc_floating_base_force(const double* pos, const int* type, int nb, const int* beads, const double* c,
+                             double* acc);
+double orc_floating_base_potential(const double* pos, const int* type, int nb, const int* beads, const double* c);
+// ZPOWERPOTENTIAL: blocks {start, count}[nb], constants {c0, c1}
+// (Blob::doZPowerForce / doZPowerPotential, include/system.h:2666-2716;
+// zPowerForce / zPowerPotential, include/MD.h:1143-1154).
+void orc_zpower_force(const double* pos, int nb, const int* blocks, const double* c, double* acc);
+double orc_zpower_potential(const double* pos, int nb, const int* blocks, const double* c);
+// ZTORQUE: blocks {start, nChains, length}[nb], constants {a, b, c, z0}
+// (Blob::doZTorqueForce / doZTorquePotential, include/system.h:2583-2664;
+// zTorqueForce / zTorquePotential, include/MD.h:1116-1141).
+void orc_ztorque_force(const double* pos, const double box[3], int nb, const int* blocks, const double* c,
+                       double* acc);
+double orc_ztorque_potential(const double* pos, const double box[3], int nb, const int* blocks, const double* c);
+
 // Runs the reference MD loop on <name>.mpd exactly as `MD <name>` does
 // (MD.cpp:72-755) with `threads` OpenMP threads (1 reproduces the reference's
 // single-thread random streams).  Returns 0 on success.

@@ -178,6 +178,11 @@ class Mpd:
     bond_consts: np.ndarray | None = None  # (k,2) l0, k per term
     bends: np.ndarray | None = None        # (k,3) BEND residue terms
     bend_consts: np.ndarray | None = None  # (k,2) a, k per term
+    # external-field residues as terms: (kind, first, second) with kind the
+    # .mpd molecule type (11 BOUNDARY, 15 FLOATING_BASE, 16 ZTORQUE, 17
+    # ZPOWERPOTENTIAL) and second = -1 for one-bead terms; 8 constants each
+    fields: np.ndarray | None = None        # (k,3)
+    field_consts: np.ndarray | None = None  # (k,8)
 
 
 def read_mpd(path: str) -> Mpd:
@@ -191,6 +196,7 @@ def read_mpd(path: str) -> Mpd:
     blocks, consts = [], []
     bond_l, bond_c, bend_l, bend_c = [], [], [], []
     sph_idx, sph_c = None, None
+    field_l, field_c = [], []
     fc = uc = None
 
     def take(k=1):
@@ -252,6 +258,8 @@ def read_mpd(path: str) -> Mpd:
                 elif mt == 9:
                     sph_idx = b[:, 0].astype(np.int32)
                     sph_c = c
+                elif mt in (11, 15, 16, 17):
+                    field_terms(mt, b, c, typ, field_l, field_c)
         elif kw == "banana":
             pass
         elif kw == "solventGamma":
@@ -274,7 +282,42 @@ def read_mpd(path: str) -> Mpd:
                bonds=np.array(bond_l, np.int32).reshape(-1, 2) if bond_l else None,
                bond_consts=np.array(bond_c, np.float64).reshape(-1, 2) if bond_c else None,
                bends=np.array(bend_l, np.int32).reshape(-1, 3) if bend_l else None,
-               bend_consts=np.array(bend_c, np.float64).reshape(-1, 2) if bend_c else None)
+               bend_consts=np.array(bend_c, np.float64).reshape(-1, 2) if bend_c else None,
+               fields=np.array(field_l, np.int32).reshape(-1, 3) if field_l else None,
+               field_consts=np.array(field_c, np.float64).reshape(-1, 8) if field_c else None)
+
+
+def field_terms(mt, b, c, typ, out_l, out_c):
+    """Terms of one external-field residue (molecule type mt, index rows b,
+    constants c), in the order the reference applies them:
+      BOUNDARY 11 (Blob::doBoundaryForce, include/system.h:2335-2349): one
+        term per bead, constants {dim, centre, -, k};
+      FLOATING_BASE 15 (doFloatingBaseForce, :2403-2422): one term per bead,
+        the 6 constants of the bead's type, then the residue's first constant
+        (the potential's z offset, :2437);
+      ZTORQUE 16 (doZTorqueForce, :2626-2664): one term per bond (l, l+1) of
+        each chain but its last, constants {a, b, c, z0};
+      ZPOWERPOTENTIAL 17 (doZPowerForce, :2693-2716): one term per bead of each
+        {start, count} block, constants {c0, c1}."""
+    pad = lambda v: list(v) + [0.0] * (8 - len(v))  # noqa: E731
+    for row in b:
+        if mt == 11:
+            out_l.append((11, int(row[0]), -1))
+            out_c.append(pad(c[:4]))
+        elif mt == 15:
+            t = int(typ[int(row[0])])
+            out_l.append((15, int(row[0]), -1))
+            out_c.append(pad(list(c[6 * t:6 * t + 6]) + [c[0]]))
+        elif mt == 17:
+            for k in range(int(row[0]), int(row[0]) + int(row[1])):
+                out_l.append((17, k, -1))
+                out_c.append(pad(c[:2]))
+        else:
+            s0, nch, ln = int(row[0]), int(row[1]), int(row[2])
+            for k in range(s0, s0 + ln * nch, ln):
+                for l in range(k, k + ln - 2):
+                    out_l.append((16, l, l + 1))
+                    out_c.append(pad(c[:4]))
 
 
 class System:

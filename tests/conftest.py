@@ -52,4 +52,6 @@ def mpd_from_golden(g):
                    bonds=g["bonds"].astype(np.int32) if len(g.get("bonds", [])) else None,
                    bond_consts=g["bond_consts"] if len(g.get("bonds", [])) else None,
                    bends=g["bends"].astype(np.int32) if len(g.get("bends", [])) else None,
-                   bend_consts=g["bend_consts"] if len(g.get("bends", [])) else None)
+                   bend_consts=g["bend_consts"] if len(g.get("bends", [])) else None,
+                   fields=g["fields"].astype(np.int32) if len(g.get("fields", [])) else None,
+                   field_consts=g["field_consts"] if len(g.get("fields", [])) else None)

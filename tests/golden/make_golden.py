@@ -17,6 +17,12 @@ Fixtures
   net200/          a 200-lipid bilayer with BOND and BEND residues (input of
                    the network trajectory and MD tests) and the sha256 of
                    every file a 48-step reference MD run of it writes.
+  field400.npz     a relaxed 400-lipid bilayer with one residue of each
+                   external-field kind (BOUNDARY, FLOATING_BASE, ZTORQUE,
+                   ZPOWERPOTENTIAL), dumped as the cases above.
+  field200/        a 200-lipid bilayer with the same residues and the sha256
+                   of every file a 48-step reference MD run of it writes.
+                   (`--only-fields` regenerates these two alone.)
   generators.json  sha256 of the reference generators' .mpd for a few seeds.
 Inputs are seeded synthetic membranes built in the reference generators' terms
 (softmold_gb300 synth_*, byte-identical to generate/liposome and bilayer).
@@ -99,6 +105,42 @@ def add_network(path, seed):
     return len(near), len(nnear), len(trip)
 
 
+def add_fields(path, seed):
+    """Adds one residue of each external-field kind after the CHAIN block of a
+    bilayer .mpd (molecule blocks `type nBond / constants / indices`):
+      BOUNDARY 11         a wall normal to z 0.6 sigma above the top heads, k 0.5,
+                          on every top-leaflet head;
+      FLOATING_BASE 15    a z well on the bottom-leaflet heads (6 constants per
+                          type; type 0 carries a nonzero first constant, which
+                          the reference's potential subtracts from z);
+      ZTORQUE 16          over every lipid chain, cut off at the midplane;
+      ZPOWERPOTENTIAL 17  on the first 300 beads.
+    """
+    m = smd.read_mpd(path)
+    z = m.pos[:, 2]
+    zc = float(np.median(z))
+    heads = np.flatnonzero(m.type == 2)
+    top = heads[z[heads] > zc]
+    bottom = heads[z[heads] <= zc]
+    wall = float(z[top].max()) + 0.6
+    fb = np.zeros((m.n_types, 6))
+    fb[0] = [1.0, 2.0, 0.1, 0.01, 0.0, 0.01]
+    fb[2] = [zc - 2.0, zc + 1.0, 0.5, 0.05, 0.0, 0.02]
+    n = len(m.type)
+    blocks = ["11\t%d\n2 %.17g 0 0.5\n" % (len(top), wall) + "".join(f"{b}\n" for b in top),
+              "15\t%d\n" % len(bottom) + " ".join(f"{x:.17g}" for x in fb.ravel()) + "\n" +
+              "".join(f"{b}\n" for b in bottom),
+              "16\t1\n2 1 1 %.17g\n0 %d 3\n" % (zc, n // 3),
+              "17\t1\n-0.01 2.1\n0 300\n"]
+    lines = open(path).read().split("\n")
+    k = next(i for i, ln in enumerate(lines) if ln.strip() == "molecule")
+    lines = lines[:k + 4] + "".join(blocks).rstrip("\n").split("\n") + lines[k + 4:]
+    text = "\n".join(lines)
+    text = re.sub(r"nMolecules (\d+)", lambda mm: f"nMolecules {int(mm.group(1)) + 4}", text)
+    open(path, "w").write(text)
+    return len(top), len(bottom)
+
+
 def run_ref_md(workdir, name):
     env = dict(os.environ, OMP_NUM_THREADS="1")
     subprocess.run([os.path.join(REF, "MD"), name], cwd=workdir, env=env, check=True,
@@ -126,6 +168,8 @@ def dump_case(workdir, name, out_name):
         bond_consts=m.bond_consts if m.bond_consts is not None else np.zeros((0, 2)),
         bends=m.bends if m.bends is not None else np.zeros((0, 3), np.int32),
         bend_consts=m.bend_consts if m.bend_consts is not None else np.zeros((0, 2)),
+        fields=m.fields if m.fields is not None else np.zeros((0, 3), np.int32),
+        field_consts=m.field_consts if m.field_consts is not None else np.zeros((0, 8)),
         keys=rd("keys.i32", np.int32), pairs=rd("pairs.i32", np.int32).reshape(-1, 2),
         pair_force=rd("pair_force.f64", np.float64).reshape(n, 3),
         force=rd("force.f64", np.float64).reshape(n, 3),
@@ -133,10 +177,39 @@ def dump_case(workdir, name, out_name):
         rand53=rd("rand53.f64", np.float64))
 
 
+def make_fields(tmp):
+    """field400 (relaxed bilayer with the four external-field residues) and
+    field200/ (their 48-step reference MD run)."""
+    smd.synth_bilayer(os.path.join(tmp, "fld.mpd"), 93, 400, 3.45, 20.0, 0.01, 0.0)
+    set_run(os.path.join(tmp, "fld.mpd"), 4, 4, 4)
+    run_ref_md(tmp, "fld")
+    add_fields(os.path.join(tmp, "fld.mpd"), 93)
+    dump_case(tmp, "fld", "field400")
+    fdir = os.path.join(HERE, "field200")
+    os.makedirs(fdir, exist_ok=True)
+    smd.synth_bilayer(os.path.join(fdir, "fld.mpd"), 6, 200, 3.45, 16.0, 0.01, 0.0)
+    add_fields(os.path.join(fdir, "fld.mpd"), 6)
+    set_run(os.path.join(fdir, "fld.mpd"), 0.96, 0.48, 0.16)
+    run_dir = os.path.join(tmp, "fldrun")
+    os.makedirs(run_dir)
+    shutil.copy(os.path.join(fdir, "fld.mpd"), run_dir)
+    run_ref_md(run_dir, "fld")
+    json.dump({os.path.basename(f): hashlib.sha256(open(f, "rb").read()).hexdigest()
+               for f in sorted(glob.glob(os.path.join(run_dir, "*")))},
+              open(os.path.join(fdir, "digests.json"), "w"), indent=1)
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "ref_dump")):
         sys.exit("oracle/_ref is missing: run oracle/build_ref.sh first")
     tmp = tempfile.mkdtemp(prefix="smd_golden_")
+    if "--only-fields" in sys.argv:  # the external-field fixtures alone
+        try:
+            make_fields(tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        print("field fixtures written to", HERE)
+        return
     try:
         # relaxed vesicle, 300 lipids in a 30^3 box
         smd.synth_vesicle(os.path.join(tmp, "ves.mpd"), 1234, 300, 3.45, 30.0)
@@ -207,6 +280,7 @@ def main():
             gens.append(dict(kind="bilayer", seed=seed, n=n, density=3.45,
                              sha256=hashlib.sha256(open(os.path.join(d, "g.mpd"), "rb").read()).hexdigest()))
         json.dump(gens, open(os.path.join(HERE, "generators.json"), "w"), indent=1)
+        make_fields(tmp)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     print("golden fixtures written to", HERE)

@@ -54,6 +54,18 @@ class Oracle:
         for f in ("orc_bond_dpotential", "orc_bend_dpotential"):
             getattr(L, f).argtypes = [D, D, C.c_int, I, D, D]
             getattr(L, f).restype = C.c_double
+        L.orc_boundary_force.argtypes = [D, D, C.c_int, I, D, D]
+        L.orc_boundary_potential.argtypes = [D, D, C.c_int, I, D]
+        L.orc_boundary_potential.restype = C.c_double
+        L.orc_floating_base_force.argtypes = [D, I, C.c_int, I, D, D]
+        L.orc_floating_base_potential.argtypes = [D, I, C.c_int, I, D]
+        L.orc_floating_base_potential.restype = C.c_double
+        L.orc_zpower_force.argtypes = [D, C.c_int, I, D, D]
+        L.orc_zpower_potential.argtypes = [D, C.c_int, I, D]
+        L.orc_zpower_potential.restype = C.c_double
+        L.orc_ztorque_force.argtypes = [D, D, C.c_int, I, D, D]
+        L.orc_ztorque_potential.argtypes = [D, D, C.c_int, I, D]
+        L.orc_ztorque_potential.restype = C.c_double
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_threads(1)
         L.orc_md_run.argtypes = [C.c_char_p, C.c_int]
@@ -101,7 +113,53 @@ class Oracle:
         if si is not None and len(si):
             self.L.orc_bead_force(len(pos), pos.ctypes.data_as(D), typ.ctypes.data_as(I), _d(g["box"]), nT,
                                   len(si), _i(si), _d(g["sphere_consts"]), acc.ctypes.data_as(D))
+        for kind, idx, c in self._field_residues(g):
+            a = acc.ctypes.data_as(D)
+            if kind == 11:
+                self.L.orc_boundary_force(pos.ctypes.data_as(D), _d(g["box"]), len(idx), _i(idx), _d(c), a)
+            elif kind == 15:
+                self.L.orc_floating_base_force(pos.ctypes.data_as(D), typ.ctypes.data_as(I), len(idx), _i(idx),
+                                               _d(c), a)
+            elif kind == 16:
+                self.L.orc_ztorque_force(pos.ctypes.data_as(D), _d(g["box"]), len(idx) // 3, _i(idx), _d(c), a)
+            else:
+                self.L.orc_zpower_force(pos.ctypes.data_as(D), len(idx) // 2, _i(idx), _d(c), a)
         return acc
+
+    @staticmethod
+    def _field_residues(g):
+        """External-field terms (kind, first, second; 8 constants each) back
+        into residue calls: runs of one kind, with the index lists and
+        constants the oracle's residue functions take (FLOATING_BASE: 6 per
+        type, slot 0 starting with the potential's z offset; ZTORQUE: one
+        one-bond chain {l, 1, 3} per term; ZPOWERPOTENTIAL: {k, 1} per term)."""
+        f = g.get("fields")
+        if f is None or len(f) == 0:
+            return []
+        f = np.asarray(f)
+        fc = np.asarray(g["field_consts"])
+        typ = np.asarray(g["type"])
+        nT = int(g["n_types"])
+        out, k0 = [], 0
+        for k in range(1, len(f) + 1):
+            if k < len(f) and f[k, 0] == f[k0, 0]:
+                continue
+            kind, run, cs = int(f[k0, 0]), f[k0:k], fc[k0:k]
+            if kind == 11:
+                idx, c = run[:, 1], cs[0, :4]
+            elif kind == 15:
+                idx = run[:, 1]
+                c = np.zeros(6 * nT)
+                for t, cc in zip(run[:, 1], cs):
+                    c[6 * typ[t]:6 * typ[t] + 6] = cc[:6]
+                c[0] = cs[0, 6]
+            elif kind == 16:
+                idx, c = np.stack([run[:, 1], np.ones(len(run), int), np.full(len(run), 3)], 1).ravel(), cs[0, :4]
+            else:
+                idx, c = np.stack([run[:, 1], np.ones(len(run), int)], 1).ravel(), cs[0, :2]
+            out.append((kind, np.ascontiguousarray(idx, np.int32), np.ascontiguousarray(c, np.float64)))
+            k0 = k
+        return out
 
     @staticmethod
     def _residues(g, kind):
@@ -138,6 +196,19 @@ class Oracle:
                 a = (pos.ctypes.data_as(D), _d(g["box"]), len(lst), _i(lst), _d(c))
                 bonded += (getattr(self.L, f"orc_{kind}_potential")(*a) if scale is None else
                            getattr(self.L, f"orc_{kind}_dpotential")(*a, _d(scale)))
+        if scale is None:  # the external fields have no size-change term in the reference
+            for kind, idx, c in self._field_residues(g):
+                if kind == 11:
+                    bonded += self.L.orc_boundary_potential(pos.ctypes.data_as(D), _d(g["box"]), len(idx), _i(idx),
+                                                            _d(c))
+                elif kind == 15:
+                    bonded += self.L.orc_floating_base_potential(pos.ctypes.data_as(D), typ.ctypes.data_as(I),
+                                                                 len(idx), _i(idx), _d(c))
+                elif kind == 16:
+                    bonded += self.L.orc_ztorque_potential(pos.ctypes.data_as(D), _d(g["box"]), len(idx) // 3,
+                                                           _i(idx), _d(c))
+                else:
+                    bonded += self.L.orc_zpower_potential(pos.ctypes.data_as(D), len(idx) // 2, _i(idx), _d(c))
         bead = 0.0
         si = g.get("sphere_index")
         if si is not None and len(si):
