@@ -42,6 +42,7 @@ class SystemDesc(C.Structure):
         ("resize_rate", C.c_int), ("first_step", C.c_int), ("skin", C.c_double),
         ("n_bonds", C.c_int), ("bonds", C.POINTER(C.c_int)), ("bond_consts", C.POINTER(C.c_double)),
         ("n_bends", C.c_int), ("bends", C.POINTER(C.c_int)), ("bend_consts", C.POINTER(C.c_double)),
+        ("n_fields", C.c_int), ("fields", C.POINTER(C.c_int)), ("field_consts", C.POINTER(C.c_double)),
     ]
 
 
@@ -361,6 +362,10 @@ class System:
                 d.n_bonds, d.bonds, d.bond_consts = len(arrs["bl"]), _ip(arrs["bl"]), _dp(arrs["bc"])
             if "el" in arrs:
                 d.n_bends, d.bends, d.bend_consts = len(arrs["el"]), _ip(arrs["el"]), _dp(arrs["ec"])
+            if m.fields is not None and len(m.fields) > 0:
+                arrs["fl"] = np.ascontiguousarray(m.fields, np.int32)
+                arrs["fcs"] = np.ascontiguousarray(m.field_consts, np.float64)
+                d.n_fields, d.fields, d.field_consts = len(arrs["fl"]), _ip(arrs["fl"]), _dp(arrs["fcs"])
             d.dt, d.gamma, d.temperature = m.dt, m.gamma, m.temperature
             d.seed = m.seed & 0xffffffff
             d.tension, d.delta_lxy = m.tension, m.delta_lxy

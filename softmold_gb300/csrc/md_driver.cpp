@@ -31,6 +31,41 @@ int die(const std::string& what) {
   return 1;
 }
 
+// Terms of one external-field residue, in the order the reference applies
+// them (kind = the molecule type; 8 constants each):
+//   BOUNDARY (Blob::doBoundaryForce, include/system.h:2335-2349): one term per
+//     bead, constants {dim, centre, -, k};
+//   FLOATING_BASE (doFloatingBaseForce, :2403-2422): one term per bead, the 6
+//     constants of the bead's type, then the residue's first constant (the
+//     potential's z offset, doFloatingBasePotential :2437);
+//   ZTORQUE (doZTorqueForce, :2626-2664): one term per bond (l, l+1) of each
+//     chain but its last, constants {a, b, c, z0};
+//   ZPOWERPOTENTIAL (doZPowerForce, :2693-2716): one term per bead of each
+//     {start, count} block, constants {c0, c1}.
+void field_terms(const smd::Molecule& m, const std::vector<int>& type, std::vector<int>& idx,
+                 std::vector<double>& cs) {
+  auto push = [&](int a, int b, std::initializer_list<double> c) {
+    idx.insert(idx.end(), {m.type, a, b});
+    std::vector<double> v(c);
+    v.resize(8, 0.0);
+    cs.insert(cs.end(), v.begin(), v.end());
+  };
+  const std::vector<double>& C = m.constants;
+  for (const auto& b : m.bonds) {
+    if (m.type == smd::MOL_BOUNDARY) {
+      push(b[0], -1, {C[0], C[1], C[2], C[3]});
+    } else if (m.type == smd::MOL_FLOATING_BASE) {
+      const double* t = C.data() + 6 * type[b[0]];
+      push(b[0], -1, {t[0], t[1], t[2], t[3], t[4], t[5], C[0]});
+    } else if (m.type == smd::MOL_ZPOWERPOTENTIAL) {
+      for (int k = b[0]; k < b[0] + b[1]; ++k) push(k, -1, {C[0], C[1]});
+    } else {
+      for (int k = b[0]; k < b[0] + b[2] * b[1]; k += b[2])
+        for (int l = k; l < k + b[2] - 2; ++l) push(l, l + 1, {C[0], C[1], C[2], C[3]});
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" int smd_md_main(const char* name_c, int precision) {
@@ -46,6 +81,8 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   std::vector<double> consts;
   std::vector<int> sphere_idx, bond_idx, bend_idx;
   std::vector<double> bond_c, bend_c;
+  std::vector<int> field_idx;
+  std::vector<double> field_c;
   const std::vector<double>* sphere_consts = nullptr;
   for (const smd::Molecule& m : S.mol) {
     if (m.type == smd::MOL_CHAIN) {
@@ -70,9 +107,13 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
       }
       for (const auto& b : m.bonds) sphere_idx.push_back(b[0]);
       sphere_consts = &m.constants;
+    } else if (m.type == smd::MOL_BOUNDARY || m.type == smd::MOL_FLOATING_BASE || m.type == smd::MOL_ZTORQUE ||
+               m.type == smd::MOL_ZPOWERPOTENTIAL) {
+      field_terms(m, S.type, field_idx, field_c);
     } else if (m.type != smd::MOL_SOLID) {
       std::cout << "Error(MD): molecule type " << m.type
-                << " is not on the GPU step of this build (supported: CHAIN, BOND, BEND, BEAD)\n";
+                << " is not on the GPU step of this build (supported: CHAIN, BOND, BEND, BEAD, BOUNDARY, "
+                   "FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL)\n";
       return 1;
     }
   }
@@ -124,6 +165,9 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   d.n_bends = (int)bend_idx.size() / 3;
   d.bends = bend_idx.data();
   d.bend_consts = bend_c.data();
+  d.n_fields = (int)field_idx.size() / 3;
+  d.fields = field_idx.data();
+  d.field_consts = field_c.data();
   d.dt = S.deltaT;
   d.gamma = gamma;
   d.temperature = S.initialTemp;

@@ -51,7 +51,7 @@ struct smd_system {
   bool mixed = true;
   int n = 0, n_rep = 0, npad = 0, kmax = 0, n_cells = 0, n_tiles = 0;
   int n_sph = 0;  // BEAD sphere beads
-  int n_terms = 0;  // BOND / BEND term entries
+  int n_terms = 0;  // BOND / BEND and external-field term entries
   long long n_chains = 0;  // CHAIN molecules (lipids)
   // adjoint work arrays (allocated by the first adjoint call)
   struct Adj {
@@ -486,6 +486,17 @@ int validate(const smd_system_desc& d, std::string& why) {
     if (d.bonds[k] < 0 || d.bonds[k] >= d.n) return why = "BOND bead index out of range", 1;
   for (int k = 0; k < 3 * d.n_bends; ++k)
     if (d.bends[k] < 0 || d.bends[k] >= d.n) return why = "BEND bead index out of range", 1;
+  if (d.n_fields < 0) return why = "negative field term count", 1;
+  if (d.n_fields > 0 && (!d.fields || !d.field_consts)) return why = "null field array in descriptor", 1;
+  for (int k = 0; k < d.n_fields; ++k) {
+    const int kind = d.fields[3 * k], a = d.fields[3 * k + 1], b = d.fields[3 * k + 2];
+    if (kind != 11 && kind != 15 && kind != 16 && kind != 17)
+      return why = "field term kind must be 11, 15, 16 or 17 (BOUNDARY, FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL)", 1;
+    if (a < 0 || a >= d.n || (kind == 16 ? (b < 0 || b >= d.n || b == a) : b != -1))
+      return why = "field term bead index out of range", 1;
+    if (kind == 11 && !(d.field_consts[8 * k] == 0 || d.field_consts[8 * k] == 1 || d.field_consts[8 * k] == 2))
+      return why = "BOUNDARY dimension must be 0, 1 or 2", 1;
+  }
   if (!(d.dt > 0)) return why = "dt must be positive", 1;
   return 0;
 }
@@ -581,6 +592,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   // chain constant sets
   std::vector<std::array<double, 4>> sets;
   std::vector<std::array<double, 2>> tsets;
+  std::vector<std::array<double, kFieldConst>> fsets;
   std::vector<std::vector<int4>> bead_terms(total);
   std::vector<int> cinfo(total, 0);
   std::vector<int> type(total, 0);
@@ -645,15 +657,38 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
       const int set = term_set(d.bond_consts[2 * k], d.bond_consts[2 * k + 1]);
       if (set < 0) return fail(1, "too many distinct BOND / BEND constant sets");
       const int a = bead + d.bonds[2 * k], b = bead + d.bonds[2 * k + 1];
-      bead_terms[a].push_back(make_int4(0 | (0 << 1) | (set << 3), a, b, -1));
-      bead_terms[b].push_back(make_int4(0 | (1 << 1) | (set << 3), a, b, -1));
+      bead_terms[a].push_back(make_int4(term_pack(kTermBond, 0, set), a, b, -1));
+      bead_terms[b].push_back(make_int4(term_pack(kTermBond, 1, set), a, b, -1));
     }
     for (int k = 0; k < d.n_bends; ++k) {
       const int set = term_set(d.bend_consts[2 * k], d.bend_consts[2 * k + 1]);
       if (set < 0) return fail(1, "too many distinct BOND / BEND constant sets");
       const int a = bead + d.bends[3 * k], b = bead + d.bends[3 * k + 1], c = bead + d.bends[3 * k + 2];
       for (int role = 0; role < 3; ++role)
-        bead_terms[role == 0 ? a : (role == 1 ? b : c)].push_back(make_int4(1 | (role << 1) | (set << 3), a, b, c));
+        bead_terms[role == 0 ? a : (role == 1 ? b : c)].push_back(
+            make_int4(term_pack(kTermBend, role, set), a, b, c));
+    }
+    // external-field terms: the same per-bead entries, constant sets in fieldD
+    for (int k = 0; k < d.n_fields; ++k) {
+      std::array<double, kFieldConst> c;
+      for (int q = 0; q < kFieldConst; ++q) c[q] = d.field_consts[kFieldConst * k + q];
+      int set = -1;
+      for (size_t q = 0; q < fsets.size() && set < 0; ++q)
+        if (fsets[q] == c) set = (int)q;
+      if (set < 0) {
+        if ((int)fsets.size() >= kMaxFieldSets) return fail(1, "too many distinct external-field constant sets");
+        fsets.push_back(c);
+        set = (int)fsets.size() - 1;
+      }
+      const int kind = d.fields[3 * k], a = bead + d.fields[3 * k + 1];
+      const int tk = kind == 11 ? kTermBoundary : (kind == 15 ? kTermFloating : (kind == 16 ? kTermZTorque : kTermZPower));
+      if (tk == kTermZTorque) {
+        const int b = bead + d.fields[3 * k + 2];
+        bead_terms[a].push_back(make_int4(term_pack(tk, 0, set), a, b, -1));
+        bead_terms[b].push_back(make_int4(term_pack(tk, 1, set), a, b, -1));
+      } else {
+        bead_terms[a].push_back(make_int4(term_pack(tk, 0, set), a, -1, -1));
+      }
     }
     bead += d.n;
   }
@@ -666,6 +701,8 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
       T.termD[q][k] = tsets[q][k];
       T.termF[q][k] = (float)tsets[q][k];
     }
+  for (size_t q = 0; q < fsets.size(); ++q)
+    for (int k = 0; k < kFieldConst; ++k) T.fieldD[q][k] = fsets[q][k];
   for (size_t q = 0; q < sets.size(); ++q)
     for (int k = 0; k < 4; ++k) {
       T.chainD[q][k] = sets[q][k];
@@ -1475,7 +1512,7 @@ int adj_check_handle(smd_system* h) {
   if (!h) return fail(1, "null handle");
   if (h->n_rep != 1) return fail(1, "the adjoint runs on single-system handles");
   if (h->n_sph) return fail(1, "the adjoint does not cover BEAD residues");
-  if (h->n_terms) return fail(1, "the adjoint does not cover BOND / BEND residues");
+  if (h->n_terms) return fail(1, "the adjoint does not cover BOND / BEND or external-field residues");
   return 0;
 }
 

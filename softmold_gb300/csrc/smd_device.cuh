@@ -24,6 +24,21 @@ namespace smd {
 constexpr int kMaxTypes = 8;
 constexpr int kMaxChainSets = 32;
 constexpr int kMaxTermSets = 64;  // distinct constant pairs of BOND / BEND residues
+constexpr int kMaxFieldSets = 64; // distinct constant sets of external-field terms
+constexpr int kFieldConst = 8;    // constants per external-field term set
+
+// Residue term entries (per bead, file order): x = kind | role << 3 | set << 5,
+// then the term's beads (file order; -1 where absent).  role: the bead's place
+// in the term.  Sets index termD/termF (BOND, BEND) or fieldD (the rest).
+enum TermKind {
+  kTermBond = 0, kTermBend = 1,        // BOND {first, second}, BEND {first, second, third}
+  kTermBoundary = 2, kTermFloating = 3, // BOUNDARY {bead}, FLOATING_BASE {bead}
+  kTermZTorque = 4, kTermZPower = 5     // ZTORQUE {first, second}, ZPOWERPOTENTIAL {bead}
+};
+__host__ __device__ inline int term_pack(int kind, int role, int set) { return kind | (role << 3) | (set << 5); }
+__host__ __device__ inline int term_kind(int x) { return x & 7; }
+__host__ __device__ inline int term_role(int x) { return (x >> 3) & 3; }
+__host__ __device__ inline int term_set(int x) { return x >> 5; }
 constexpr int kBlock = 256;
 // threads per CTA of the per-bead step kernels (bin, reorder, integrator):
 // small CTAs spread a small system over every SM
@@ -138,6 +153,7 @@ struct Tables {  // force/potential tables (float and double) in constant-like m
   double chainD[kMaxChainSets][4];
   float termF[kMaxTermSets][2];   // BOND {l0, k} / BEND {a, k} constant sets
   double termD[kMaxTermSets][2];
+  double fieldD[kMaxFieldSets][kFieldConst];  // external-field term constants (FP64)
 };
 
 // All device pointers of one handle.

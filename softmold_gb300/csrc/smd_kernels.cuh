@@ -1320,11 +1320,144 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
   }
 }
 
+// ---------------------------------------------------------------- external fields
+// BOUNDARY, FLOATING_BASE, ZTORQUE and ZPOWERPOTENTIAL residues, in FP64 in
+// both forms (steep walls; few beads), with the reference's formulas and
+// quirks (boundaryF/P, floatingBaseForce/Potential, zTorqueForce/Potential,
+// zPowerForce/Potential, include/MD.h:458-617, 1116-1154).  A bead's own
+// terms read its master position (before this thread moves it); the two
+// beads of a ZTORQUE term read the current mirror, which no thread writes
+// during the step, so both see the same bond.
+template <bool MIXED>
+__device__ __forceinline__ Vec3<double> mirror_pos(const DevPtrs& P, int cur, int s, const double box[3]) {
+  if constexpr (MIXED) {
+    const uint4 m = P.m4[cur][s];
+    return Vec3<double>{(double)m.x * (box[0] * (1.0 / 4294967296.0)), (double)m.y * (box[1] * (1.0 / 4294967296.0)),
+                        (double)m.z * (box[2] * (1.0 / 4294967296.0))};
+  } else {
+    const double4 m = P.d4[cur][s];
+    return Vec3<double>{m.x, m.y, m.z};
+  }
+}
+
+// ZTORQUE bond of file-order beads (a, b): d = x_a - x_b (minimum image) and
+// the height of its middle folded into [0, Lz).
+template <bool MIXED>
+__device__ __forceinline__ void ztorque_bond(const DevPtrs& P, int cur, int a, int b, const double box[3],
+                                             Vec3<double>& d, double& z) {
+  const int sa = P.inv[a], sb = P.inv[b];
+  const Vec3<double> pa = mirror_pos<MIXED>(P, cur, sa, box);
+  if constexpr (MIXED) {
+    const uint4 ma = P.m4[cur][sa], mb = P.m4[cur][sb];
+    d = Vec3<double>{frac_delta_d(ma.x, mb.x, box[0] * (1.0 / 4294967296.0)),
+                     frac_delta_d(ma.y, mb.y, box[1] * (1.0 / 4294967296.0)),
+                     frac_delta_d(ma.z, mb.z, box[2] * (1.0 / 4294967296.0))};
+  } else {
+    const Vec3<double> pb = mirror_pos<MIXED>(P, cur, sb, box);
+    double e[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
+    for (int k = 0; k < 3; ++k) {
+      if (e[k] > box[k] / 2.0) e[k] -= box[k];
+      if (e[k] < -box[k] / 2.0) e[k] += box[k];
+    }
+    d = Vec3<double>{e[0], e[1], e[2]};
+  }
+  z = pa.z + d.z / 2.0;
+  while (z >= box[2]) z -= box[2];
+  while (z < 0) z += box[2];
+}
+
+template <bool MIXED>
+__device__ __noinline__ void field_force(const DevPtrs& P, int cur, int i, const int4 t, const double box[3],
+                                         Vec3<double>& ff) {
+  const double* c = P.tab->fieldD[term_set(t.x)];
+  const int kind = term_kind(t.x);
+  if (kind == kTermZTorque) {
+    Vec3<double> d;
+    double z;
+    ztorque_bond<MIXED>(P, cur, t.y, t.z, box, d, z);
+    const double mag = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+    double eps = c[0] - c[1] * tanh(c[2] * (z - c[3]));
+    if (z > c[3]) eps = 0;
+    const double m = -eps * (d.z / (mag * mag * mag * mag));
+    const double sg = term_role(t.x) == 0 ? 1.0 : -1.0;
+    ff.x += sg * (d.z * m * d.x);
+    ff.y += sg * (d.z * m * d.y);
+    ff.z += sg * (-m * (d.x * d.x + d.y * d.y));
+    return;
+  }
+  const double pos[3] = {P.x[i], P.y[i], P.z[i]};
+  if (kind == kTermBoundary) {
+    const int dim = (int)c[0];
+    double d = pos[dim] - c[1];
+    d -= (d > box[dim] / 2.0) ? box[dim] : 0;
+    d += (d < -box[dim] / 2.0) ? box[dim] : 0;
+    const double dir = (d < 0) ? -1.0 : 1.0;
+    d = fabs(d);
+    const double d2 = d * d;
+    const double mag = (d2 <= 2.0) ? c[3] * (4.0 / (d2 * d2 * d) - 2.0 / (d2 * d)) : 0.0;
+    (dim == 0 ? ff.x : (dim == 1 ? ff.y : ff.z)) += mag * dir;
+  } else if (kind == kTermFloating) {
+    const double z = pos[2];
+    if (z <= c[0]) {
+      ff.z += c[3] * z * z * z - 2 * c[3] * c[0] * z * z + (2 * c[2] + c[3] * c[0] * c[0]) * z;
+    } else if (z < c[1]) {
+      const double rcz = z - c[1];
+      ff.z += c[5] * (rcz * rcz) * (2 * z * z - (4 * c[1] - 7 * c[0]) * z + 2 * c[1] * c[1] + c[0] * (-7 * c[1] + 6 * c[0]));
+    }
+  } else if (kind == kTermZPower) {
+    ff.z += c[0] * pow(pos[2], c[1]);
+  }
+}
+
+// Potential of a term owned by this bead (one-bead terms; ZTORQUE: its
+// first bead).  The FLOATING_BASE potential subtracts the residue's first
+// constant (c[6]) from z and the ZTORQUE potential has no height cut-off, as
+// in the reference.  Both are out of line: they run only for systems with
+// field residues and keep their registers out of the common pass.
+template <bool MIXED>
+__device__ __noinline__ double field_potential(const DevPtrs& P, int cur, int i, const int4 t, const double box[3]) {
+  const double* c = P.tab->fieldD[term_set(t.x)];
+  const int kind = term_kind(t.x);
+  if (kind == kTermZTorque) {
+    Vec3<double> d;
+    double z;
+    ztorque_bond<MIXED>(P, cur, t.y, t.z, box, d, z);
+    const double cs = fabs(d.z) / sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+    const double eps = c[0] - c[1] * tanh(c[2] * (z - c[3]));
+    return eps * (1.0 - cs * cs) / 2.0;
+  }
+  const double pos[3] = {P.x[i], P.y[i], P.z[i]};
+  if (kind == kTermBoundary) {
+    const int dim = (int)c[0];
+    double d = pos[dim] - c[1];
+    d -= (d > box[dim] / 2.0) ? box[dim] : 0;
+    d += (d < -box[dim] / 2.0) ? box[dim] : 0;
+    d = fabs(d);
+    d = d * d;
+    return (d <= 2.0) ? c[3] * (1.0 / (d * d) - 1.0 / d) : 0.0;
+  }
+  if (kind == kTermFloating) {
+    const double z = pos[2] - c[6];
+    if (z <= c[0]) {
+      const double rmz = c[0] - z;
+      return c[2] * (c[0] * c[0] - z * z) + c[3] * rmz * rmz * rmz * ((c[0] / 3.0) - (1.0 / 4.0) * rmz) + c[4];
+    }
+    if (z < c[1]) {
+      const double rcz = c[1] - z;
+      return c[5] * rcz * rcz * rcz * (rcz * ((2.0 / 5.0) * rcz - (7.0 / 4.0) * c[0]) + (2.0) * c[0] * c[0]);
+    }
+    return 0.0;
+  }
+  if (kind == kTermZPower) return -c[0] * pow(pos[2], c[1] + 1) / (c[1] + 1);
+  return 0.0;
+}
+
 // Bonded force on bead i: its share of the CHAIN bonds and bends (the bead
 // at chain position p takes bonds (p-1,p), (p,p+1) and bends (p-2..p),
 // (p-1..p+1), (p..p+2)), then its BOND / BEND residue terms in entry order.
 // FP32 in the mixed form (vectors exact from the fractional mirror), FP64 in
-// the plain form.  Every step variant takes its bonded force from here.
+// the plain form; an external-field term's force is evaluated in FP64 and
+// added in R.  Every step variant takes its bonded force from here.
 template <bool MIXED>
 __device__ __forceinline__ Vec3<typename std::conditional<MIXED, float, double>::type> bonded_force(
     const DevPtrs& P, int cur, int i, int ci, const double box[3], const RepState& rs) {
@@ -1349,10 +1482,18 @@ __device__ __forceinline__ Vec3<typename std::conditional<MIXED, float, double>:
     const int e1 = P.term_off[o + 1];
     for (int e = P.term_off[o]; e < e1; ++e) {
       const int4 t = P.terms[e];
-      const int role = (t.x >> 1) & 3, set = t.x >> 3;
+      const int kind = term_kind(t.x), role = term_role(t.x), set = term_set(t.x);
+      if (kind > kTermBend) {
+        Vec3<double> f1{0.0, 0.0, 0.0};
+        field_force<MIXED>(P, cur, i, t, box, f1);
+        fb.x += (R)f1.x;
+        fb.y += (R)f1.y;
+        fb.z += (R)f1.z;
+        continue;
+      }
       const R* cf;
       if constexpr (MIXED) cf = T.termF[set]; else cf = T.termD[set];
-      if ((t.x & 1) == 0)  // bond (first, second): the bead's force is mag (x_self - x_other)
+      if (kind == kTermBond)  // bond (first, second): the bead's force is mag (x_self - x_other)
         bond_term<R>(term_vec<MIXED, R>(P, cur, o, role == 0 ? t.z : t.y, box, rs), cf, (R)1, fb);
       else  // bend (first, second, third): da = x1 - x2, db = x2 - x3
         bend_term<R>(term_vec<MIXED, R>(P, cur, t.y, t.z, box, rs), term_vec<MIXED, R>(P, cur, t.z, t.w, box, rs),
@@ -1660,9 +1801,14 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
                              (float)(rs.scale[2] * rs.scale[2] - 1.0)};
       for (int e = P.term_off[o]; e < e1; ++e) {
         const int4 t = P.terms[e];
-        const int role = (t.x >> 1) & 3, set = t.x >> 3;
+        const int kind = term_kind(t.x), role = term_role(t.x), set = term_set(t.x);
+        if (kind > kTermBend) {  // external fields: energy only (no size-change term in the reference)
+          if constexpr ((FL & F_ENERGY) != 0)
+            if (role == 0) e_bond += field_potential<MIXED>(P, cur, i, t, box);
+          continue;
+        }
         const double* cd = T.termD[set];
-        if ((t.x & 1) == 0) {  // bond (first, second): the bead's force is mag (x_self - x_other)
+        if (kind == kTermBond) {  // bond (first, second): the bead's force is mag (x_self - x_other)
           if constexpr ((FL & (F_DU | F_ENERGY)) != 0) {
             if (role == 0) {  // energy terms owned by the first bead
               if constexpr (MIXED && (FL & F_DU) != 0)
