@@ -66,11 +66,14 @@ typedef struct smd_system_desc {
   const double* bend_consts;    /* n_bends*2: a, k of each term's residue */
   int n_fields;                 /* terms of external-field residues, in the order the reference applies them */
   const int* fields;            /* n_fields*3: kind (the .mpd molecule type: 11 BOUNDARY, 15 FLOATING_BASE,
-                                   16 ZTORQUE, 17 ZPOWERPOTENTIAL), first bead, second bead (ZTORQUE; else -1) */
+                                   16 ZTORQUE, 17 ZPOWERPOTENTIAL, 19 BALL), first bead, second bead
+                                   (ZTORQUE, BALL; else -1) */
   const double* field_consts;   /* n_fields*8: BOUNDARY {dim, centre, -, k} (Blob::doBoundaryForce);
                                    FLOATING_BASE the 6 constants of the bead's type, then the residue's
                                    first constant (doFloatingBaseForce); ZTORQUE {a, b, c, z0} for one
-                                   bond (l, l+1) (doZTorqueForce); ZPOWERPOTENTIAL {c0, c1} (doZPowerForce) */
+                                   bond (l, l+1) (doZTorqueForce); ZPOWERPOTENTIAL {c0, c1} (doZPowerForce);
+                                   BALL {r0, k, the bond's own first bead} with first = the residue's
+                                   first bond's first bead (doBallForce / doBallPotential) */
 } smd_system_desc;
 
 typedef struct smd_system smd_system;
@@ -79,7 +82,7 @@ typedef struct smd_energy {
   double pair;     /* CellOpt::computePotential */
   double bonded;   /* Blob::doChainPotential, doBondPotential, doBendPotential and the
                       external-field potentials (doBoundaryPotential, doFloatingBasePotential,
-                      doZTorquePotential, doZPowerPotential) */
+                      doZTorquePotential, doZPowerPotential, doBallPotential) */
   double sphere;   /* Blob::doBeadPotential */
   double kinetic;  /* Kinetic::compute: sum v^2/2 */
 } smd_energy;

@@ -127,6 +127,9 @@ struct OracleMD {
       } else if (m.type == smd::MOL_ZPOWERPOTENTIAL) {
         const std::vector<int> L = column(m, 2);
         orc_zpower_force(pos(), (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
+      } else if (m.type == smd::MOL_BALL) {
+        const std::vector<int> L = column(m, 2);
+        orc_ball_force(pos(), sys.size, (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
       } else if (m.type == smd::MOL_SOLID) {
       } else {
         err = "molecule type " + std::to_string(m.type) + " is not supported";
@@ -193,6 +196,8 @@ struct OracleMD {
         pot += orc_ztorque_potential(pos(), sys.size, (int)m.bonds.size(), column(m, 3).data(), m.constants.data());
       } else if (m.type == smd::MOL_ZPOWERPOTENTIAL) {
         pot += orc_zpower_potential(pos(), (int)m.bonds.size(), column(m, 2).data(), m.constants.data());
+      } else if (m.type == smd::MOL_BALL) {
+        pot += orc_ball_potential(pos(), sys.size, (int)m.bonds.size(), column(m, 2).data(), m.constants.data());
       }
     }
     return pot;

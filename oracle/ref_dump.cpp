@@ -126,6 +126,7 @@ int main(int argc, char** argv) {
       case FLOATING_BASE: System.doFloatingBaseForce(k); break;
       case ZTORQUE: System.doZTorqueForce(k); break;
       case ZPOWERPOTENTIAL: System.doZPowerForce(k); break;
+      case BALL: System.doBallForce(k); break;
       default: break;
     }
   }
@@ -150,6 +151,7 @@ int main(int argc, char** argv) {
       case FLOATING_BASE: bonded += System.doFloatingBasePotential(k); break;
       case ZTORQUE: bonded += System.doZTorquePotential(k); break;
       case ZPOWERPOTENTIAL: bonded += System.doZPowerPotential(k); break;
+      case BALL: bonded += System.doBallPotential(k); break;
       default: break;
     }
   }

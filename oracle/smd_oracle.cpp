@@ -980,4 +980,53 @@ double orc_ztorque_potential(const double* pos, const double box[3], int nb, con
   return total;
 }
 
+
+void orc_ball_force(const double* pos, const double box[3], int nb, const int* bonds, const double* c, double* acc) {
+  if (nb <= 0) return;
+  const int first = bonds[0];
+  double ax = 0, ay = 0, az = 0;
+  for (int j = 0; j < nb; ++j) {
+    const int second = bonds[2 * j + 1];
+    V3 d = diff(pos, first, second, box);
+    double dr = d.x * d.x + d.y * d.y + d.z * d.z;
+    V3 aFirst{0, 0, 0};
+    if (dr < c[0] * c[0]) {
+      dr = std::sqrt(dr);
+      double magnitude = dr - c[0];
+      magnitude = -magnitude * c[1] / dr;
+      d.x *= magnitude;
+      d.y *= magnitude;
+      d.z *= magnitude;
+      aFirst.x += d.x;
+      aFirst.y += d.y;
+      aFirst.z += d.z;
+      acc[3 * second] -= d.x;
+      acc[3 * second + 1] -= d.y;
+      acc[3 * second + 2] -= d.z;
+    }
+    ax += aFirst.x;
+    ay += aFirst.y;
+    az += aFirst.z;
+  }
+  acc[3 * first] += ax;
+  acc[3 * first + 1] += ay;
+  acc[3 * first + 2] += az;
+}
+
+double orc_ball_potential(const double* pos, const double box[3], int nb, const int* bonds, const double* c) {
+  double total = 0;
+  for (int j = 0; j < nb; ++j) {
+    const V3 d = diff(pos, bonds[2 * j], bonds[2 * j + 1], box);
+    double dr = d.x * d.x + d.y * d.y + d.z * d.z;
+    double potential = 0;
+    if (dr < c[0] * c[0]) {
+      dr = std::sqrt(dr);
+      potential = dr - c[0];
+      potential = 0.5 * c[1] * potential * potential;
+    }
+    total += potential;
+  }
+  return total;
+}
+
 }  // extern "C"

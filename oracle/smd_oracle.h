@@ -115,6 +115,14 @@ void orc_ztorque_force(const double* pos, const double box[3], int nb, const int
                        double* acc);
 double orc_ztorque_potential(const double* pos, const double box[3], int nb, const int* blocks, const double* c);
 
+// BALL: bonds {first, second}[nb], constants {r0, k}: harmonicHalfF on each
+// bond, all pulling the first bond's first bead; the potential takes each
+// bond's own first bead (Blob::doBallForce / doBallPotential,
+// include/system.h:1937-1971, 2750-2779; harmonicHalfF / harmonicHalfP,
+// include/MD.h:1164-1222).
+void orc_ball_force(const double* pos, const double box[3], int nb, const int* bonds, const double* c, double* acc);
+double orc_ball_potential(const double* pos, const double box[3], int nb, const int* bonds, const double* c);
+
 // Runs the reference MD loop on <name>.mpd exactly as `MD <name>` does
 // (MD.cpp:72-755) with `threads` OpenMP threads (1 reproduces the reference's
 // single-thread random streams).  Returns 0 on success.

@@ -181,7 +181,8 @@ class Mpd:
     bend_consts: np.ndarray | None = None  # (k,2) a, k per term
     # external-field residues as terms: (kind, first, second) with kind the
     # .mpd molecule type (11 BOUNDARY, 15 FLOATING_BASE, 16 ZTORQUE, 17
-    # ZPOWERPOTENTIAL) and second = -1 for one-bead terms; 8 constants each
+    # ZPOWERPOTENTIAL, 19 BALL) and second = -1 for one-bead terms; 8
+    # constants each
     fields: np.ndarray | None = None        # (k,3)
     field_consts: np.ndarray | None = None  # (k,8)
 
@@ -259,7 +260,7 @@ def read_mpd(path: str) -> Mpd:
                 elif mt == 9:
                     sph_idx = b[:, 0].astype(np.int32)
                     sph_c = c
-                elif mt in (11, 15, 16, 17):
+                elif mt in (11, 15, 16, 17, 19):
                     field_terms(mt, b, c, typ, field_l, field_c)
         elif kw == "banana":
             pass
@@ -299,7 +300,10 @@ def field_terms(mt, b, c, typ, out_l, out_c):
       ZTORQUE 16 (doZTorqueForce, :2626-2664): one term per bond (l, l+1) of
         each chain but its last, constants {a, b, c, z0};
       ZPOWERPOTENTIAL 17 (doZPowerForce, :2693-2716): one term per bead of each
-        {start, count} block, constants {c0, c1}."""
+        {start, count} block, constants {c0, c1};
+      BALL 19 (doBallForce, :1937-1971): one term per bond (first of the
+        residue's first bond, this bond's second), constants {r0, k, this
+        bond's first} (the potential, :2750-2779, takes each bond's own first)."""
     pad = lambda v: list(v) + [0.0] * (8 - len(v))  # noqa: E731
     for row in b:
         if mt == 11:
@@ -309,6 +313,9 @@ def field_terms(mt, b, c, typ, out_l, out_c):
             t = int(typ[int(row[0])])
             out_l.append((15, int(row[0]), -1))
             out_c.append(pad(list(c[6 * t:6 * t + 6]) + [c[0]]))
+        elif mt == 19:
+            out_l.append((19, int(b[0][0]), int(row[1])))
+            out_c.append(pad([c[0], c[1], float(row[0])]))
         elif mt == 17:
             for k in range(int(row[0]), int(row[0]) + int(row[1])):
                 out_l.append((17, k, -1))

@@ -41,7 +41,11 @@ int die(const std::string& what) {
 //   ZTORQUE (doZTorqueForce, :2626-2664): one term per bond (l, l+1) of each
 //     chain but its last, constants {a, b, c, z0};
 //   ZPOWERPOTENTIAL (doZPowerForce, :2693-2716): one term per bead of each
-//     {start, count} block, constants {c0, c1}.
+//     {start, count} block, constants {c0, c1};
+//   BALL (doBallForce, :1937-1971): one term per bond (the residue's first
+//     bond's first bead, this bond's second), constants {r0, k, this bond's
+//     first} (the potential, doBallPotential :2750-2779, takes each bond's
+//     own first).
 void field_terms(const smd::Molecule& m, const std::vector<int>& type, std::vector<int>& idx,
                  std::vector<double>& cs) {
   auto push = [&](int a, int b, std::initializer_list<double> c) {
@@ -59,6 +63,8 @@ void field_terms(const smd::Molecule& m, const std::vector<int>& type, std::vect
       push(b[0], -1, {t[0], t[1], t[2], t[3], t[4], t[5], C[0]});
     } else if (m.type == smd::MOL_ZPOWERPOTENTIAL) {
       for (int k = b[0]; k < b[0] + b[1]; ++k) push(k, -1, {C[0], C[1]});
+    } else if (m.type == smd::MOL_BALL) {
+      push(m.bonds[0][0], b[1], {C[0], C[1], (double)b[0]});
     } else {
       for (int k = b[0]; k < b[0] + b[2] * b[1]; k += b[2])
         for (int l = k; l < k + b[2] - 2; ++l) push(l, l + 1, {C[0], C[1], C[2], C[3]});
@@ -108,12 +114,12 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
       for (const auto& b : m.bonds) sphere_idx.push_back(b[0]);
       sphere_consts = &m.constants;
     } else if (m.type == smd::MOL_BOUNDARY || m.type == smd::MOL_FLOATING_BASE || m.type == smd::MOL_ZTORQUE ||
-               m.type == smd::MOL_ZPOWERPOTENTIAL) {
+               m.type == smd::MOL_ZPOWERPOTENTIAL || m.type == smd::MOL_BALL) {
       field_terms(m, S.type, field_idx, field_c);
     } else if (m.type != smd::MOL_SOLID) {
       std::cout << "Error(MD): molecule type " << m.type
                 << " is not on the GPU step of this build (supported: CHAIN, BOND, BEND, BEAD, BOUNDARY, "
-                   "FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL)\n";
+                   "FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL, BALL)\n";
       return 1;
     }
   }

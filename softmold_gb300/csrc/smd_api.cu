@@ -490,10 +490,16 @@ int validate(const smd_system_desc& d, std::string& why) {
   if (d.n_fields > 0 && (!d.fields || !d.field_consts)) return why = "null field array in descriptor", 1;
   for (int k = 0; k < d.n_fields; ++k) {
     const int kind = d.fields[3 * k], a = d.fields[3 * k + 1], b = d.fields[3 * k + 2];
-    if (kind != 11 && kind != 15 && kind != 16 && kind != 17)
-      return why = "field term kind must be 11, 15, 16 or 17 (BOUNDARY, FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL)", 1;
-    if (a < 0 || a >= d.n || (kind == 16 ? (b < 0 || b >= d.n || b == a) : b != -1))
+    if (kind != 11 && kind != 15 && kind != 16 && kind != 17 && kind != 19)
+      return why = "field term kind must be 11, 15, 16, 17 or 19 (BOUNDARY, FLOATING_BASE, ZTORQUE, "
+                   "ZPOWERPOTENTIAL, BALL)", 1;
+    const bool pair = (kind == 16 || kind == 19);
+    if (a < 0 || a >= d.n || (pair ? (b < 0 || b >= d.n || b == a) : b != -1))
       return why = "field term bead index out of range", 1;
+    if (kind == 19) {
+      const double own = d.field_consts[8 * k + 2];
+      if (!(own >= 0 && own < d.n && own == (double)(int)own)) return why = "BALL term's own first bead out of range", 1;
+    }
     if (kind == 11 && !(d.field_consts[8 * k] == 0 || d.field_consts[8 * k] == 1 || d.field_consts[8 * k] == 2))
       return why = "BOUNDARY dimension must be 0, 1 or 2", 1;
   }
@@ -672,6 +678,10 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     for (int k = 0; k < d.n_fields; ++k) {
       std::array<double, kFieldConst> c;
       for (int q = 0; q < kFieldConst; ++q) c[q] = d.field_consts[kFieldConst * k + q];
+      const int kind = d.fields[3 * k], a = bead + d.fields[3 * k + 1];
+      const int tk = kind == 11 ? kTermBoundary
+                     : (kind == 15 ? kTermFloating : (kind == 16 ? kTermZTorque : (kind == 19 ? kTermBall : kTermZPower)));
+      if (tk == kTermBall) c[2] += bead;  // the potential's own first bead, a global index like the others
       int set = -1;
       for (size_t q = 0; q < fsets.size() && set < 0; ++q)
         if (fsets[q] == c) set = (int)q;
@@ -680,9 +690,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
         fsets.push_back(c);
         set = (int)fsets.size() - 1;
       }
-      const int kind = d.fields[3 * k], a = bead + d.fields[3 * k + 1];
-      const int tk = kind == 11 ? kTermBoundary : (kind == 15 ? kTermFloating : (kind == 16 ? kTermZTorque : kTermZPower));
-      if (tk == kTermZTorque) {
+      if (tk == kTermZTorque || tk == kTermBall) {
         const int b = bead + d.fields[3 * k + 2];
         bead_terms[a].push_back(make_int4(term_pack(tk, 0, set), a, b, -1));
         bead_terms[b].push_back(make_int4(term_pack(tk, 1, set), a, b, -1));

@@ -33,7 +33,8 @@ constexpr int kFieldConst = 8;    // constants per external-field term set
 enum TermKind {
   kTermBond = 0, kTermBend = 1,        // BOND {first, second}, BEND {first, second, third}
   kTermBoundary = 2, kTermFloating = 3, // BOUNDARY {bead}, FLOATING_BASE {bead}
-  kTermZTorque = 4, kTermZPower = 5     // ZTORQUE {first, second}, ZPOWERPOTENTIAL {bead}
+  kTermZTorque = 4, kTermZPower = 5,    // ZTORQUE {first, second}, ZPOWERPOTENTIAL {bead}
+  kTermBall = 6                         // BALL {centre, second}
 };
 __host__ __device__ inline int term_pack(int kind, int role, int set) { return kind | (role << 3) | (set << 5); }
 __host__ __device__ inline int term_kind(int x) { return x & 7; }

@@ -1321,13 +1321,13 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
 }
 
 // ---------------------------------------------------------------- external fields
-// BOUNDARY, FLOATING_BASE, ZTORQUE and ZPOWERPOTENTIAL residues, in FP64 in
-// both forms (steep walls; few beads), with the reference's formulas and
+// BOUNDARY, FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL and BALL residues, in FP64
+// in both forms (steep walls; few beads), with the reference's formulas and
 // quirks (boundaryF/P, floatingBaseForce/Potential, zTorqueForce/Potential,
-// zPowerForce/Potential, include/MD.h:458-617, 1116-1154).  A bead's own
+// zPowerForce/Potential, harmonicHalfF/P, include/MD.h:458-617, 1116-1222).  A bead's own
 // terms read its master position (before this thread moves it); the two
-// beads of a ZTORQUE term read the current mirror, which no thread writes
-// during the step, so both see the same bond.
+// beads of a ZTORQUE or BALL term read the current mirror, which no thread
+// writes during the step, so both see the same bond.
 template <bool MIXED>
 __device__ __forceinline__ Vec3<double> mirror_pos(const DevPtrs& P, int cur, int s, const double box[3]) {
   if constexpr (MIXED) {
@@ -1371,6 +1371,21 @@ __device__ __noinline__ void field_force(const DevPtrs& P, int cur, int i, const
                                          Vec3<double>& ff) {
   const double* c = P.tab->fieldD[term_set(t.x)];
   const int kind = term_kind(t.x);
+  if (kind == kTermBall) {  // harmonicHalfF: pushes the centre and the bead apart inside r0
+    Vec3<double> d;
+    double z;
+    ztorque_bond<MIXED>(P, cur, t.y, t.z, box, d, z);
+    double dr = d.x * d.x + d.y * d.y + d.z * d.z;
+    if (dr < c[0] * c[0]) {
+      dr = sqrt(dr);
+      const double m = -(dr - c[0]) * c[1] / dr;
+      const double sg = term_role(t.x) == 0 ? 1.0 : -1.0;
+      ff.x += sg * (d.x * m);
+      ff.y += sg * (d.y * m);
+      ff.z += sg * (d.z * m);
+    }
+    return;
+  }
   if (kind == kTermZTorque) {
     Vec3<double> d;
     double z;
@@ -1418,6 +1433,15 @@ template <bool MIXED>
 __device__ __noinline__ double field_potential(const DevPtrs& P, int cur, int i, const int4 t, const double box[3]) {
   const double* c = P.tab->fieldD[term_set(t.x)];
   const int kind = term_kind(t.x);
+  if (kind == kTermBall) {  // between the bond's own first bead (constant 2) and the second
+    Vec3<double> d;
+    double z;
+    ztorque_bond<MIXED>(P, cur, (int)c[2], t.z, box, d, z);
+    double dr = d.x * d.x + d.y * d.y + d.z * d.z;
+    if (!(dr < c[0] * c[0])) return 0.0;
+    dr = sqrt(dr) - c[0];
+    return 0.5 * c[1] * dr * dr;
+  }
   if (kind == kTermZTorque) {
     Vec3<double> d;
     double z;

@@ -114,7 +114,9 @@ def add_fields(path, seed):
                           type; type 0 carries a nonzero first constant, which
                           the reference's potential subtracts from z);
       ZTORQUE 16          over every lipid chain, cut off at the midplane;
-      ZPOWERPOTENTIAL 17  on the first 300 beads.
+      ZPOWERPOTENTIAL 17  on the first 300 beads;
+      BALL 19             a soft ball of radius 1.5 around one top head, bonded
+                          to the beads within 2 sigma of it.
     """
     m = smd.read_mpd(path)
     z = m.pos[:, 2]
@@ -127,16 +129,24 @@ def add_fields(path, seed):
     fb[0] = [1.0, 2.0, 0.1, 0.01, 0.0, 0.01]
     fb[2] = [zc - 2.0, zc + 1.0, 0.5, 0.05, 0.0, 0.02]
     n = len(m.type)
+    # BALL: a soft exclusion ball of radius 1.5 around one top head, tethered
+    # to the beads within 2 sigma of it
+    centre = int(top[0])
+    dc = m.pos - m.pos[centre]
+    dc -= m.box * np.round(dc / m.box)
+    rc_ = np.sqrt((dc ** 2).sum(1))
+    ball = [int(k) for k in np.flatnonzero((rc_ < 2.0) & (np.arange(n) != centre))]
     blocks = ["11\t%d\n2 %.17g 0 0.5\n" % (len(top), wall) + "".join(f"{b}\n" for b in top),
               "15\t%d\n" % len(bottom) + " ".join(f"{x:.17g}" for x in fb.ravel()) + "\n" +
               "".join(f"{b}\n" for b in bottom),
               "16\t1\n2 1 1 %.17g\n0 %d 3\n" % (zc, n // 3),
-              "17\t1\n-0.01 2.1\n0 300\n"]
+              "17\t1\n-0.01 2.1\n0 300\n",
+              "19\t%d\n1.5 20\n" % len(ball) + "".join(f"{centre} {b}\n" for b in ball)]
     lines = open(path).read().split("\n")
     k = next(i for i, ln in enumerate(lines) if ln.strip() == "molecule")
     lines = lines[:k + 4] + "".join(blocks).rstrip("\n").split("\n") + lines[k + 4:]
     text = "\n".join(lines)
-    text = re.sub(r"nMolecules (\d+)", lambda mm: f"nMolecules {int(mm.group(1)) + 4}", text)
+    text = re.sub(r"nMolecules (\d+)", lambda mm: f"nMolecules {int(mm.group(1)) + 5}", text)
     open(path, "w").write(text)
     return len(top), len(bottom)
 

@@ -66,6 +66,9 @@ class Oracle:
         L.orc_ztorque_force.argtypes = [D, D, C.c_int, I, D, D]
         L.orc_ztorque_potential.argtypes = [D, D, C.c_int, I, D]
         L.orc_ztorque_potential.restype = C.c_double
+        L.orc_ball_force.argtypes = [D, D, C.c_int, I, D, D]
+        L.orc_ball_potential.argtypes = [D, D, C.c_int, I, D]
+        L.orc_ball_potential.restype = C.c_double
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_threads(1)
         L.orc_md_run.argtypes = [C.c_char_p, C.c_int]
@@ -122,6 +125,8 @@ class Oracle:
                                                _d(c), a)
             elif kind == 16:
                 self.L.orc_ztorque_force(pos.ctypes.data_as(D), _d(g["box"]), len(idx) // 3, _i(idx), _d(c), a)
+            elif kind == 19:
+                self.L.orc_ball_force(pos.ctypes.data_as(D), _d(g["box"]), len(idx) // 2, _i(idx), _d(c), a)
             else:
                 self.L.orc_zpower_force(pos.ctypes.data_as(D), len(idx) // 2, _i(idx), _d(c), a)
         return acc
@@ -132,7 +137,8 @@ class Oracle:
         into residue calls: runs of one kind, with the index lists and
         constants the oracle's residue functions take (FLOATING_BASE: 6 per
         type, slot 0 starting with the potential's z offset; ZTORQUE: one
-        one-bond chain {l, 1, 3} per term; ZPOWERPOTENTIAL: {k, 1} per term)."""
+        one-bond chain {l, 1, 3} per term; ZPOWERPOTENTIAL: {k, 1} per term;
+        BALL: the residue's bonds)."""
         f = g.get("fields")
         if f is None or len(f) == 0:
             return []
@@ -155,6 +161,8 @@ class Oracle:
                 c[0] = cs[0, 6]
             elif kind == 16:
                 idx, c = np.stack([run[:, 1], np.ones(len(run), int), np.full(len(run), 3)], 1).ravel(), cs[0, :4]
+            elif kind == 19:  # bonds {own first (constant 2), second}
+                idx, c = np.stack([cs[:, 2].astype(int), run[:, 2]], 1).ravel(), cs[0, :2]
             else:
                 idx, c = np.stack([run[:, 1], np.ones(len(run), int)], 1).ravel(), cs[0, :2]
             out.append((kind, np.ascontiguousarray(idx, np.int32), np.ascontiguousarray(c, np.float64)))
@@ -207,6 +215,9 @@ class Oracle:
                 elif kind == 16:
                     bonded += self.L.orc_ztorque_potential(pos.ctypes.data_as(D), _d(g["box"]), len(idx) // 3,
                                                            _i(idx), _d(c))
+                elif kind == 19:
+                    bonded += self.L.orc_ball_potential(pos.ctypes.data_as(D), _d(g["box"]), len(idx) // 2,
+                                                        _i(idx), _d(c))
                 else:
                     bonded += self.L.orc_zpower_potential(pos.ctypes.data_as(D), len(idx) // 2, _i(idx), _d(c))
         bead = 0.0

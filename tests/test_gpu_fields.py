@@ -1,11 +1,13 @@
-"""External-field residues on the GPU: BOUNDARY, FLOATING_BASE, ZTORQUE and
-ZPOWERPOTENTIAL (Blob::doBoundaryForce, doFloatingBaseForce, doZTorqueForce,
-doZPowerForce and their potentials, include/system.h:2335-2447, 2583-2716,
-3138-3151; the formulas in include/MD.h:458-617, 1116-1154).
+"""External-field residues on the GPU: BOUNDARY, FLOATING_BASE, ZTORQUE,
+ZPOWERPOTENTIAL and BALL (Blob::doBoundaryForce, doFloatingBaseForce,
+doZTorqueForce, doZPowerForce, doBallForce and their potentials,
+include/system.h:1937-1971, 2335-2447, 2583-2779, 3138-3151; the formulas in
+include/MD.h:458-617, 1116-1222).
 
 field400 is a relaxed 400-lipid bilayer carrying one residue of each kind:
 a wall above the top heads, a z well on the bottom heads, a torque on every
-chain's first bond below the midplane and a z power law on 300 beads.  Its
+chain's first bond below the midplane, a z power law on 300 beads and a
+soft ball around one head.  Its
 forces and energies were dumped from the reference's own code; field200 is
 a 48-step reference MD run with the same residues.  The reference's
 barostat adds no size-change term for these residues, so dU is that of the
@@ -33,7 +35,7 @@ FIELD = os.path.join(GOLDEN, "field200")
 def test_field_forces_against_reference(built, precision):
     g = load_golden("field400")
     kinds, counts = np.unique(g["fields"][:, 0], return_counts=True)
-    assert list(kinds) == [11, 15, 16, 17] and counts.min() > 100
+    assert list(kinds) == [11, 15, 16, 17, 19] and counts[:4].min() > 100 and counts[4] > 20
     s = smd.System(mpd_from_golden(g), precision=precision)
     scale = np.abs(g["force"]).max()
     f = s.forces()
@@ -96,7 +98,7 @@ def test_md_executable_with_fields(built, tmp_path, precision):
     assert r.returncode == 0, r.stdout + r.stderr
     assert set(os.listdir(tmp_path)) == set(json.load(open(os.path.join(FIELD, "digests.json"))))
     first = open(tmp_path / "potential_fld.dat").readline().split()
-    assert first[0] == "0" and abs(float(first[1]) - (-13155.1)) < 0.1
+    assert first[0] == "0" and abs(float(first[1]) - (-13109.1)) < 0.1
 
 
 def test_fields_batched_as_alone(built):
