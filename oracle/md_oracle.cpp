@@ -130,6 +130,9 @@ struct OracleMD {
       } else if (m.type == smd::MOL_BALL) {
         const std::vector<int> L = column(m, 2);
         orc_ball_force(pos(), sys.size, (int)m.bonds.size(), L.data(), m.constants.data(), acc.data());
+      } else if (m.type == smd::MOL_NANOCORE) {
+        const std::vector<int> L = column(m, 1);
+        orc_nanocore_force(N, pos(), sys.size, (int)L.size(), L.data(), m.constants.data(), acc.data());
       } else if (m.type == smd::MOL_SOLID) {
       } else {
         err = "molecule type " + std::to_string(m.type) + " is not supported";
@@ -140,6 +143,14 @@ struct OracleMD {
   }
   void bead_mass_divide() {
     for (const smd::Molecule& m : sys.mol) {
+      if (m.type == smd::MOL_NANOCORE) {  // each core by its own 4 pi R^2 (MD.cpp:291-303)
+        for (int j = (int)m.bonds.size() - 1; j >= 0; --j) {
+          const double R = m.constants[22 * j + smd::kBeadRadius];
+          const double mass = (4.0) * M_PI * R * R;
+          for (int d = 0; d < 3; ++d) acc[3 * m.bonds[j][0] + d] /= mass;
+        }
+        continue;
+      }
       if (m.type != smd::MOL_BEAD) continue;
       const double R = m.constants[smd::kBeadRadius];
       const double mass = (4.0) * M_PI * R * R;
@@ -198,6 +209,12 @@ struct OracleMD {
         pot += orc_zpower_potential(pos(), (int)m.bonds.size(), column(m, 2).data(), m.constants.data());
       } else if (m.type == smd::MOL_BALL) {
         pot += orc_ball_potential(pos(), sys.size, (int)m.bonds.size(), column(m, 2).data(), m.constants.data());
+      } else if (m.type == smd::MOL_NANOCORE) {
+        const std::vector<int> L = column(m, 1);
+        const double bp = orc_nanocore_potential(N, pos(), sys.size, (int)L.size(), L.data(), m.constants.data());
+        *beadPot += bp;
+        pot += bp;
+        ++*nBeadRes;
       }
     }
     return pot;

@@ -9,7 +9,7 @@
 //   pair_force.f64   N*3 accelerations from CellOpt::computeForce alone
 //   force.f64        N*3 from computeForce + every residue's do*Force
 //   energy.f64       [pair U, bonded U (CHAIN, BOND, BEND and the external-field
-//                     residues), bead U, then for each scale s_k:
+//                     residues), bead U (BEAD and NANOCORE), then for each scale s_k:
 //                     pair dU(s_k), bonded dU(s_k), bead dU(s_k)]
 //   rand53.f64       first 4096 MTRand(seed).rand53() draws
 // Run with OMP_NUM_THREADS=1 so traversal and summation orders are serial.
@@ -127,6 +127,7 @@ int main(int argc, char** argv) {
       case ZTORQUE: System.doZTorqueForce(k); break;
       case ZPOWERPOTENTIAL: System.doZPowerForce(k); break;
       case BALL: System.doBallForce(k); break;
+      case NANOCORE: System.doNanoCoreForce(k); break;
       default: break;
     }
   }
@@ -152,6 +153,7 @@ int main(int argc, char** argv) {
       case ZTORQUE: bonded += System.doZTorquePotential(k); break;
       case ZPOWERPOTENTIAL: bonded += System.doZPowerPotential(k); break;
       case BALL: bonded += System.doBallPotential(k); break;
+      case NANOCORE: bead += System.doNanoCorePotential(k); break;
       default: break;
     }
   }

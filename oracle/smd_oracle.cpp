@@ -1029,4 +1029,46 @@ double orc_ball_potential(const double* pos, const double box[3], int nb, const 
   return total;
 }
 
+
+void orc_nanocore_force(int n, const double* pos, const double box[3], int nb, const int* idx, const double* C,
+                        double* acc) {
+  for (int j = 0; j < nb; ++j) {
+    const int f = idx[j];
+    const double* Cj = C + 22 * j;
+    const double cutoffRad = Cj[0];
+    const double cut2 = cutoffRad * cutoffRad;
+    double ax = 0, ay = 0, az = 0;
+    for (int k = 0; k < n; ++k) {
+      if (k == f) continue;
+      const V3 d = diff(pos, f, k, box);
+      V3 ab{0, 0, 0};
+      V3 a2 = accv(acc, k);
+      bead_force_fn(d, ab, a2, Cj, cut2);
+      setv(acc, k, a2);
+      ax += ab.x;
+      ay += ab.y;
+      az += ab.z;
+    }
+    acc[3 * f] += ax;
+    acc[3 * f + 1] += ay;
+    acc[3 * f + 2] += az;
+  }
+}
+
+double orc_nanocore_potential(int n, const double* pos, const double box[3], int nb, const int* idx,
+                              const double* C) {
+  double potential = 0;
+  for (int j = 0; j < nb; ++j) {
+    const int f = idx[j];
+    const double* Cj = C + 22 * j;
+    const double cutoffRad = Cj[0];
+    const double cut2 = cutoffRad * cutoffRad;
+    for (int k = 0; k < n; ++k) {
+      if (k == f) continue;
+      potential += bead_potential_fn(diff(pos, f, k, box), Cj, cut2);
+    }
+  }
+  return potential;
+}
+
 }  // extern "C"

@@ -123,6 +123,15 @@ double orc_ztorque_potential(const double* pos, const double box[3], int nb, con
 void orc_ball_force(const double* pos, const double box[3], int nb, const int* bonds, const double* c, double* acc);
 double orc_ball_potential(const double* pos, const double box[3], int nb, const int* bonds, const double* c);
 
+// NANOCORE: cores idx[nb], 22 constants per core C[22*nb]: each core against
+// every other bead (other cores included) with its own constants, brute force
+// as the reference does below 50 cores (Blob::doNanoCoreForce /
+// doNanoCorePotential, include/system.h:2216-2263, 3029-3073).
+void orc_nanocore_force(int n, const double* pos, const double box[3], int nb, const int* idx, const double* C,
+                        double* acc);
+double orc_nanocore_potential(int n, const double* pos, const double box[3], int nb, const int* idx,
+                              const double* C);
+
 // Runs the reference MD loop on <name>.mpd exactly as `MD <name>` does
 // (MD.cpp:72-755) with `threads` OpenMP threads (1 reproduces the reference's
 // single-thread random streams).  Returns 0 on success.

@@ -185,6 +185,9 @@ class Mpd:
     # constants each
     fields: np.ndarray | None = None        # (k,3)
     field_consts: np.ndarray | None = None  # (k,8)
+    # NANOCORE residue: core bead indices and 22 constants per core
+    core_index: np.ndarray | None = None    # (k,)
+    core_consts: np.ndarray | None = None   # (k,22)
 
 
 def read_mpd(path: str) -> Mpd:
@@ -199,6 +202,7 @@ def read_mpd(path: str) -> Mpd:
     bond_l, bond_c, bend_l, bend_c = [], [], [], []
     sph_idx, sph_c = None, None
     field_l, field_c = [], []
+    core_idx, core_c = None, None
     fc = uc = None
 
     def take(k=1):
@@ -262,6 +266,9 @@ def read_mpd(path: str) -> Mpd:
                     sph_c = c
                 elif mt in (11, 15, 16, 17, 19):
                     field_terms(mt, b, c, typ, field_l, field_c)
+                elif mt == 18:
+                    core_idx = b[:, 0].astype(np.int32)
+                    core_c = c.reshape(nb, 22)
         elif kw == "banana":
             pass
         elif kw == "solventGamma":
@@ -286,7 +293,8 @@ def read_mpd(path: str) -> Mpd:
                bends=np.array(bend_l, np.int32).reshape(-1, 3) if bend_l else None,
                bend_consts=np.array(bend_c, np.float64).reshape(-1, 2) if bend_c else None,
                fields=np.array(field_l, np.int32).reshape(-1, 3) if field_l else None,
-               field_consts=np.array(field_c, np.float64).reshape(-1, 8) if field_c else None)
+               field_consts=np.array(field_c, np.float64).reshape(-1, 8) if field_c else None,
+               core_index=core_idx, core_consts=core_c)
 
 
 def field_terms(mt, b, c, typ, out_l, out_c):

@@ -54,4 +54,6 @@ def mpd_from_golden(g):
                    bends=g["bends"].astype(np.int32) if len(g.get("bends", [])) else None,
                    bend_consts=g["bend_consts"] if len(g.get("bends", [])) else None,
                    fields=g["fields"].astype(np.int32) if len(g.get("fields", [])) else None,
-                   field_consts=g["field_consts"] if len(g.get("fields", [])) else None)
+                   field_consts=g["field_consts"] if len(g.get("fields", [])) else None,
+                   core_index=g["core_index"].astype(np.int32) if len(g.get("core_index", [])) else None,
+                   core_consts=g["core_consts"] if len(g.get("core_index", [])) else None)

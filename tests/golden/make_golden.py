@@ -151,6 +151,56 @@ def add_fields(path, seed):
     return len(top), len(bottom)
 
 
+def to_nanocore(path, sep):
+    """Turns the BEAD residue of a vesicle-and-sphere .mpd into a NANOCORE
+    residue of two cores (molecule block `18 nBond / 22 constants per core /
+    indices`): the sphere bead and a new bead of its type `sep` sigma from it,
+    tangent to the vesicle, both with the sphere-head row of the BEAD table
+    (the row applies to every partner type)."""
+    m = smd.read_mpd(path)
+    s0 = int(m.sphere_index[0])
+    ts, nT = int(m.type[s0]), m.n_types
+    row = m.sphere_consts[22 * (ts * nT + 2):22 * (ts * nT + 2) + 22]
+    centre = m.pos[np.arange(len(m.type)) != s0].mean(0)
+    r = m.pos[s0] - centre
+    t = np.cross(r, [0.0, 0.0, 1.0]) if abs(r[2]) < 0.9 * np.linalg.norm(r) else np.cross(r, [1.0, 0.0, 0.0])
+    p2 = m.pos[s0] + sep * t / np.linalg.norm(t)
+    n = len(m.type)
+    tok = open(path).read().split("\n")
+    out, i = [], 0
+    while i < len(tok):
+        ln = tok[i]
+        key = ln.strip()
+        if key.startswith("nParticles"):
+            out.append(f"nParticles {n + 1} ")
+        elif key == "positions":
+            out.extend(tok[i:i + 1 + n])
+            out.append(" %d %.15g %.15g %.15g" % (ts, *p2))
+            i += n + 1
+            continue
+        elif key == "velocities":
+            out.extend(tok[i:i + 1 + n])
+            out.append(" 0 0 0")
+            i += n + 1
+            continue
+        elif key.split() == ["9", "1"] or key.startswith("9\t"):
+            # the BEAD block: header, its 22 nT^2 constants and one index
+            out.append("18\t2")
+            out.append(" " + " ".join("%.17g" % x for x in np.concatenate([row, row])))
+            out.append(f" {s0}")
+            out.append(f" {n}")
+            vals = 0
+            i += 1
+            while vals < 22 * nT * nT + 1:
+                vals += len(tok[i].split())
+                i += 1
+            continue
+        else:
+            out.append(ln)
+        i += 1
+    open(path, "w").write("\n".join(out))
+
+
 def run_ref_md(workdir, name):
     env = dict(os.environ, OMP_NUM_THREADS="1")
     subprocess.run([os.path.join(REF, "MD"), name], cwd=workdir, env=env, check=True,
@@ -180,6 +230,8 @@ def dump_case(workdir, name, out_name):
         bend_consts=m.bend_consts if m.bend_consts is not None else np.zeros((0, 2)),
         fields=m.fields if m.fields is not None else np.zeros((0, 3), np.int32),
         field_consts=m.field_consts if m.field_consts is not None else np.zeros((0, 8)),
+        core_index=m.core_index if m.core_index is not None else np.zeros(0, np.int32),
+        core_consts=m.core_consts if m.core_consts is not None else np.zeros((0, 22)),
         keys=rd("keys.i32", np.int32), pairs=rd("pairs.i32", np.int32).reshape(-1, 2),
         pair_force=rd("pair_force.f64", np.float64).reshape(n, 3),
         force=rd("force.f64", np.float64).reshape(n, 3),
@@ -209,10 +261,38 @@ def make_fields(tmp):
               open(os.path.join(fdir, "digests.json"), "w"), indent=1)
 
 
+def make_nanocore(tmp):
+    """core300 (a 300-lipid vesicle with a NANOCORE residue of two cores,
+    0.8 sigma outside its heads and 3.9 sigma apart, at the edge of each other's
+    well) and core200/ (a 48-step reference MD run of a 200-lipid one)."""
+    smd.synth_vesicle_sphere(os.path.join(tmp, "core.mpd"), 99, 300, 3.45, 40.0, 3.0, -10.0, 300.0, 0.8, 100.0)
+    to_nanocore(os.path.join(tmp, "core.mpd"), 3.9)
+    dump_case(tmp, "core", "core300")
+    cdir = os.path.join(HERE, "core200")
+    os.makedirs(cdir, exist_ok=True)
+    smd.synth_vesicle_sphere(os.path.join(cdir, "core.mpd"), 8, 200, 3.45, 36.0, 3.0, -10.0, 300.0, 0.8, 100.0)
+    to_nanocore(os.path.join(cdir, "core.mpd"), 3.9)
+    set_run(os.path.join(cdir, "core.mpd"), 0.96, 0.48, 0.16)
+    run_dir = os.path.join(tmp, "corerun")
+    os.makedirs(run_dir)
+    shutil.copy(os.path.join(cdir, "core.mpd"), run_dir)
+    run_ref_md(run_dir, "core")
+    json.dump({os.path.basename(f): hashlib.sha256(open(f, "rb").read()).hexdigest()
+               for f in sorted(glob.glob(os.path.join(run_dir, "*")))},
+              open(os.path.join(cdir, "digests.json"), "w"), indent=1)
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "ref_dump")):
         sys.exit("oracle/_ref is missing: run oracle/build_ref.sh first")
     tmp = tempfile.mkdtemp(prefix="smd_golden_")
+    if "--only-nanocore" in sys.argv:  # the NANOCORE fixtures alone
+        try:
+            make_nanocore(tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        print("nanocore fixtures written to", HERE)
+        return
     if "--only-fields" in sys.argv:  # the external-field fixtures alone
         try:
             make_fields(tmp)
@@ -291,6 +371,7 @@ def main():
                              sha256=hashlib.sha256(open(os.path.join(d, "g.mpd"), "rb").read()).hexdigest()))
         json.dump(gens, open(os.path.join(HERE, "generators.json"), "w"), indent=1)
         make_fields(tmp)
+        make_nanocore(tmp)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     print("golden fixtures written to", HERE)

@@ -69,6 +69,9 @@ class Oracle:
         L.orc_ball_force.argtypes = [D, D, C.c_int, I, D, D]
         L.orc_ball_potential.argtypes = [D, D, C.c_int, I, D]
         L.orc_ball_potential.restype = C.c_double
+        L.orc_nanocore_force.argtypes = [C.c_int, D, D, C.c_int, I, D, D]
+        L.orc_nanocore_potential.argtypes = [C.c_int, D, D, C.c_int, I, D]
+        L.orc_nanocore_potential.restype = C.c_double
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_threads(1)
         L.orc_md_run.argtypes = [C.c_char_p, C.c_int]
@@ -116,6 +119,10 @@ class Oracle:
         if si is not None and len(si):
             self.L.orc_bead_force(len(pos), pos.ctypes.data_as(D), typ.ctypes.data_as(I), _d(g["box"]), nT,
                                   len(si), _i(si), _d(g["sphere_consts"]), acc.ctypes.data_as(D))
+        ci = g.get("core_index")
+        if ci is not None and len(ci):
+            self.L.orc_nanocore_force(len(pos), pos.ctypes.data_as(D), _d(g["box"]), len(ci), _i(ci),
+                                      _d(np.ascontiguousarray(g["core_consts"]).ravel()), acc.ctypes.data_as(D))
         for kind, idx, c in self._field_residues(g):
             a = acc.ctypes.data_as(D)
             if kind == 11:
@@ -226,6 +233,10 @@ class Oracle:
             a = (len(pos), pos.ctypes.data_as(D), typ.ctypes.data_as(I), _d(g["box"]), nT, len(si), _i(si),
                  _d(g["sphere_consts"]))
             bead = self.L.orc_bead_potential(*a) if scale is None else self.L.orc_bead_dpotential(*a, _d(scale))
+        ci = g.get("core_index")
+        if ci is not None and len(ci) and scale is None:  # the reference drops its size-change term
+            bead += self.L.orc_nanocore_potential(len(pos), pos.ctypes.data_as(D), _d(g["box"]), len(ci), _i(ci),
+                                                  _d(np.ascontiguousarray(g["core_consts"]).ravel()))
         return pair, bonded, bead
 
 

@@ -18,14 +18,16 @@ from conftest import GOLDEN
 TRAJ = os.path.join(GOLDEN, "traj_bil")
 NET = os.path.join(GOLDEN, "net200")
 FIELD = os.path.join(GOLDEN, "field200")
+CORE = os.path.join(GOLDEN, "core200")
 
 
 @pytest.mark.skipif(platform.machine() != "x86_64", reason="digests are of x86-64 glibc number formatting")
-@pytest.mark.parametrize("where,name", [(TRAJ, "bil"), (NET, "net"), (FIELD, "fld")])
+@pytest.mark.parametrize("where,name", [(TRAJ, "bil"), (NET, "net"), (FIELD, "fld"), (CORE, "core")])
 def test_md_oracle_matches_reference_outputs(oracle, tmp_path, where, name):
     """traj_bil: CHAIN lipids, barostat on; net200: the same with BOND and
     BEND residues over the heads; field200: with one residue of each
-    external-field kind (BOUNDARY, FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL)."""
+    external-field kind (BOUNDARY, FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL,
+    BALL); core200: a vesicle with a two-core NANOCORE residue."""
     from oracle_binding import MD
     shutil.copy(os.path.join(where, name + ".mpd"), tmp_path)
     env = dict(os.environ, OMP_NUM_THREADS="1")
