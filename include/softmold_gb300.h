@@ -74,6 +74,12 @@ typedef struct smd_system_desc {
                                    bond (l, l+1) (doZTorqueForce); ZPOWERPOTENTIAL {c0, c1} (doZPowerForce);
                                    BALL {r0, k, the bond's own first bead} with first = the residue's
                                    first bond's first bead (doBallForce / doBallPotential) */
+  int sphere_nanocore;          /* 1: the sphere beads form a NANOCORE residue (Blob::doNanoCoreForce):
+                                   sphere_consts holds 22 constants per bead, each bead acts on every
+                                   other bead (other cores included) with its own row and has the mass
+                                   4 pi R^2 of its own radius, divided once a step
+                                   (MD.cpp:291-303, 495-507); no sphere-sphere term,
+                                   no size-change term */
 } smd_system_desc;
 
 typedef struct smd_system smd_system;

@@ -43,6 +43,7 @@ class SystemDesc(C.Structure):
         ("n_bonds", C.c_int), ("bonds", C.POINTER(C.c_int)), ("bond_consts", C.POINTER(C.c_double)),
         ("n_bends", C.c_int), ("bends", C.POINTER(C.c_int)), ("bend_consts", C.POINTER(C.c_double)),
         ("n_fields", C.c_int), ("fields", C.POINTER(C.c_int)), ("field_consts", C.POINTER(C.c_double)),
+        ("sphere_nanocore", C.c_int),
     ]
 
 
@@ -349,9 +350,16 @@ class System:
                         uc=np.ascontiguousarray(m.uconst, np.float64),
                         cb=np.ascontiguousarray(m.chain_blocks, np.int32),
                         cc=np.ascontiguousarray(m.chain_consts, np.float64))
-            if m.sphere_index is not None and len(m.sphere_index) > 0:
+            has_bead = m.sphere_index is not None and len(m.sphere_index) > 0
+            has_core = m.core_index is not None and len(m.core_index) > 0
+            if has_bead and has_core:
+                raise SmdError("a BEAD and a NANOCORE residue in one system are not on the GPU step of this build")
+            if has_bead:
                 arrs["si"] = np.ascontiguousarray(m.sphere_index, np.int32)
                 arrs["sc"] = np.ascontiguousarray(m.sphere_consts, np.float64)
+            elif has_core:
+                arrs["si"] = np.ascontiguousarray(m.core_index, np.int32)
+                arrs["sc"] = np.ascontiguousarray(np.asarray(m.core_consts, np.float64).ravel())
             self._keep.append(arrs)
             d = descs[k]
             d.n = len(m.type)
@@ -366,6 +374,7 @@ class System:
             if "si" in arrs:
                 d.n_spheres = len(arrs["si"])
                 d.sphere_index, d.sphere_consts = _ip(arrs["si"]), _dp(arrs["sc"])
+                d.sphere_nanocore = 1 if has_core else 0
             else:
                 d.n_spheres = 0
             for key, lk, ck in (("bonds", "bl", "bc"), ("bends", "el", "ec")):

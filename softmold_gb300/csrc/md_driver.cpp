@@ -90,6 +90,8 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   std::vector<int> field_idx;
   std::vector<double> field_c;
   const std::vector<double>* sphere_consts = nullptr;
+  bool nanocore = false;
+  int n_bead_res = 0;  // BEAD and NANOCORE residues: the beadPotential_ output (dataExtraction.h:1031-1040)
   for (const smd::Molecule& m : S.mol) {
     if (m.type == smd::MOL_CHAIN) {
       for (const auto& b : m.bonds) {
@@ -106,20 +108,22 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
         bend_idx.insert(bend_idx.end(), {b[0], b[1], b[2]});
         bend_c.insert(bend_c.end(), m.constants.begin(), m.constants.begin() + 2);
       }
-    } else if (m.type == smd::MOL_BEAD) {
+    } else if (m.type == smd::MOL_BEAD || m.type == smd::MOL_NANOCORE) {
       if (sphere_consts) {
-        std::cout << "Error(MD): more than one BEAD residue is not on the GPU step of this build\n";
+        std::cout << "Error(MD): more than one BEAD or NANOCORE residue is not on the GPU step of this build\n";
         return 1;
       }
       for (const auto& b : m.bonds) sphere_idx.push_back(b[0]);
       sphere_consts = &m.constants;
+      nanocore = (m.type == smd::MOL_NANOCORE);
+      ++n_bead_res;
     } else if (m.type == smd::MOL_BOUNDARY || m.type == smd::MOL_FLOATING_BASE || m.type == smd::MOL_ZTORQUE ||
                m.type == smd::MOL_ZPOWERPOTENTIAL || m.type == smd::MOL_BALL) {
       field_terms(m, S.type, field_idx, field_c);
     } else if (m.type != smd::MOL_SOLID) {
       std::cout << "Error(MD): molecule type " << m.type
-                << " is not on the GPU step of this build (supported: CHAIN, BOND, BEND, BEAD, BOUNDARY, "
-                   "FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL, BALL)\n";
+                << " is not on the GPU step of this build (supported: CHAIN, BOND, BEND, BEAD, NANOCORE, "
+                   "BOUNDARY, FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL, BALL)\n";
       return 1;
     }
   }
@@ -165,6 +169,7 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   d.n_spheres = (int)sphere_idx.size();
   d.sphere_index = sphere_idx.data();
   d.sphere_consts = sphere_consts ? sphere_consts->data() : nullptr;
+  d.sphere_nanocore = nanocore ? 1 : 0;
   d.n_bonds = (int)bond_idx.size() / 2;
   d.bonds = bond_idx.data();
   d.bond_consts = bond_c.data();
@@ -195,7 +200,8 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   const bool t0 = (S.initialTime == 0);
   if (smd_prepare(h, t0 ? 0 : 1, t0 ? &e0 : nullptr)) return die("smd_prepare");
   if (t0) {
-    obs.compute(S, S.initialTime, S.pos.data(), S.vel.data(), S.pos.data(), e0.pair + e0.bonded + e0.sphere, 0, 0);
+    obs.compute(S, S.initialTime, S.pos.data(), S.vel.data(), S.pos.data(), e0.pair + e0.bonded + e0.sphere,
+                e0.sphere, n_bead_res);
     smd::xyz_append_frame(frames, N, S.type.data(), S.pos.data(), err);
   }
   std::cerr << "starting main loop: \n";
@@ -239,7 +245,7 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
         return die("measure");
       for (int k = 0; k < 3; ++k) S.size[k] = box[k];
       obs.compute(S, S.initialTime, pos.data(), vel.data(), pos.data(), e.pair + e.bonded + e.sphere, e.sphere,
-                  0);
+                  n_bead_res);
       current = time(NULL);
       if (smd_advance(h, 0, 0)) return die("smd_advance");
       it = m + 1;

@@ -469,7 +469,7 @@ int validate(const smd_system_desc& d, std::string& why) {
     if (s < 0 || (long long)s + (long long)c * l > d.n) return why = "CHAIN block out of range", 1;
   }
   if (d.n_spheres < 0 || d.n_spheres > kMaxSpheres)
-    return why = "at most " + std::to_string(kMaxSpheres) + " BEAD beads per system", 1;
+    return why = "at most " + std::to_string(kMaxSpheres) + " BEAD or NANOCORE beads per system", 1;
   if (d.n_spheres > 0) {
     if (!d.sphere_index || !d.sphere_consts) return why = "null BEAD array in descriptor", 1;
     for (int k = 0; k < d.n_spheres; ++k) {
@@ -477,7 +477,12 @@ int validate(const smd_system_desc& d, std::string& why) {
       for (int q = 0; q < k; ++q)
         if (d.sphere_index[q] == d.sphere_index[k]) return why = "BEAD bead listed twice", 1;
     }
-    if (!(d.sphere_consts[kBeadRadiusConst] > 0)) return why = "BEAD radius must be positive", 1;
+    if (d.sphere_nanocore) {
+      for (int k = 0; k < d.n_spheres; ++k)
+        if (!(d.sphere_consts[kBeadConst * k + kBeadRadiusConst] > 0)) return why = "NANOCORE radius must be positive", 1;
+    } else if (!(d.sphere_consts[kBeadRadiusConst] > 0)) {
+      return why = "BEAD radius must be positive", 1;
+    }
   }
   if (d.n_bonds < 0 || d.n_bends < 0) return why = "negative BOND / BEND term count", 1;
   if (d.n_bonds > 0 && (!d.bonds || !d.bond_consts)) return why = "null BOND array in descriptor", 1;
@@ -540,7 +545,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   const smd_system_desc& d0 = descs[0];
   for (int r = 0; r < n_rep; ++r)
     if (n_rep > 1 && descs[r].n_spheres > 0)
-      return fail(1, "BEAD residues are supported in single-system handles, not in batches");
+      return fail(1, "BEAD and NANOCORE residues are supported in single-system handles, not in batches");
   for (int r = 1; r < n_rep; ++r) {
     const smd_system_desc& d = descs[r];
     if (d.n_types != d0.n_types || d.cutoff != d0.cutoff || d.dt != d0.dt)
@@ -647,7 +652,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
         for (int q = 0; q < l; ++q) cinfo[bead + s + c2 * l + q] = cinfo_pack(q, l, set);
     }
     for (int k = 0; k < d.n_spheres; ++k) {
-      if (cinfo[bead + d.sphere_index[k]] != 0) return fail(1, "a BEAD bead is also a CHAIN member");
+      if (cinfo[bead + d.sphere_index[k]] != 0) return fail(1, "a BEAD or NANOCORE bead is also a CHAIN member");
       cinfo[bead + d.sphere_index[k]] = (int)(0xC0000000u | (unsigned)k);
     }
     // BOND / BEND terms: per-bead entries (file order), constant sets shared
@@ -770,7 +775,8 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     return rc;
   // ---- BEAD spheres (single-system handles)
   if (d0.n_spheres > 0) {
-    const int nc = kBeadConst * d0.n_types * d0.n_types;
+    // BEAD: one row per ordered type pair; NANOCORE: one row per core
+    const int nc = d0.sphere_nanocore ? kBeadConst * d0.n_spheres : kBeadConst * d0.n_types * d0.n_types;
     double* dC = nullptr;
     float* fC = nullptr;
     if ((rc = h->alloc(&P.sph, 1)) || (rc = h->alloc(&dC, nc)) || (rc = h->alloc(&fC, nc))) return rc;
@@ -779,10 +785,17 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     SphereDev sd;
     std::memset(&sd, 0, sizeof sd);
     sd.n = d0.n_spheres;
-    for (int k = 0; k < sd.n; ++k) sd.orig[k] = d0.sphere_index[k];
+    sd.nanocore = d0.sphere_nanocore ? 1 : 0;
+    for (int k = 0; k < sd.n; ++k) {
+      sd.orig[k] = d0.sphere_index[k];
+      // its row: BEAD row 0 (constant 0 is the range, constant 4 the radius);
+      // NANOCORE its own (MD.cpp:280-303)
+      const double* C = d0.sphere_consts + (sd.nanocore ? kBeadConst * k : 0);
+      const double R = C[kBeadRadiusConst];
+      sd.mass[k] = 4.0 * M_PI * R * R;
+      sd.cut2[k] = C[0] * C[0];
+    }
     const double R = d0.sphere_consts[kBeadRadiusConst];
-    sd.mass = 4.0 * M_PI * R * R;  // MD.cpp:340-355
-    sd.cut2 = d0.sphere_consts[0] * d0.sphere_consts[0];
     sd.bb_cut2 = (R + R + 2.0) * (R + R + 2.0);
     SMD_CUDA(cudaMemcpy(P.sph, &sd, sizeof sd, cudaMemcpyHostToDevice));
     SMD_CUDA(cudaMemcpy(dC, d0.sphere_consts, nc * sizeof(double), cudaMemcpyHostToDevice));
@@ -1519,7 +1532,7 @@ int adj_load(smd_system* h, const double* xs, const double* vs, bool force) {
 int adj_check_handle(smd_system* h) {
   if (!h) return fail(1, "null handle");
   if (h->n_rep != 1) return fail(1, "the adjoint runs on single-system handles");
-  if (h->n_sph) return fail(1, "the adjoint does not cover BEAD residues");
+  if (h->n_sph) return fail(1, "the adjoint does not cover BEAD or NANOCORE residues");
   if (h->n_terms) return fail(1, "the adjoint does not cover BOND / BEND or external-field residues");
   return 0;
 }

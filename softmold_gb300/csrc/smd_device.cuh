@@ -67,16 +67,19 @@ struct RepParams {  // per replica, fixed
   int cell_begin, cell_cap;
 };
 
-// BEAD residue of a single-system handle (include/system.h:2043-2212): the
-// spheres' file-order indices, mass 4 pi R^2 (MD.cpp:340-355) and the sums of
-// the other beads' reactions on each sphere, gathered during k_integ and used
-// by k_sphere.  MIXED sums are int64 in units of 2^-32 (order-independent).
+// BEAD residue of a single-system handle (include/system.h:2043-2212), or a
+// NANOCORE residue (:2216-2263, each core with its own 22-constant row): the
+// spheres' file-order indices, masses 4 pi R^2 (MD.cpp:280-303, 340-355) and
+// the sums of the other beads' reactions on each sphere, gathered during
+// k_integ and used by k_sphere.  MIXED sums are int64 in units of 2^-32
+// (order-independent).
 struct SphereDev {
   int n;
+  int nanocore;     // 1: a NANOCORE residue (per-sphere rows, no sphere-sphere term, no dU)
   int orig[kMaxSpheres];
-  double mass;
-  double cut2;      // (R + rc)^2: bead-sphere range (row 0, constant 0)
-  double bb_cut2;   // (2R + 2)^2: sphere-sphere range
+  double mass[kMaxSpheres];   // 4 pi R^2 of each sphere
+  double cut2[kMaxSpheres];   // bead-sphere range of each sphere (its row's constant 0, squared)
+  double bb_cut2;   // (2R + 2)^2: sphere-sphere range (BEAD)
   long long fq[kMaxSpheres][3];
   double fd[kMaxSpheres][3];
 };

@@ -1246,7 +1246,10 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
   for (int s = 0; s < P.n_sph; ++s) {
     const int os = S->orig[s];
     double r[3] = {0.0, 0.0, 0.0};
-    if (active && o != os) {
+    // BEAD: a sphere bead meets the other spheres only through the
+    // sphere-sphere term (k_sphere); NANOCORE: every core is an ordinary
+    // partner of the others
+    if (active && o != os && (!me_sphere || S->nanocore)) {
       const int js = P.inv[os];
       double d[3];
       int ts;
@@ -1258,7 +1261,7 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
         const float fx = frac_delta(ms.x, mu.x, rs.len_per_frac[0]);
         const float fy = frac_delta(ms.y, mu.y, rs.len_per_frac[1]);
         const float fz = frac_delta(ms.z, mu.z, rs.len_per_frac[2]);
-        near = (fx * fx + fy * fy + fz * fz) < (float)S->cut2 * 1.001f + 0.01f;
+        near = (fx * fx + fy * fy + fz * fz) < (float)S->cut2[s] * 1.001f + 0.01f;
         if (near) {
           d[0] = frac_delta_d(ms.x, mu.x, box[0] * (1.0 / 4294967296.0));
           d[1] = frac_delta_d(ms.y, mu.y, box[1] * (1.0 / 4294967296.0));
@@ -1277,16 +1280,20 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
         near = true;
       }
       if (near) {
-        const double* row = P.sphC + kBeadConst * (ts * nT + ti);
+        const double* row = S->nanocore ? P.sphC + kBeadConst * s : P.sphC + kBeadConst * (ts * nT + ti);
+        const double cut2 = S->cut2[s];
         const double dr2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        if constexpr ((FL & F_ENERGY) != 0) e_sph += bead_pot(dr2, row, S->cut2);
+        if constexpr ((FL & F_ENERGY) != 0) e_sph += bead_pot(dr2, row, cut2);
         if constexpr ((FL & F_DU) != 0) {
-          const double e0 = d[0] * rs.scale[0], e1 = d[1] * rs.scale[1], e2 = d[2] * rs.scale[2];
-          du_sph += bead_pot(dr2, row, S->cut2) - bead_pot(e0 * e0 + e1 * e1 + e2 * e2, row, S->cut2);
+          // the reference's barostat drops the NANOCORE difference (MD.cpp:657-661)
+          if (!S->nanocore) {
+            const double e0 = d[0] * rs.scale[0], e1 = d[1] * rs.scale[1], e2 = d[2] * rs.scale[2];
+            du_sph += bead_pot(dr2, row, cut2) - bead_pot(e0 * e0 + e1 * e1 + e2 * e2, row, cut2);
+          }
         }
         if constexpr ((FL & F_ENERGY) == 0) {
-          if (!me_sphere) {
-            const double mag = bead_mag(dr2, row, S->cut2);
+          {
+            const double mag = bead_mag(dr2, row, cut2);
             for (int a = 0; a < 3; ++a) r[a] = d[a] * mag;
             fs.x -= r[0];
             fs.y -= r[1];
@@ -1315,6 +1322,20 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
             for (int a = 0; a < 3; ++a)
               if (r[a] != 0.0) atomicAdd(&S->fd[s][a], r[a]);
         }
+      }
+    }
+  }
+  // NANOCORE: a core's share of the other cores' terms (their reactions on it)
+  // joins its own sum, which k_sphere integrates
+  if constexpr ((FL & F_ENERGY) == 0) {
+    if (me_sphere && S->nanocore) {
+      const int me = P.cinfo[i] & 0xffff;
+      const double f[3] = {fs.x, fs.y, fs.z};
+      for (int a = 0; a < 3; ++a) {
+        if constexpr (MIXED)
+          atomicAdd((unsigned long long*)&S->fq[me][a], (unsigned long long)__double2ll_rn(f[a] * 4294967296.0));
+        else
+          atomicAdd(&S->fd[me][a], f[a]);
       }
     }
   }
@@ -2095,10 +2116,12 @@ __global__ void k_mc(DevPtrs P) {
 // Completes a stopped step: optional restart half-kick, optional box rescale
 // of an accepted MC move, then the next step's first half-kick and drift.
 // mode bit 0: restart half-kick (MD.cpp:300-308); bit 1: the stopped step was
-// a loop step.  A BEAD sphere's stored acceleration is its undivided force;
-// the reference divides it by the sphere mass after the forces and again
+// a loop step.  A sphere's stored acceleration is its undivided force.  The
+// reference divides a BEAD sphere's by its mass after the forces and again
 // before first() (MD.cpp:340-355, 480-509), so a first half-kick that follows
-// a second one uses a / m^2, the one of a fresh start a / m.
+// a second one uses a / m^2, the one of a fresh start a / m.  A NANOCORE
+// core is divided after the forces only (MD.cpp:291-303, 495-507): a / m
+// after a second half-kick, the undivided a at a fresh start.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBeadBlock) k_finish(DevPtrs P, int cur, int mode, int apply_mc, StepEnd se) {
   const int i = blockIdx.x * kBeadBlock + threadIdx.x;
@@ -2121,10 +2144,13 @@ __global__ void __launch_bounds__(kBeadBlock) k_finish(DevPtrs P, int cur, int m
       double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
       double af[3] = {a[0], a[1], a[2]};
       if (sphere) {
-        const double m = P.sph->mass;
+        const double m = P.sph->mass[P.cinfo[i] & 0xffff];
+        const bool core = P.sph->nanocore;
         for (int d = 0; d < 3; ++d) {
-          a[d] = a[d] / m;
-          af[d] = (mode & 3) ? a[d] / m : a[d];
+          const double a0 = a[d];
+          a[d] = a0 / m;
+          if (mode & 3) af[d] = core ? a[d] : a[d] / m;
+          else af[d] = core ? a0 : a[d];
         }
       }
       for (int d = 0; d < 3; ++d) {
@@ -2162,10 +2188,11 @@ __global__ void __launch_bounds__(kBeadBlock) k_finish(DevPtrs P, int cur, int m
   finalize_step(P, bm, se);
 }
 
-// BEAD spheres after k_integ (one warp, one sphere per lane): the total force
-// on each sphere (its non-bonded force, the reactions gathered in k_integ and
-// the sphere-sphere terms, include/system.h:2072-2098), its Langevin term,
-// the mass division of MD.cpp:480-509 and, in a loop step, both half-kicks,
+// BEAD spheres and NANOCORE cores after k_integ (one warp, one sphere per
+// lane): the total force on each sphere (its non-bonded force, the reactions
+// gathered in k_integ and the BEAD sphere-sphere terms,
+// include/system.h:2072-2098, or the cores' terms on each other), its
+// Langevin term, the mass division of MD.cpp:480-509 and, in a loop step, both half-kicks,
 // the drift and the wrap; then the step's list-rebuild decision.  The same
 // flags as k_integ select the variant.
 template <bool MIXED, int FL>
@@ -2197,7 +2224,7 @@ __global__ void __launch_bounds__(32) k_sphere(DevPtrs P, int cur, StepEnd se) {
       }
     }
     if constexpr ((FL & F_PAIRONLY) == 0) {
-      for (int t = 0; t < S->n; ++t) {
+      for (int t = 0; t < S->n && !S->nanocore; ++t) {  // BEAD sphere-sphere terms
         if (t == s) continue;
         const int jt = P.inv[S->orig[t]];
         double d[3];
@@ -2247,7 +2274,7 @@ __global__ void __launch_bounds__(32) k_sphere(DevPtrs P, int cur, StepEnd se) {
       double v[3] = {P.vx[j], P.vy[j], P.vz[j]};
       double a[3];
       for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
-      const double m = S->mass, h = rp.dt * 0.5;
+      const double m = S->mass[s], h = rp.dt * 0.5;
       if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
         P.ax[j] = a[0];
         P.ay[j] = a[1];
@@ -2263,7 +2290,8 @@ __global__ void __launch_bounds__(32) k_sphere(DevPtrs P, int cur, StepEnd se) {
         double x[3] = {P.x[j], P.y[j], P.z[j]};
         if (ti != 0) {
           for (int d = 0; d < 3; ++d) {
-            const double a1 = a[d] / m, a2 = a1 / m;
+            // the next first() half-kick: a BEAD sphere's divided again, a core's not
+            const double a1 = a[d] / m, a2 = S->nanocore ? a1 : a1 / m;
             if constexpr (MIXED) {
               v[d] = fma(a2, h, fma(a1, h, v[d]));
               x[d] = fma(v[d], rp.dt, x[d]);
