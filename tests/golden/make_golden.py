@@ -23,6 +23,12 @@ Fixtures
   field200/        a 200-lipid bilayer with the same residues and the sha256
                    of every file a 48-step reference MD run of it writes.
                    (`--only-fields` regenerates these two alone.)
+  core300.npz      a 300-lipid vesicle with a NANOCORE residue of two cores;
+  core200/         its 48-step reference MD run (`--only-nanocore`).
+  mix400.npz       a relaxed 400-lipid bilayer with 40 % of its lipids
+                   retyped HEAD2/TAIL2 over 8-type tables;
+  mix200/          a 200-lipid two-lipid bilayer's 48-step reference MD run
+                   with a temperature ramp (`--only-mixed`).
   generators.json  sha256 of the reference generators' .mpd for a few seeds.
 Inputs are seeded synthetic membranes built in the reference generators' terms
 (softmold_gb300 synth_*, byte-identical to generate/liposome and bilayer).
@@ -149,6 +155,104 @@ def add_fields(path, seed):
     text = re.sub(r"nMolecules (\d+)", lambda mm: f"nMolecules {int(mm.group(1)) + 5}", text)
     open(path, "w").write(text)
     return len(top), len(bottom)
+
+
+def mixed_tables(rc=2.0, rm=1.0):
+    """The 8-type two-body tables of a two-lipid membrane in the terms of
+    generate/continuumSphereAndBilayer.cpp:95-131 (HEAD 2, TAIL 3, HEAD2 6,
+    TAIL2 7): every pair Umin 0 / Umax 100 except the tail pairs and the
+    HEAD-HEAD2 pair (Umax 200).  TAIL-TAIL2 takes -5.5, the value
+    generate/bilayer.cpp:76-80 carries, so the cross pair differs from the
+    like pairs.  Formulas of mpd::laradjiRevaleeFC / PC."""
+    nT = 8
+    umax = np.full(nT * nT, 100.0)
+    umin = np.zeros(nT * nT)
+    for a, b, lo in ((3, 3, -6.0), (7, 7, -6.0), (7, 3, -5.5), (3, 7, -5.5), (6, 2, -6.0), (2, 6, -6.0)):
+        umin[a + b * nT], umax[a + b * nT] = lo, 200.0
+    fc, pc = [], []
+    for i in range(nT):
+        for j in range(nT):
+            g = i + j * nT
+            fc += [rm, 2.0 * (umax[g] - umin[g]) / (rm * rm), 0.0, rc,
+                   6.0 * umin[g] / ((rc - rm) ** 2), 6.0 * umin[g] / ((rc - rm) ** 3)]
+            pc += [rm, (umax[g] - umin[g]) / (rm * rm), umin[g], rc,
+                   3.0 * umin[g] / ((rc - rm) ** 2), 2.0 * umin[g] / ((rc - rm) ** 3)]
+    return np.array(fc), np.array(pc)
+
+
+def to_mixed(path, seed, frac=0.4, ramp=None):
+    """Turns a 6-type bilayer .mpd into a two-lipid one: nTypes 8 with
+    mixed_tables(), a seeded `frac` of the lipids (three-bead CHAIN members)
+    retyped HEAD2/TAIL2.  `ramp` (final temperature, step interval) adds a
+    temperature ramp.  The thermostat stays `gamma`: the reference's reader
+    stores a `gammaType` line into a vector it has not sized
+    (include/system.h:1266-1269, sized only by setGammaType, :4519-4525) and
+    crashes on it."""
+    m = smd.read_mpd(path)
+    rng = np.random.default_rng(seed)
+    n_lip = len(m.type) // 3
+    pick = np.zeros(len(m.type), bool)
+    for lip in rng.permutation(n_lip)[:int(frac * n_lip)]:
+        pick[3 * lip:3 * lip + 3] = True
+    fc, pc = mixed_tables()
+    row = lambda v: "".join(" " + " ".join("%.15g" % x for x in v[k:k + 6]) + "\n"  # noqa: E731
+                            for k in range(0, len(v), 6))
+    lines = open(path).read().split("\n")
+    out, i = [], 0
+    while i < len(lines):
+        ln = lines[i]
+        key = ln.split()[0] if ln.split() else ""
+        if key == "nTypes":
+            out.append("nTypes 8 ")
+        elif key == "finalTemp" and ramp is not None:
+            out.append("finalTemp %.15g " % ramp[0])
+        elif key in ("twoBodyFconst", "twoBodyUconst"):
+            out.append(ln)
+            out.extend(row(fc if key == "twoBodyFconst" else pc).rstrip("\n").split("\n"))
+            i += 1
+            while lines[i].strip():
+                i += 1
+            continue
+        elif key == "positions":
+            out.append(ln)
+            for b in range(len(m.type)):
+                i += 1
+                tok = lines[i].split()
+                t = int(tok[0])
+                if pick[b]:
+                    t = {2: 6, 3: 7}[t]
+                out.append(" %d %s" % (t, " ".join(tok[1:])))
+        else:
+            out.append(ln)
+        i += 1
+    text = "\n".join(out).rstrip("\n") + "\n"
+    if ramp is not None:
+        text += "tempStepInterval %.15g \n" % ramp[1]
+    open(path, "w").write(text)
+    return int(pick.sum()) // 3
+
+
+def make_mixed(tmp):
+    """mix400 (a relaxed 400-lipid bilayer, 40 % of its lipids retyped
+    HEAD2/TAIL2 over 8-type tables) and mix200/ (a 48-step
+    reference MD run of a 200-lipid one with a temperature ramp)."""
+    smd.synth_bilayer(os.path.join(tmp, "mix.mpd"), 95, 400, 3.45, 20.0, 0.01, 0.0)
+    set_run(os.path.join(tmp, "mix.mpd"), 4, 4, 4)
+    run_ref_md(tmp, "mix")
+    to_mixed(os.path.join(tmp, "mix.mpd"), 95)
+    dump_case(tmp, "mix", "mix400")
+    mdir = os.path.join(HERE, "mix200")
+    os.makedirs(mdir, exist_ok=True)
+    smd.synth_bilayer(os.path.join(mdir, "mix.mpd"), 10, 200, 3.45, 16.0, 0.01, 0.0)
+    set_run(os.path.join(mdir, "mix.mpd"), 0.96, 0.48, 0.16)
+    to_mixed(os.path.join(mdir, "mix.mpd"), 10, ramp=(3.3, 0.16))
+    run_dir = os.path.join(tmp, "mixrun")
+    os.makedirs(run_dir)
+    shutil.copy(os.path.join(mdir, "mix.mpd"), run_dir)
+    run_ref_md(run_dir, "mix")
+    json.dump({os.path.basename(f): hashlib.sha256(open(f, "rb").read()).hexdigest()
+               for f in sorted(glob.glob(os.path.join(run_dir, "*")))},
+              open(os.path.join(mdir, "digests.json"), "w"), indent=1)
 
 
 def to_nanocore(path, sep):
@@ -286,6 +390,13 @@ def main():
     if not os.path.exists(os.path.join(REF, "ref_dump")):
         sys.exit("oracle/_ref is missing: run oracle/build_ref.sh first")
     tmp = tempfile.mkdtemp(prefix="smd_golden_")
+    if "--only-mixed" in sys.argv:  # the two-lipid fixtures alone
+        try:
+            make_mixed(tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        print("mixed fixtures written to", HERE)
+        return
     if "--only-nanocore" in sys.argv:  # the NANOCORE fixtures alone
         try:
             make_nanocore(tmp)
@@ -372,6 +483,7 @@ def main():
         json.dump(gens, open(os.path.join(HERE, "generators.json"), "w"), indent=1)
         make_fields(tmp)
         make_nanocore(tmp)
+        make_mixed(tmp)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     print("golden fixtures written to", HERE)

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 from conftest import load_golden
 
-CASES = ["ves300", "bil400", "sphere300", "net400", "field400", "core300"]
+CASES = ["ves300", "bil400", "sphere300", "net400", "field400", "core300", "mix400"]
 
 
 @pytest.mark.parametrize("case", CASES)
