@@ -7,7 +7,8 @@ restatement of the reference `MD` loop run the same 400-lipid bilayer with the
 constant-tension barostat on; after equilibration their time averages of
 temperature, area per lipid, potential energy per bead and bilayer thickness
 must agree within 4 combined standard errors (block averages) plus a 0.5 %
-allowance for the finite run.
+allowance for the finite run.  A 2,048-lipid bilayer compares the
+height-fluctuation spectrum of the reference's structureFactorFrames tool.
 """
 import os
 import re
@@ -104,3 +105,56 @@ def test_observables_match_reference_statistics(built, tmp_path):
         allowed = 4.0 * np.hypot(sg, sc) + 0.005 * abs(mc)
         print(f"{key}: gpu {mg:.5f} +- {sg:.5f}  reference {mc:.5f} +- {sc:.5f}")
         assert abs(mg - mc) <= allowed, (key, mg, sg, mc, sc)
+
+
+SF_LIPIDS = 2048
+SF_TOTAL_TAU = 200.0
+SF_STORE_TAU = 1.0
+SF_GRID = 16
+
+
+def _prepare_sf(dirpath):
+    p = os.path.join(dirpath, "bil.mpd")
+    smd.synth_bilayer(p, 2025, SF_LIPIDS, 3.45, 20.0, 0.01, 0.0)
+    t = open(p).read()
+    t = re.sub(r"finalTime \S+", f"finalTime {SF_TOTAL_TAU}", t)
+    t = re.sub(r"storeInterval \S+", f"storeInterval {SF_STORE_TAU}", t)
+    t = re.sub(r"measureInterval \S+", f"measureInterval {MEASURE_TAU}", t)
+    open(p, "w").write(t)
+
+
+def test_undulation_spectrum_matches_reference_statistics(built, tmp_path):
+    """The height-fluctuation spectrum of analysis/structureFactorFrames.cpp
+    (head beads, a 16 x 16 grid, frames from 20 tau) of a 2,048-lipid
+    bilayer run for 200 tau with the barostat on: the GPU `MD` executable
+    against the oracle's restatement of the reference loop, ring by ring,
+    within 4 combined standard errors (5 blocks) plus 5 % for the finite run.
+    Two oracle runs with different seeds differ by at most 1.3 combined
+    errors on this protocol."""
+    from analysis_obs import structure_factor_frames
+    from oracle_binding import MD as ORACLE_MD
+    gpu, cpu = tmp_path / "gpu", tmp_path / "cpu"
+    gpu.mkdir()
+    cpu.mkdir()
+    _prepare_sf(str(gpu))
+    _prepare_sf(str(cpu))
+    r1 = subprocess.run([smd.MD_EXE, "bil"], cwd=gpu, capture_output=True, text=True,
+                        env=dict(os.environ, SMD_PRECISION="mixed"))
+    assert r1.returncode == 0, r1.stdout + r1.stderr
+    threads = str(min(16, os.cpu_count() or 1))
+    r2 = subprocess.run([ORACLE_MD, "bil", threads], cwd=cpu, capture_output=True, text=True,
+                        env=dict(os.environ, OMP_NUM_THREADS=threads))
+    assert r2.returncode == 0, r2.stdout + r2.stderr
+    spectra = {}
+    for d, tag in ((gpu, "gpu"), (cpu, "cpu")):
+        q, S = structure_factor_frames(str(d / "frames_bil.xyz"), str(d / "size_bil.dat"), SF_STORE_TAU,
+                                       EQUIL_TAU, SF_GRID, SF_GRID, [2])
+        assert len(S) >= 150
+        spectra[tag] = (q, [_block_mean(S[:, k], blocks=5) for k in range(S.shape[1])])
+    qg, sg = spectra["gpu"]
+    qc, sc = spectra["cpu"]
+    assert np.allclose(qg, qc, rtol=0.02)  # the barostat left boxes of the same size
+    for k, ((mg, eg), (mc, ec)) in enumerate(zip(sg, sc)):
+        allowed = 4.0 * np.hypot(eg, ec) + 0.05 * abs(mc)
+        print(f"q {qc[k]:.3f}: gpu {mg:.5f} +- {eg:.5f}  reference {mc:.5f} +- {ec:.5f}")
+        assert abs(mg - mc) <= allowed, (k, mg, eg, mc, ec)
