@@ -52,6 +52,7 @@ struct smd_system {
   int n = 0, n_rep = 0, npad = 0, kmax = 0, n_cells = 0, n_tiles = 0;
   int n_sph = 0;  // BEAD sphere beads
   int n_terms = 0;  // BOND / BEND and external-field term entries
+  bool has_fields = false;  // any external-field term entry
   long long n_chains = 0;  // CHAIN molecules (lipids)
   // adjoint work arrays (allocated by the first adjoint call)
   struct Adj {
@@ -273,6 +274,9 @@ template <int FL>
 int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   auto& P = h->P;
   constexpr bool kLoopStep = (FL & (F_FORCES | F_ENERGY | F_INIT)) == 0;
+  // the loop's two integrator variants also come without the field-term
+  // call, whose out-of-line ABI costs them registers and a stack frame
+  constexpr bool kHot = FL == 0 || FL == (F_STOP | F_DU);
   if (kLoopStep && h->profile) {
     if (int rc = prof_mark(h)) return rc;
   }
@@ -292,11 +296,25 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
     } else {
       SMD_LAUNCH(h, (k_force<true, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
     }
-    SMD_PDL(h, k_integ<true, FL>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+    if constexpr (kHot) {
+      if (!h->has_fields)
+        SMD_PDL(h, k_integ<true, FL>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+      else
+        SMD_PDL(h, k_integ<true, FL | F_FIELDS>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+    } else {
+      SMD_PDL(h, k_integ<true, FL | F_FIELDS>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+    }
     if (h->n_sph) SMD_LAUNCH(h, (k_sphere<true, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   } else {
     SMD_LAUNCH(h, (k_force<false, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
-    SMD_PDL(h, k_integ<false, FL>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+    if constexpr (kHot) {
+      if (!h->has_fields)
+        SMD_PDL(h, k_integ<false, FL>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+      else
+        SMD_PDL(h, k_integ<false, FL | F_FIELDS>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+    } else {
+      SMD_PDL(h, k_integ<false, FL | F_FIELDS>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+    }
     if (h->n_sph) SMD_LAUNCH(h, (k_sphere<false, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
   }
   if (kLoopStep && h->profile) {
@@ -824,6 +842,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
       P.terms = dterms;
       P.n_terms = (int)flat.size();
       h->n_terms = P.n_terms;
+      for (const int4& t : flat) h->has_fields = h->has_fields || term_kind(t.x) > kTermBend;
     }
   }
   // ---- upload state (sorted order = file order until the first build)

@@ -19,7 +19,9 @@ enum StepFlags {
   F_INIT = 8,       // start-up force: store a only, start-up noise phase
   F_FORCES = 16,    // conservative forces only, written to P.force_out (file order)
   F_PAIRONLY = 32,  // with F_FORCES: non-bonded part only
-  F_ENERGY = 64     // energies only (pair, bonded, kinetic) into RepState
+  F_ENERGY = 64,    // energies only (pair, bonded, kinetic) into RepState
+  F_FIELDS = 128    // the system has external-field terms (their out-of-line
+                    // evaluation is compiled in only with this flag)
 };
 
 // ------------------------------------------------------------ last block
@@ -1503,7 +1505,7 @@ __device__ __noinline__ double field_potential(const DevPtrs& P, int cur, int i,
 // FP32 in the mixed form (vectors exact from the fractional mirror), FP64 in
 // the plain form; an external-field term's force is evaluated in FP64 and
 // added in R.  Every step variant takes its bonded force from here.
-template <bool MIXED>
+template <bool MIXED, bool FIELDS>
 __device__ __forceinline__ Vec3<typename std::conditional<MIXED, float, double>::type> bonded_force(
     const DevPtrs& P, int cur, int i, int ci, const double box[3], const RepState& rs) {
   using R = typename std::conditional<MIXED, float, double>::type;
@@ -1529,11 +1531,13 @@ __device__ __forceinline__ Vec3<typename std::conditional<MIXED, float, double>:
       const int4 t = P.terms[e];
       const int kind = term_kind(t.x), role = term_role(t.x), set = term_set(t.x);
       if (kind > kTermBend) {
-        Vec3<double> f1{0.0, 0.0, 0.0};
-        field_force<MIXED>(P, cur, i, t, box, f1);
-        fb.x += (R)f1.x;
-        fb.y += (R)f1.y;
-        fb.z += (R)f1.z;
+        if constexpr (FIELDS) {
+          Vec3<double> f1{0.0, 0.0, 0.0};
+          field_force<MIXED>(P, cur, i, t, box, f1);
+          fb.x += (R)f1.x;
+          fb.y += (R)f1.y;
+          fb.z += (R)f1.z;
+        }
         continue;
       }
       const R* cf;
@@ -1796,7 +1800,7 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
   const bool sphere = (ci < 0) && (ci & 0x40000000);  // integrated by k_sphere
   // bonded forces: one function for every step variant, so stopped and
   // running steps round them alike
-  if constexpr ((FL & (F_PAIRONLY | F_ENERGY)) == 0) fb = bonded_force<MIXED>(P, cur, i, ci, box, rs);
+  if constexpr ((FL & (F_PAIRONLY | F_ENERGY)) == 0) fb = bonded_force<MIXED, (FL & F_FIELDS) != 0>(P, cur, i, ci, box, rs);
   if ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0 && ci < 0 && !(ci & 0x40000000)) {
     const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
     // the chain's difference vectors in R (exact from the fractional
@@ -1848,7 +1852,7 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
         const int4 t = P.terms[e];
         const int kind = term_kind(t.x), role = term_role(t.x), set = term_set(t.x);
         if (kind > kTermBend) {  // external fields: energy only (no size-change term in the reference)
-          if constexpr ((FL & F_ENERGY) != 0)
+          if constexpr ((FL & F_ENERGY) != 0 && (FL & F_FIELDS) != 0)
             if (role == 0) e_bond += field_potential<MIXED>(P, cur, i, t, box);
           continue;
         }
