@@ -29,6 +29,10 @@ Fixtures
                    retyped HEAD2/TAIL2 over 8-type tables;
   mix200/          a 200-lipid two-lipid bilayer's 48-step reference MD run
                    with a temperature ramp (`--only-mixed`).
+  restart_bil/,    the checkpoint a reference run of traj_bil / core200
+  restart_core/    stores at t = 0.48, extended to 0.96, and the sha256 of
+                   every file the reference's continuation writes
+                   (`--only-restart`; made after traj_bil and core200).
   generators.json  sha256 of the reference generators' .mpd for a few seeds.
 Inputs are seeded synthetic membranes built in the reference generators' terms
 (softmold_gb300 synth_*, byte-identical to generate/liposome and bilayer).
@@ -255,6 +259,31 @@ def make_mixed(tmp):
               open(os.path.join(mdir, "digests.json"), "w"), indent=1)
 
 
+def make_restart(tmp):
+    """restart_bil/ and restart_core/: the checkpoint a reference MD run of
+    traj_bil / core200 stores at t = 0.48 (x(t+dt), v(t+dt/2), initialTime
+    0.48), extended to finalTime 0.96, and the sha256 of every file the
+    reference's continuation from it writes (MD.cpp:274-308 restart)."""
+    for src, name in ((os.path.join(HERE, "traj_bil", "bil.mpd"), "bil"),
+                      (os.path.join(HERE, "core200", "core.mpd"), "core")):
+        first = os.path.join(tmp, "first_" + name)
+        os.makedirs(first)
+        shutil.copy(src, first)
+        set_run(os.path.join(first, name + ".mpd"), 0.48, 0.48, 0.16)
+        run_ref_md(first, name)
+        rdir = os.path.join(HERE, "restart_" + name)
+        os.makedirs(rdir, exist_ok=True)
+        shutil.copy(os.path.join(first, name + ".mpd"), rdir)
+        set_run(os.path.join(rdir, name + ".mpd"), 0.96, 0.48, 0.16)
+        run_dir = os.path.join(tmp, "cont_" + name)
+        os.makedirs(run_dir)
+        shutil.copy(os.path.join(rdir, name + ".mpd"), run_dir)
+        run_ref_md(run_dir, name)
+        json.dump({os.path.basename(f): hashlib.sha256(open(f, "rb").read()).hexdigest()
+                   for f in sorted(glob.glob(os.path.join(run_dir, "*")))},
+                  open(os.path.join(rdir, "digests.json"), "w"), indent=1)
+
+
 def to_nanocore(path, sep):
     """Turns the BEAD residue of a vesicle-and-sphere .mpd into a NANOCORE
     residue of two cores (molecule block `18 nBond / 22 constants per core /
@@ -390,6 +419,13 @@ def main():
     if not os.path.exists(os.path.join(REF, "ref_dump")):
         sys.exit("oracle/_ref is missing: run oracle/build_ref.sh first")
     tmp = tempfile.mkdtemp(prefix="smd_golden_")
+    if "--only-restart" in sys.argv:  # the checkpoint-continuation fixtures alone
+        try:
+            make_restart(tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        print("restart fixtures written to", HERE)
+        return
     if "--only-mixed" in sys.argv:  # the two-lipid fixtures alone
         try:
             make_mixed(tmp)
@@ -484,6 +520,7 @@ def main():
         make_fields(tmp)
         make_nanocore(tmp)
         make_mixed(tmp)
+        make_restart(tmp)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     print("golden fixtures written to", HERE)
