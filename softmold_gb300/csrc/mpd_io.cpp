@@ -2,6 +2,7 @@
 #include "mpd_io.h"
 
 #include <cmath>
+#include <cstdio>
 #include <fstream>
 #include <iomanip>
 #include <map>
@@ -394,17 +395,28 @@ std::string mpd_serialize(const MpdSystem& s) {
   return out;
 }
 
+// The file is written beside its target and renamed over it, so a run that
+// dies while storing leaves the previous checkpoint whole (MDcuda keeps a
+// second copy for the same purpose, MDcuda.cu:87-112, 353-360); the bytes
+// and the final file set are those of a direct write.
 int mpd_write_file(const std::string& path, const MpdSystem& s, std::string& err) {
-  std::ofstream f(path, std::ios::out | std::ios::trunc);
+  const std::string tmp = path + ".part";
+  std::ofstream f(tmp, std::ios::out | std::ios::trunc);
   if (!f.is_open()) {
-    err = "Could not open " + path + " for writing";
+    err = "Could not open " + tmp + " for writing";
     return 10;
   }
   f << mpd_serialize(s);
   f.close();
   if (f.fail()) {
-    err = "Write failed for " + path;
+    std::remove(tmp.c_str());
+    err = "Write failed for " + tmp;
     return 11;
+  }
+  if (std::rename(tmp.c_str(), path.c_str()) != 0) {
+    std::remove(tmp.c_str());
+    err = "Could not replace " + path;
+    return 12;
   }
   return 0;
 }
