@@ -479,8 +479,21 @@ int validate(const smd_system_desc& d, std::string& why) {
     for (int k = 0; k < 3; ++k) {
       const double x = d.pos[3 * i + k];
       if (!(x >= 0 && x <= d.box[k])) return why = "position out of the box", 1;
+      if (!std::isfinite(d.vel[3 * i + k])) return why = "velocity not finite", 1;
     }
   }
+  const auto finite = [](const double* a, long long m) {
+    for (long long k = 0; k < m; ++k)
+      if (!std::isfinite(a[k])) return false;
+    return true;
+  };
+  const long long ntab = 6LL * d.n_types * d.n_types;
+  if (!finite(d.fconst, ntab) || !finite(d.uconst, ntab)) return why = "pair table value not finite", 1;
+  if (d.n_chain_blocks > 0 && !finite(d.chain_consts, 4LL * d.n_chain_blocks))
+    return why = "CHAIN constant not finite", 1;
+  if (!std::isfinite(d.dt) || !std::isfinite(d.gamma) || !(d.gamma >= 0) || !std::isfinite(d.temperature) ||
+      !(d.temperature >= 0) || !std::isfinite(d.tension) || !std::isfinite(d.delta_lxy))
+    return why = "dt, gamma, temperature, tension or deltaLXY not finite (or gamma / temperature negative)", 1;
   for (int b = 0; b < d.n_chain_blocks; ++b) {
     const int s = d.chain_blocks[3 * b], c = d.chain_blocks[3 * b + 1], l = d.chain_blocks[3 * b + 2];
     if (l < 3 || l > 4095) return why = "CHAIN length must be in 3..4095", 1;
@@ -526,6 +539,13 @@ int validate(const smd_system_desc& d, std::string& why) {
     if (kind == 11 && !(d.field_consts[8 * k] == 0 || d.field_consts[8 * k] == 1 || d.field_consts[8 * k] == 2))
       return why = "BOUNDARY dimension must be 0, 1 or 2", 1;
   }
+  if (d.n_bonds > 0 && !finite(d.bond_consts, 2LL * d.n_bonds)) return why = "BOND constant not finite", 1;
+  if (d.n_bends > 0 && !finite(d.bend_consts, 2LL * d.n_bends)) return why = "BEND constant not finite", 1;
+  if (d.n_fields > 0 && !finite(d.field_consts, 8LL * d.n_fields)) return why = "field constant not finite", 1;
+  if (d.n_spheres > 0 &&
+      !finite(d.sphere_consts, d.sphere_nanocore ? (long long)kBeadConst * d.n_spheres
+                                                  : (long long)kBeadConst * d.n_types * d.n_types))
+    return why = "BEAD / NANOCORE constant not finite", 1;
   if (!(d.dt > 0)) return why = "dt must be positive", 1;
   return 0;
 }
@@ -962,6 +982,18 @@ int smd_set_state(smd_system* h, const double* pos, const double* vel) {
   double* vs = h->xfer + n3;
   if (pos) SMD_CUDA(cudaMemcpyAsync(xs, pos, n3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   if (vel) SMD_CUDA(cudaMemcpyAsync(vs, vel, n3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SMD_LAUNCH(h, k_state_check<<<h->grid(), kBlock, 0, h->stream>>>(P, pos ? xs : nullptr, vel ? vs : nullptr));
+  {
+    Global g;
+    SMD_CUDA(cudaMemcpyAsync(&g, P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream));
+    SMD_CUDA(cudaStreamSynchronize(h->stream));
+    if (g.error & 4) {
+      g.error &= ~4;
+      SMD_CUDA(cudaMemcpy(P.g, &g, sizeof(Global), cudaMemcpyHostToDevice));
+      return fail(9, "smd_set_state: a position outside its replica's box or not finite, or a velocity that is "
+                     "not finite (the handle's state is unchanged)");
+    }
+  }
   SMD_LAUNCH(h, k_state_load<<<h->grid(), kBlock, 0, h->stream>>>(P, pos ? xs : nullptr, vel ? vs : nullptr));
   if (pos) {
     if (h->mixed)

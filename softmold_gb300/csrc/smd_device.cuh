@@ -118,7 +118,7 @@ struct Global {  // single instance
   float last_disp;
   unsigned int blocks_done;    // last-block counter
   int rebuild;                 // 1: rebuild the Verlet list before the next force pass
-  int error;                   // bit 0: list overflow, bit 1: cell overflow (>kMaxCell)
+  int error;                   // bit 0: list overflow, bit 1: cell overflow (>kMaxCell), bit 2: refused set_state input
   int need_nbr;                // largest neighbour count seen on overflow
   int max_nbr;                 // largest neighbour count of any list build so far
   int trial_slot;              // staged barostat trial used by the next MC step

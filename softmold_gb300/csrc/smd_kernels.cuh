@@ -2394,6 +2394,26 @@ __global__ void __launch_bounds__(kBlock) k_state_save(DevPtrs P, double* xs, do
 
 // The inverse scatter: file-order positions and / or velocities into the
 // sorted device arrays (the caller refreshes the mirror after positions).
+// Checks a state staged for smd_set_state (file order): every position
+// inside its replica's box and every velocity finite, else bit 2 of the
+// error word.  It runs before the state is loaded, so a refused state
+// leaves the handle's own untouched.
+__global__ void __launch_bounds__(kBlock) k_state_check(DevPtrs P, const double* xs, const double* vs) {
+  const int o = blockIdx.x * kBlock + threadIdx.x;
+  if (o >= P.n) return;
+  bool bad = false;
+  if (xs) {
+    const RepState& rs = P.rs[rep_of(P, o)];
+    for (int k = 0; k < 3; ++k) {
+      const double x = xs[3 * o + k];
+      bad = bad || !(x >= 0.0 && x <= rs.box[k]);
+    }
+  }
+  if (vs)
+    for (int k = 0; k < 3; ++k) bad = bad || !isfinite(vs[3 * o + k]);
+  if (bad) atomicOr(&P.g->error, 4);
+}
+
 __global__ void __launch_bounds__(kBlock) k_state_load(DevPtrs P, const double* xs, const double* vs) {
   const int i = blockIdx.x * kBlock + threadIdx.x;
   if (i >= P.n) return;

@@ -3,7 +3,8 @@
 The list is sized from the start configuration (twice the largest neighbour
 count plus a margin).  A denser state set later must grow it, not overflow
 it; a list cell holding more beads than the list kernels stage (a collapsed
-system) is refused with an error by the kernels' own bounds checks.
+system) is refused with an error by the kernels' own bounds checks; a state
+that is out of its box or not finite is refused before it is loaded.
 """
 import numpy as np
 import pytest
@@ -51,3 +52,30 @@ def test_collapsed_cell_is_refused(built):
                             delta_lxy=0.0)
     with pytest.raises(smd.SmdError, match="more than 1024 beads"):
         smd.System(m, precision=smd.MIXED)
+
+
+@pytest.mark.parametrize("bad", ["outside", "nan position", "inf velocity"])
+def test_refused_state_leaves_the_handle_unchanged(built, bad):
+    """smd_set_state checks the staged state on the device before loading it
+    (a position outside its replica's box or not finite, a velocity that is
+    not finite): the call is refused, the handle keeps its state and runs on."""
+    g = load_golden("bil400")
+    s = smd.System(mpd_from_golden(g), precision=smd.MIXED)
+    p0, v0 = s.state()
+    pos, vel = p0.copy(), v0.copy()
+    if bad == "outside":
+        pos[10, 0] = s.box()[0] + 0.1
+    elif bad == "nan position":
+        pos[20, 2] = np.nan
+    else:
+        vel[30, 1] = np.inf
+    with pytest.raises(smd.SmdError, match="state is unchanged"):
+        s.set_state(pos, vel)
+    p1, v1 = s.state()
+    assert np.array_equal(p1, p0) and np.array_equal(v1, v0)
+    s.set_state(p0, v0)  # a valid state is still taken
+    s.prepare()
+    s.advance(8)
+    p, v = s.state()
+    assert np.isfinite(p).all() and np.isfinite(v).all()
+    s.close()

@@ -80,6 +80,13 @@ def _bad(**kw):
     ("chain", "CHAIN block out of range"),
     ("bond", "BOND bead index out of range"),
     ("dt", "dt must be positive"),
+    ("nan position", "position out of the box"),
+    ("inf velocity", "velocity not finite"),
+    ("nan table", "pair table value not finite"),
+    ("nan chain", "CHAIN constant not finite"),
+    ("inf gamma", "gamma, temperature"),
+    ("negative temperature", "gamma, temperature"),
+    ("nan bond", "BOND constant not finite"),
 ])
 def test_invalid_descriptors_are_refused_before_any_device_work(built, change, message):
     """The descriptor checks run on the host before the device is touched,
@@ -105,6 +112,27 @@ def test_invalid_descriptors_are_refused_before_any_device_work(built, change, m
         m = _bad(chain_blocks=np.array([[len(pos) - 2, 1, 3]], np.int32), chain_consts=np.array([[0.7, 100, 1, 100]]))
     elif change == "bond":
         m = _bad(bonds=np.array([[0, len(pos)]], np.int32), bond_consts=np.array([[0.7, 100.0]]))
+    elif change == "nan position":
+        pos[3, 1] = np.nan
+        m = _bad(pos=pos)
+    elif change == "inf velocity":
+        vel = np.array(g["vel"], np.float64)
+        vel[5, 2] = np.inf
+        m = _bad(vel=vel)
+    elif change == "nan table":
+        fc = np.array(g["fconst"], np.float64).copy()
+        fc[7] = np.nan
+        m = _bad(fconst=fc)
+    elif change == "nan chain":
+        cc = np.array(g["chain_consts"], np.float64).reshape(-1, 4).copy()
+        cc[0, 1] = np.nan
+        m = _bad(chain_consts=cc)
+    elif change == "inf gamma":
+        m = _bad(gamma=np.inf)
+    elif change == "negative temperature":
+        m = _bad(temperature=-1.0)
+    elif change == "nan bond":
+        m = _bad(bonds=np.array([[0, 1]], np.int32), bond_consts=np.array([[0.7, np.nan]]))
     else:
         m = _bad(dt=0.0)
     with pytest.raises(smd.SmdError, match=message):
@@ -117,3 +145,23 @@ def test_batch_replicas_must_share_the_pair_tables(built):
     f[0] += 1.0
     with pytest.raises(smd.SmdError, match="share the pair tables"):
         smd.System([a, _bad(fconst=f)])
+
+
+@pytest.mark.parametrize("case,message", [
+    ("missing", "Could not open"),
+    ("truncated", "is missing (end of file)"),
+    ("corrupt", "is not a numerical type"),
+])
+def test_md_executable_refuses_bad_input_files(built, tmp_path, case, message):
+    """A missing, truncated or corrupt .mpd is reported with a message (the
+    reference's Script reader throws with one) before any device work, and
+    no output file is written."""
+    src = open(os.path.join(GOLDEN, "traj_bil", "bil.mpd")).read()
+    if case == "truncated":
+        (tmp_path / "bil.mpd").write_text(src[:3000])
+    elif case == "corrupt":
+        (tmp_path / "bil.mpd").write_text(src.replace("cutoff 2", "cutoff two", 1))
+    r = subprocess.run([smd.MD_EXE, "bil"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode != 0
+    assert message in r.stdout + r.stderr
+    assert sorted(os.listdir(tmp_path)) == ([] if case == "missing" else ["bil.mpd"])
