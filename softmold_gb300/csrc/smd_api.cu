@@ -876,10 +876,9 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     for (int r = 0; r < n_rep; ++r) {
       const smd_system_desc& d = descs[r];
       std::memset(&rs[r], 0, sizeof(RepState));
-      for (int k = 0; k < 3; ++k) {
-        rs[r].box[k] = d.box[k];
-        rs[r].scale[k] = 1.0;
-      }
+      const double one[3] = {1.0, 1.0, 1.0};
+      for (int k = 0; k < 3; ++k) rs[r].box[k] = d.box[k];
+      set_scale(rs[r], one);
       derive_box(rs[r], h->rp[r].cell_cap, T.list_cut);
       for (int i = 0; i < d.n; ++i, ++b) {
         hx[b] = d.pos[3 * i];
@@ -1095,7 +1094,7 @@ int smd_compute_dU(smd_system* h, const double scale[3], double* dU) {
   for (auto& s : rs) {
     s.dU_pair = s.dU_bond = 0;
     s.dUq_pair = s.dUq_bond = 0;
-    for (int k = 0; k < 3; ++k) s.scale[k] = scale[k];
+    set_scale(s, scale);
   }
   SMD_CUDA(cudaMemcpyAsync(h->P.rs, rs.data(), h->n_rep * sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
   if ((rc = launch_step<F_DU | F_ENERGY>(h))) return rc;

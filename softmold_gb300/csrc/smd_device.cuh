@@ -91,6 +91,8 @@ struct RepState {  // per replica, updated on the device
   float pad_f;
   double trial_box[3];
   double scale[3];   // scale of the last accepted / current trial
+  float sq_f[3];     // fma(scale, scale, -1) in FP32, set with scale (the mixed size-change terms)
+  float pad_sq;
   double dU_pair, dU_bond;  // FP64 form: U(x) - U(s x) summed in any order
   long long dUq_pair, dUq_bond;  // mixed form: the same in units of 2^-32, summed exactly
   double e_pair, e_bond, e_kin, e_sphere;
@@ -100,6 +102,15 @@ struct RepState {  // per replica, updated on the device
   int ncell[3];
   int pad;
 };
+
+// Sets a replica's trial scale and its FP32 factors s^2 - 1 (one rounding of
+// the exact s^2 - 1, on the host and the device alike).
+__host__ __device__ inline void set_scale(RepState& rs, const double s[3]) {
+  for (int d = 0; d < 3; ++d) {
+    rs.scale[d] = s[d];
+    rs.sq_f[d] = (float)fma(s[d], s[d], -1.0);
+  }
+}
 
 // Size-change energy of a replica's current trial.  The mixed form rounds
 // each pair term (once per pair) and each bead's bonded term to 2^-32 before

@@ -1106,7 +1106,14 @@ __device__ __forceinline__ float bend_dpot_f(Vec3<float> da, Vec3<float> db, con
 // float -> int64 rounded to nearest, the same value as __float2ll_rn: values
 // below 2^31 in magnitude (nearly every pair term) take the 32-bit conversion.
 __device__ __forceinline__ long long f2ll_rn(float y) {
-  return (fabsf(y) < 2147483648.f) ? (long long)__float2int_rn(y) : __float2ll_rn(y);
+  // y = a 2^16 + b exactly, a = rint(y 2^-16) and |b| <= 2^15 (for |y| >= 2^16
+  // a 2^16 is within a factor two of y, so the subtraction is exact; below,
+  // a = 0): two 32-bit conversions instead of the 64-bit one.  a 2^16 is an
+  // even integer, so rounding b to nearest even rounds y so.  Exact for
+  // |y| < 2^46.
+  const float a = rintf(y * (1.0f / 65536.0f));
+  const float b = fmaf(-a, 65536.0f, y);
+  return ((long long)__float2int_rn(a) << 16) + (long long)__float2int_rn(b);
 }
 
 // Difference vectors e[k] = x(p-2+k) - x(p-1+k), k = 0..3, of the chain
@@ -1577,9 +1584,9 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
   const float s0 = rs.len_per_frac[0], s1 = rs.len_per_frac[1], s2 = rs.len_per_frac[2];
   float sq0 = 0.f, sq1 = 0.f, sq2 = 0.f;
   if constexpr ((FL & F_DU) != 0) {
-    sq0 = (float)(rs.scale[0] * rs.scale[0] - 1.0);
-    sq1 = (float)(rs.scale[1] * rs.scale[1] - 1.0);
-    sq2 = (float)(rs.scale[2] * rs.scale[2] - 1.0);
+    sq0 = rs.sq_f[0];
+    sq1 = rs.sq_f[1];
+    sq2 = rs.sq_f[2];
   }
   const float* rowF = sF + 6 * ti * nT;
   const float* rowU = sU + 6 * ti * nT;
@@ -1812,8 +1819,7 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
     // size-change differences in FP64 (plain) or factored FP32 (mixed)
     if constexpr (MIXED && (FL & F_DU) != 0) {
       const float* cf = T.chainF[set];
-      const float sq[3] = {(float)(rs.scale[0] * rs.scale[0] - 1.0), (float)(rs.scale[1] * rs.scale[1] - 1.0),
-                           (float)(rs.scale[2] * rs.scale[2] - 1.0)};
+      const float sq[3] = {rs.sq_f[0], rs.sq_f[1], rs.sq_f[2]};
       float du = 0.f;
       if (valid[2]) du += bond_dpot_f(er[2], sq, cf);
       if (valid[2] && valid[3]) du += bend_dpot_f(er[2], er[3], sq, cf + 2);
@@ -1846,8 +1852,7 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
     if (P.n_terms > 0) {
       const int o = P.orig[i];
       const int e1 = P.term_off[o + 1];
-      const float sq_f[3] = {(float)(rs.scale[0] * rs.scale[0] - 1.0), (float)(rs.scale[1] * rs.scale[1] - 1.0),
-                             (float)(rs.scale[2] * rs.scale[2] - 1.0)};
+      const float sq_f[3] = {rs.sq_f[0], rs.sq_f[1], rs.sq_f[2]};
       for (int e = P.term_off[o]; e < e1; ++e) {
         const int4 t = P.terms[e];
         const int kind = term_kind(t.x), role = term_role(t.x), set = term_set(t.x);
@@ -2069,16 +2074,15 @@ __global__ void k_trial(DevPtrs P) {
   rs.dUq_pair = 0;
   rs.dUq_bond = 0;
   if (P.rp[r].dlxy == 0) {
-    for (int d = 0; d < 3; ++d) rs.scale[d] = 1.0;
+    const double one[3] = {1.0, 1.0, 1.0};
+    set_scale(rs, one);
     return;
   }
   const double u1 = P.trial_u[((size_t)trial * P.n_rep + r) * 2];
   double nb[3], s[3];
   trial_box(rs.box, P.rp[r].dlxy, u1, nb, s);
-  for (int d = 0; d < 3; ++d) {
-    rs.trial_box[d] = nb[d];
-    rs.scale[d] = s[d];
-  }
+  for (int d = 0; d < 3; ++d) rs.trial_box[d] = nb[d];
+  set_scale(rs, s);
   rs.dU_pair = 0.0;
   rs.dU_bond = 0.0;
   rs.dUq_pair = 0;
