@@ -1,8 +1,8 @@
 // ORACLE — test infrastructure only.
 //
 // CPU restatement of the SoftMold implicit-solvent MD step (the reference's
-// MD.cpp loop and the CellOpt / Blob / Verlet / Langevin code it calls).  It is
-// the checker for the CUDA library: only tests/, __graft_entry__.smoke() and
+// MD.cpp loop and the CellOpt / Blob / Verlet / Langevin code it calls).  It
+// checks the CUDA library's results: only tests/, __graft_entry__.smoke() and
 // bench.py's CPU-baseline arm may load or run it, never the product path.
 //
 // Parity of this restatement is pinned by golden vectors dumped from the

@@ -353,7 +353,7 @@ class System:
             has_bead = m.sphere_index is not None and len(m.sphere_index) > 0
             has_core = m.core_index is not None and len(m.core_index) > 0
             if has_bead and has_core:
-                raise SmdError("a BEAD and a NANOCORE residue in one system are not on the GPU step of this build")
+                raise SmdError("a BEAD and a NANOCORE residue in one system are not supported on the GPU step")
             if has_bead:
                 arrs["si"] = np.ascontiguousarray(m.sphere_index, np.int32)
                 arrs["sc"] = np.ascontiguousarray(m.sphere_consts, np.float64)

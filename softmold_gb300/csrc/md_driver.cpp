@@ -110,7 +110,7 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
       }
     } else if (m.type == smd::MOL_BEAD || m.type == smd::MOL_NANOCORE) {
       if (sphere_consts) {
-        std::cout << "Error(MD): more than one BEAD or NANOCORE residue is not on the GPU step of this build\n";
+        std::cout << "Error(MD): more than one BEAD or NANOCORE residue is not supported on the GPU step\n";
         return 1;
       }
       for (const auto& b : m.bonds) sphere_idx.push_back(b[0]);
@@ -122,7 +122,7 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
       field_terms(m, S.type, field_idx, field_c);
     } else if (m.type != smd::MOL_SOLID) {
       std::cout << "Error(MD): molecule type " << m.type
-                << " is not on the GPU step of this build (supported: CHAIN, BOND, BEND, BEAD, NANOCORE, "
+                << " is not supported on the GPU step (supported: CHAIN, BOND, BEND, BEAD, NANOCORE, "
                    "BOUNDARY, FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL, BALL)\n";
       return 1;
     }

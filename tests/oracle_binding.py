@@ -1,6 +1,6 @@
 """ctypes binding of the CPU oracle (oracle/_build/libsmd_oracle.so) for tests.
 
-The oracle is the checker: tests call it beside the CUDA library and compare.
+Tests call the oracle beside the CUDA library and compare the two.
 """
 import ctypes as C
 import os
