@@ -258,10 +258,18 @@ int smd_synth_vesicle_sphere(const char* path, int seed, int n_lipids, double ar
  * (6*n_types^2) and d_force (n*3, overwritten) are device pointers owned by
  * the caller; work is queued on `stream` (a cudaStream_t, NULL = default) and
  * not waited for.  At most SMD_STATIC_MAX_BEADS beads and
- * SMD_STATIC_MAX_CELLS cells (int(L/rc) per axis); larger inputs are
- * rejected.  Calls share the scratch: calls that overlap on the GPU race.
- * The first call on a device looks up the scratch address; make it before
- * any stream capture. */
+ * SMD_STATIC_MAX_CELLS cells (int(L/rc) per axis); larger inputs, and box
+ * edges that are not finite and positive, are rejected.  Positions must be
+ * wrapped into [0, L] for the forces to be the reference's, and types must
+ * lie in [0, n_types).  The device arrays are not checked on the host, but
+ * no value in them makes a kernel access memory outside the caller's arrays
+ * and the scratch: cell indices are clamped into the grid and types are
+ * range-checked before the table lookup; a bead whose position is not
+ * finite, or whose type or a neighbour's type within rc is outside
+ * [0, n_types), gets a NaN force.  Calls share the scratch: calls that
+ * overlap on the GPU race.  The first call on a device looks up the scratch
+ * address; make it before any stream capture, and do not call this entry
+ * point on a device again after cudaDeviceReset of that device. */
 #define SMD_STATIC_MAX_BEADS 32768
 #define SMD_STATIC_MAX_CELLS 32768
 int smd_pair_forces_static(const double* d_pos, const int* d_type, int n, const double box[3], double cutoff,
