@@ -1,0 +1,174 @@
+"""Every benchmarked workload against the FP64 oracle at its own size.
+
+The golden fixtures pin the device on a few hundred lipids; these tests run
+each benchmarked configuration at full size (the same seeded synthetic inputs
+as bench.py) and compare the device with the oracle's one-pass restatement of
+the reference (oracle/smd_oracle.cpp) on the same state:
+
+  * cell keys of the reference grid, bit-exact (CellOpt::build,
+    include/algorithms/cellOpt.h:510-710);
+  * the set of pairs within rc taken from the Verlet list, bit-exact against
+    the reference traversal's pairs;
+  * forces: plain FP64 within 1e-12 and the mixed form within 1e-5 of max |F|
+    (max and RMS), pair-only and total (computeForce + doChainForce +
+    doBeadForce, cellOpt.h:712-926, include/system.h:1782-1866, 2043-2212);
+  * pair, bonded and sphere energies, and the size-change difference U(x) -
+    U(s x) for three trial scales (computePotential, computeDPotential,
+    doChainDPotential, doBeadDPotential).
+
+The state is taken after a short mixed run from the generator's start, so it
+is a relaxed membrane rather than a lattice.  The workloads are:
+  vesicle5k   5,000-lipid vesicle, 15,000 beads, 60^3 box;
+  bilayer20k  20,000-lipid bilayer, 60,000 beads, barostat on;
+  sphere80k   80,000-lipid vesicle with one continuum sphere, 240,001 beads
+              in a 190^3 box (about 439,000 list cells: the multi-CTA scan);
+  batch       four replicas of the 64-bilayer batch (ragged sizes, their own
+              tensions and boxes), one handle;
+  bilayer10k  the adjoint workload's 10,000-lipid bilayer, 30,000 beads;
+  sparse300   a 300-lipid vesicle in a 100^3 box: 64,000 list cells, the
+              multi-CTA scan on a case small enough to run in a second.
+"""
+import dataclasses
+import os
+
+import numpy as np
+import pytest
+
+import softmold_gb300 as smd
+
+pytestmark = pytest.mark.gpu
+
+PLAIN_TOL = 1e-12
+MIXED_TOL = 1e-5
+SCALES = np.array([[1.004, 1.004, 1.0 / 1.004 ** 2], [0.996, 0.996, 1.0 / 0.996 ** 2], [1.01, 0.995, 1.0]])
+
+
+def _synth(tmp, name):
+    """(list of Mpd, steps to relax) of a workload, built as bench.py builds it."""
+    p = os.path.join(tmp, name + ".mpd")
+    if name == "vesicle5k":
+        smd.synth_vesicle(p, 1000, 5000, 3.45, 60.0)
+    elif name == "bilayer20k":
+        smd.synth_bilayer(p, 1000, 20000, 3.45, 15.0, 0.01, 0.0)
+    elif name == "sphere80k":
+        smd.synth_vesicle_sphere(p, 1000, 80000, 3.45, 190.0, 5.0, -10.0, 300.0, 2.0, 100.0)
+    elif name == "bilayer10k":
+        smd.synth_bilayer(p, 1000, 10000, 3.45, 15.0, 0.0, 0.0)
+    elif name == "sparse300":
+        smd.synth_vesicle(p, 77, 300, 3.45, 100.0)
+    elif name == "batch":
+        rng = np.random.default_rng(64)
+        lipids = rng.integers(1000, 8001, size=64)
+        tensions = rng.uniform(0.0, 1.0, size=64)
+        ms = []
+        for k in (0, 17, 40, 63):
+            q = os.path.join(tmp, f"batch{k}.mpd")
+            smd.synth_bilayer(q, 5000 + k, int(lipids[k]), 3.45, 15.0, 0.01, float(tensions[k]))
+            ms.append(smd.read_mpd(q))
+        return ms
+    return [smd.read_mpd(p)]
+
+
+def _case(m, pos, box):
+    """The oracle's view (a golden-case dict) of system m at state pos, box."""
+    g = {"pos": np.ascontiguousarray(pos), "type": np.asarray(m.type, np.int32), "box": np.asarray(box, np.float64),
+         "cutoff": m.cutoff, "n_types": m.n_types, "fconst": m.fconst, "uconst": m.uconst,
+         "chain_blocks": m.chain_blocks, "chain_consts": m.chain_consts}
+    if m.sphere_index is not None and len(m.sphere_index):
+        g["sphere_index"] = m.sphere_index
+        g["sphere_consts"] = m.sphere_consts
+    return g
+
+
+@pytest.fixture(scope="module", params=["sparse300", "vesicle5k", "bilayer20k", "bilayer10k", "batch", "sphere80k"])
+def relaxed(request, tmp_path_factory, built):
+    """(name, systems, mixed handle, per-replica states) after 200 mixed steps."""
+    ms = _synth(str(tmp_path_factory.mktemp(request.param)), request.param)
+    s = smd.System(ms if len(ms) > 1 else ms[0], precision=smd.MIXED)
+    s.prepare()
+    s.advance(200)
+    pos, vel = s.state()
+    offs = np.cumsum([0] + [len(m.type) for m in ms])
+    reps = []
+    for r, m in enumerate(ms):
+        a, b = offs[r], offs[r + 1]
+        reps.append(dataclasses.replace(m, pos=pos[a:b].copy(), vel=vel[a:b].copy(), box=s.box(r)))
+    yield request.param, ms, s, reps
+    s.close()
+
+
+def _both_forms(reps):
+    """Plain and mixed handles built from the relaxed states."""
+    arg = reps if len(reps) > 1 else reps[0]
+    return smd.System(arg, precision=smd.PLAIN_FP64), smd.System(arg, precision=smd.MIXED)
+
+
+def test_cell_keys_and_pair_set(relaxed, oracle):
+    name, _, s, reps = relaxed
+    keys = s.cell_keys()
+    pairs = s.pair_list()
+    base = 0
+    got_pairs = []
+    for m in reps:
+        n = len(m.type)
+        want = oracle.cell_keys(m.pos, m.box, m.cutoff)
+        assert np.array_equal(keys[base:base + n], want), name
+        ref = np.sort(oracle.pair_list(m.pos, m.box, m.cutoff), axis=1).astype(np.int64)
+        sel = (pairs[:, 0] >= base) & (pairs[:, 0] < base + n)
+        got = np.sort(pairs[sel] - base, axis=1).astype(np.int64)
+        assert (got >= 0).all() and (got < n).all(), name
+        got_pairs.append(len(got))
+        ref_k = np.unique(ref[:, 0] * n + ref[:, 1])
+        got_k = np.unique(got[:, 0] * n + got[:, 1])
+        assert len(ref_k) == len(ref) and len(got_k) == len(got), name  # each pair once
+        assert np.array_equal(got_k, ref_k), (name, len(got_k), len(ref_k))
+        base += n
+    assert sum(got_pairs) == len(pairs)
+
+
+def test_forces_against_oracle(relaxed, oracle):
+    name, _, _, reps = relaxed
+    p, q = _both_forms(reps)
+    fp_pair, fp = p.forces(pair_only=True), p.forces()
+    fm_pair, fm = q.forces(pair_only=True), q.forces()
+    p.close()
+    q.close()
+    base = 0
+    for m in reps:
+        n = len(m.type)
+        g = _case(m, m.pos, m.box)
+        ref_pair = oracle.forces(g, pair_only=True)
+        ref = oracle.forces(g)
+        scale = np.abs(ref).max()
+        sl = slice(base, base + n)
+        err_plain = max(np.abs(fp[sl] - ref).max(), np.abs(fp_pair[sl] - ref_pair).max()) / scale
+        err_mixed = max(np.abs(fm[sl] - ref).max(), np.abs(fm_pair[sl] - ref_pair).max()) / scale
+        rms_mixed = np.sqrt(np.mean((fm[sl] - ref) ** 2)) / scale
+        print(f"{name}: {n} beads, plain max {err_plain:.2e}, mixed max {err_mixed:.2e} rms {rms_mixed:.2e}")
+        assert err_plain <= PLAIN_TOL, (name, err_plain)
+        assert err_mixed <= MIXED_TOL, (name, err_mixed)
+        assert rms_mixed <= MIXED_TOL
+        base += n
+
+
+def test_energies_and_size_change(relaxed, oracle):
+    name, _, _, reps = relaxed
+    p, q = _both_forms(reps)
+    try:
+        for h, tol, dtol in ((p, 1e-12, 1e-10), (q, 2e-6, 2e-4)):
+            e = h.energy()
+            dus = [h.dU(sc) for sc in SCALES]
+            for r, m in enumerate(reps):
+                g = _case(m, m.pos, m.box)
+                pair, bonded, bead = oracle.energies(g)
+                assert abs(e[r]["pair"] - pair) <= tol * abs(pair), (name, r, e[r]["pair"], pair)
+                assert abs(e[r]["bonded"] - bonded) <= tol * abs(bonded), (name, r)
+                assert abs(e[r]["sphere"] - bead) <= tol * max(abs(bead), 1e-300) + 1e-12 * abs(pair), (name, r)
+                for sc, du in zip(SCALES, dus):
+                    dp, db, dbead = oracle.energies(g, scale=sc)
+                    want = dp + db + dbead
+                    ref_scale = (abs(pair) + abs(bonded) + abs(bead)) * np.abs(sc - 1).max()
+                    assert abs(du[r] - want) <= dtol * ref_scale, (name, r, sc, du[r], want)
+    finally:
+        p.close()
+        q.close()
