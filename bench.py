@@ -7,19 +7,31 @@ barostat on (deltaLXY 0.01, tension 0), Langevin gamma 1, kT 3, dt 0.02,
 mixed precision.  Seeded synthetic input built in the reference generator's
 geometry, equilibrated for 1,000 untimed steps.
 
-One bench step = one barostat period, 8 MD loop iterations (MD.cpp:335-729,
-resizeRate 8), on the device-resident state, launched as one CUDA graph; L2 is
-flushed (256 MiB write) between timed steps and every step is bracketed by
-CUDA events on the library's stream.  `e2e` runs the same metric through the C
-ABI with host buffers: per e2e step the state is uploaded, 48 iterations are
-advanced, the energies are measured and the state is read back.
+One bench step = 64 MD loop iterations (MD.cpp:335-729), eight barostat
+periods of resizeRate 8, on the device-resident state, launched as one CUDA
+graph per period; L2 is flushed (256 MiB write) between timed steps and every
+step is bracketed by CUDA events on the library's stream.  `e2e` runs the same
+metric through the C ABI with host buffers: per e2e step the state is
+uploaded, 48 iterations are advanced, the energies are measured and the state
+is read back.
+
+`roofline` is the whole MD step against HBM: 176 algorithmic bytes per
+bead-step (x and v FP64 read and write, the 16-byte position mirror written
+and read, the int64 force accumulator written and read) times the measured
+bead-steps/s, over the measured copy bandwidth.  `kernels` gives the same
+figure for the pair pass + integrator alone, timed per launch with CUDA
+events, and `issue` the instruction-issue bound of the step from the warp
+instructions the committed ncu capture counted.  `force_err` is the mixed
+form's force error against the oracle's FP64 forces on the bench's own state.
 
 Other workloads (--workload): vesicle5k (15,000-bead vesicle, no barostat),
 batch64 (64 independent bilayers of 1,000-8,000 lipids and tension 0-1, one
 handle, one set of launches per step), sphere80k (240,001-bead vesicle with a
 continuum sphere) and adjoint10k (gradient of a 200-step window of a
-30,000-bead bilayer: forward, recompute and backward passes).  Under torchrun every rank runs its own
-copy of the workload (weak scaling, no data-path collective).
+30,000-bead bilayer: forward, recompute and backward passes).  Under torchrun
+every rank runs its own copy of the workload (weak scaling, no data-path
+collective), except batch64, whose 64 replicas are split across the ranks
+(strong scaling).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--workload bilayer20k|vesicle5k|batch64|sphere80k|adjoint10k]
@@ -45,7 +57,21 @@ ALG_BYTES_PER_BEAD_STEP = 176  # x,v FP64 r/w 96 + position mirror w/r 32 + forc
 METRIC = "bead-steps/s on 1 GB300 (mixed precision)"
 UNIT = "bead-steps/s"
 E2E_INTERVAL = 48  # six barostat periods: one e2e step = upload, 48 MD steps, energies, download
-PERIOD = 8         # MD steps per bench step: one barostat period (resizeRate, MD.cpp:67)
+PERIOD = 8         # MD steps of one barostat period (resizeRate, MD.cpp:67)
+STEP_MD = 8 * PERIOD  # MD steps per bench step
+SMS = 152          # GB300 streaming multiprocessors
+ISSUE_PER_SM_CLK = 4  # warp instructions issued per SM and clock (four schedulers)
+# DRAM bytes and warp instructions per bead and MD step of the mixed step,
+# summed over every kernel of the step with its launches per MD step, from one
+# ncu capture of the workload (metrics dram__bytes_read.sum,
+# dram__bytes_write.sum, smsp__inst_executed.sum per kernel; the command and
+# the per-kernel table are in profiles/step_traffic_bilayer60k.md).  Traffic
+# is a named constant because ncu cannot run inside the timed region.
+STEP_PROFILE = {
+    "bilayer20k": {"dram_bytes_per_bead_step": 819.0, "warp_inst_per_bead_step": 622.0,
+                   "source": "profiles/step_traffic_bilayer60k.md (ncu, cold caches: an upper bound on the bench's "
+                             "L2-resident DRAM traffic)"},
+}
 
 
 def load_peaks():
@@ -56,9 +82,11 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def workload(args, rank, tmpdir):
-    """(paths, systems, config) of the benchmarked workload for one rank."""
+def workload(args, rank, tmpdir, world=1):
+    """(paths, systems, config) of the benchmarked workload for one rank.
+    The config dict describes the whole job and is the same in both arms."""
     import softmold_gb300 as smd
+    from softmold_gb300.scaling import replica_range
     if args.workload == "bilayer20k":
         path = os.path.join(tmpdir, f"bench{rank}.mpd")
         smd.synth_bilayer(path, 1000 + rank, 20000, 3.45, 15.0, 0.01, 0.0)
@@ -87,13 +115,15 @@ def workload(args, rank, tmpdir):
                            "3-bead lipids (30,000 beads), box fixed, kT 3, gamma 1, dt 0.02"}
         paths = [path]
     elif args.workload == "batch64":
-        rng = np.random.default_rng(64 + 1000 * rank)
+        # the same 64 replicas for every job size; under torchrun each rank
+        # advances its share (replica_range) and the job's total is fixed
+        rng = np.random.default_rng(64)
         lipids = rng.integers(1000, 8001, size=64)
         tensions = rng.uniform(0.0, 1.0, size=64)
         paths = []
-        for k in range(64):
+        for k in replica_range(64, rank, world):
             path = os.path.join(tmpdir, f"bench{rank}_{k}.mpd")
-            smd.synth_bilayer(path, 5000 + 64 * rank + k, int(lipids[k]), 3.45, 15.0, 0.01, float(tensions[k]))
+            smd.synth_bilayer(path, 5000 + k, int(lipids[k]), 3.45, 15.0, 0.01, float(tensions[k]))
             paths.append(path)
         cfg = {"workload": "64 independent flat bilayers in one batch, 3-bead lipids per replica uniform in "
                            "[1000, 8000] (seeded), tension uniform in [0, 1], own seed and box each, z 15 sigma, "
@@ -204,21 +234,35 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
+def oracle_time(path, threads, steps):
+    """Seconds of `steps` MD steps of the oracle's restatement of the
+    reference loop (oracle/md_oracle.cpp) on .mpd `path`, timed in a fresh
+    Python process that loads nothing but the oracle: inside this process,
+    beside torch's OpenMP runtime and the CUDA context, the same loop runs
+    about 30 % slower (10.4 M against 14.2 M bead-steps/s on the 60,000-bead
+    bilayer, 16 Arm cores)."""
+    code = ("import ctypes as C, sys\n"
+            "lib = C.CDLL(sys.argv[1])\n"
+            "lib.orc_md_time.argtypes = [C.c_char_p, C.c_int, C.c_int]\n"
+            "lib.orc_md_time.restype = C.c_double\n"
+            "print(lib.orc_md_time(sys.argv[2].encode(), int(sys.argv[3]), int(sys.argv[4])))\n")
+    lib = os.path.join(ROOT, "oracle", "_build", "libsmd_oracle.so")
+    r = subprocess.run([sys.executable, "-c", code, lib, path[:-4], str(threads), str(steps)], capture_output=True,
+                       text=True, env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
+    try:
+        t = float(r.stdout.strip().splitlines()[-1])
+    except (ValueError, IndexError):
+        t = -1.0
+    if r.returncode != 0 or t < 0:
+        raise RuntimeError(f"the oracle could not run {path}: {r.stderr[-300:]}")
+    return t
+
+
 def cpu_baseline(path, threads, target_s=12.0):
     """The oracle's restatement of the reference MD loop on the host cores."""
-    import ctypes as C
-    lib = C.CDLL(os.path.join(ROOT, "oracle", "_build", "libsmd_oracle.so"))
-    lib.orc_md_time.argtypes = [C.c_char_p, C.c_int, C.c_int]
-    lib.orc_md_time.restype = C.c_double
-    name = path[:-4].encode()
-    t = lib.orc_md_time(name, threads, 4)
-    if t < 0:
-        raise RuntimeError(f"the oracle could not run {path}")
+    t = oracle_time(path, threads, 4)
     steps = max(4, int(4 * target_s / max(t, 1e-3)))
-    t = lib.orc_md_time(name, threads, steps)
-    if t < 0:
-        raise RuntimeError(f"the oracle could not run {path}")
-    return steps, t
+    return steps, oracle_time(path, threads, steps)
 
 
 def melt_on_host(path, threads, steps):
@@ -244,10 +288,10 @@ def melt_on_host(path, threads, steps):
 
 def run_reference(args, rank, world):
     """--impl reference: the reference's CPU algorithm (the oracle port of
-    MD.cpp, built here) on all host threads, same workload and metric."""
+    MD.cpp, built here) on all host threads, same workload, config and
+    metric; one bench step is a sample of STEP_MD MD steps."""
     if rank != 0:
         return
-    import softmold_gb300 as smd
     from softmold_gb300 import build
     build.build_oracle()
     with tempfile.TemporaryDirectory() as tmp:
@@ -263,21 +307,19 @@ def run_reference(args, rank, world):
         lib = C.CDLL(os.path.join(ROOT, "oracle", "_build", "libsmd_oracle.so"))
         lib.orc_md_time.argtypes = [C.c_char_p, C.c_int, C.c_int]
         lib.orc_md_time.restype = C.c_double
-        # one bench step: one barostat period (PERIOD MD steps) of the system,
-        # or of one replica of a batch in turn (replicas are independent:
-        # bead-steps and times add)
-        per_step = PERIOD
+        # one bench step: STEP_MD MD steps of the system, or of one replica of
+        # a batch in turn (replicas are independent: bead-steps and times add)
         for k in range(args.warmup):
             lib.orc_md_time(paths[k % len(paths)][:-4].encode(), threads, 2)
         total, units = 0.0, 0
         for k in range(args.steps):
             j = k % len(paths)
-            total += lib.orc_md_time(paths[j][:-4].encode(), threads, per_step)
-            units += len(ms[j].type) * per_step
+            total += lib.orc_md_time(paths[j][:-4].encode(), threads, STEP_MD)
+            units += len(ms[j].type) * STEP_MD
         value = units / total
         n = sum(len(m.type) for m in ms)
         what = f"the {n}-bead workload" if len(ms) == 1 else f"replicas of the {len(ms)}-replica batch in turn"
-        sample = f"{args.steps} samples of {per_step} MD steps of {what}, after {melt} untimed steps from the lattice start"
+        sample = f"{args.steps} samples of {STEP_MD} MD steps of {what}, after {melt} untimed steps from the lattice start"
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
@@ -286,6 +328,27 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }), flush=True)
+
+
+def oracle_forces(ms, pos, boxes):
+    """The oracle's FP64 conservative forces (CellOpt::computeForce +
+    Blob::doChainForce + doBeadForce restated in oracle/smd_oracle.cpp) of
+    every replica at the given state, in input order: the checker behind
+    force_err."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_binding import Oracle
+    orc = Oracle()
+    out, base = [], 0
+    for m, b in zip(ms, boxes):
+        n = len(m.type)
+        g = {"pos": np.ascontiguousarray(pos[base:base + n]), "type": m.type, "box": b, "cutoff": m.cutoff,
+             "n_types": m.n_types, "fconst": m.fconst, "chain_blocks": m.chain_blocks,
+             "chain_consts": m.chain_consts}
+        if m.sphere_index is not None and len(m.sphere_index):
+            g["sphere_index"], g["sphere_consts"] = m.sphere_index, m.sphere_consts
+        out.append(orc.forces(g))
+        base += n
+    return np.concatenate(out)
 
 
 def bench_adjoint(args, s, stream, n, cfg, world, rank, dist):
@@ -318,11 +381,32 @@ def bench_adjoint(args, s, stream, n, cfg, world, rank, dist):
         dist.destroy_process_group()
 
 
+def profile_run(args):
+    """The workload kernel by kernel, for ncu (which cannot see the kernel
+    nodes of graphs with conditional nodes): the default launch
+    configuration (8 lanes per bead, the flat list build with 128 threads),
+    1,001 equilibration steps, then args.profile_run steps."""
+    import softmold_gb300 as smd
+    from softmold_gb300 import build
+    build.build_library()
+    tmp = tempfile.mkdtemp(prefix="smd_prof_")
+    _, ms, _ = workload(args, 0, tmp)
+    s = smd.System(ms if len(ms) > 1 else ms[0], precision=smd.MIXED, skin=args.skin)
+    s.use_graphs(False)
+    s.set_tuning(8, 0)
+    s.prepare()
+    s.advance(1001)
+    r0 = s.rebuilds()
+    s.advance(args.profile_run)
+    print(f"rebuilds {s.rebuilds() - r0} in {args.profile_run} steps; launches {s.launches()}")
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="bilayer20k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -330,6 +414,9 @@ def main():
     ap.add_argument("--skin", type=float, default=0.5)
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the step kernels one by one (for profilers that cannot see kernels in graphs)")
+    ap.add_argument("--profile-run", type=int, default=0, metavar="STEPS",
+                    help="for ncu: equilibrate the workload kernel by kernel with the default launch "
+                         "configuration, run STEPS more MD steps and exit (no timing, no JSON line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -339,6 +426,8 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
+    if args.profile_run:
+        return profile_run(args)
 
     import torch
     torch.cuda.set_device(local)
@@ -353,7 +442,7 @@ def main():
     build.build_library()
 
     tmp = tempfile.mkdtemp(prefix="smd_bench_")
-    paths, ms, cfg = workload(args, rank, tmp)
+    paths, ms, cfg = workload(args, rank, tmp, world)
     m = ms if len(ms) > 1 else ms[0]
     n = sum(len(x.type) for x in ms)
     stream = torch.cuda.Stream()
@@ -370,7 +459,7 @@ def main():
         return bench_adjoint(args, s, stream, n, cfg, world, rank, dist)
 
     def timed_loop(sys_, steps):
-        """`steps` bench steps of PERIOD MD steps each, L2 flushed before each."""
+        """`steps` bench steps of STEP_MD MD steps each, L2 flushed before each."""
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
         l0 = sys_.timing()[2]
@@ -378,13 +467,13 @@ def main():
             for k in range(steps):
                 flush.zero_()
                 starts[k].record(stream)
-                sys_.advance(PERIOD, asynchronous=True)
+                sys_.advance(STEP_MD, asynchronous=True)
                 ends[k].record(stream)
         torch.cuda.synchronize()
         sys_.sync()
         launches = sys_.timing()[2] - l0
-        ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-        return sum(ms), launches
+        ms_ = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+        return sum(ms_), launches
 
     timed_loop(s, W)
     rebuilds0 = s.rebuilds()
@@ -405,16 +494,16 @@ def main():
         dist.barrier()
     rebuilds = s.rebuilds() - rebuilds0
     last_disp, slack = s.list_state()
-    value, _, max_s = job_throughput(n * PERIOD * K, total_ms / 1e3, dist, "cuda")
+    value, _, max_s = job_throughput(n * STEP_MD * K, total_ms / 1e3, dist, "cuda")
     max_ms = 1e3 * max_s
-    # per-kernel times of the pair and integrate passes (profiling mode records
+    # per-launch times of the pair and integrate passes (profiling mode records
     # events around every step, so it launches kernel by kernel, untimed here)
     s.profile(True)
-    timed_loop(s, min(K, 25))
+    timed_loop(s, min(K, 4))
     kernel_ms, kernel_launches, _ = s.timing()
     s.profile(False)
 
-    # FP64 plain form on the same state, and the mixed form's force error
+    # FP64 plain form on the same state
     pos, vel = s.state()
     boxes = [s.box(r) for r in range(len(ms))]  # the boxes of this state (the e2e run below moves them on)
     offs = np.cumsum([0] + [len(x.type) for x in ms])
@@ -431,14 +520,10 @@ def main():
     f_mixed = s.forces()
     p.prepare()
     p.advance(1)  # step % PERIOD == 1, where a barostat period starts
-    fscale = np.abs(f_plain).max()
-    force_err = {"max": float(np.abs(f_mixed - f_plain).max() / fscale),
-                 "rms": float(np.sqrt(np.mean((f_mixed - f_plain) ** 2)) / fscale),
-                 "reference": "plain FP64 GPU form (matches the CPU oracle to 1e-12)"}
-    kp = min(K, 10)
+    kp = min(K, 3)
     timed_loop(p, 1)
     plain_ms, _ = timed_loop(p, kp)
-    plain_value, _, _ = job_throughput(n * PERIOD * kp, plain_ms / 1e3, dist, "cuda")
+    plain_value, _, _ = job_throughput(n * STEP_MD * kp, plain_ms / 1e3, dist, "cuda")
     p.close()
 
     # end to end through the C ABI with host buffers
@@ -461,26 +546,43 @@ def main():
            "d2h_bytes_per_step": int(hp.nbytes + hv.nbytes + 32),
            "md_steps_per_e2e_step": E2E_INTERVAL, "potential_last": e[0]["pair"] + e[0]["bonded"]}
 
+    # the whole step against HBM (176 algorithmic bytes per bead-step), and
+    # the pair + integrate passes alone from their per-launch CUDA events
     peak, peak_kind = load_peaks()
-    achieved = None
+    us_md_step = max_ms * 1e3 / (K * STEP_MD)
+    achieved = value * ALG_BYTES_PER_BEAD_STEP / 1e9
+    prof = STEP_PROFILE.get(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": prof["dram_bytes_per_bead_step"] * n if prof else None,
+                "traffic_per": "MD step, every kernel of the step (DRAM read + write)",
+                "alg_bytes_per_bead_step": ALG_BYTES_PER_BEAD_STEP, "alg_bytes_per_md_step": ALG_BYTES_PER_BEAD_STEP * n,
+                "kernel": "the whole MD step (every kernel, list builds and barostat passes included)",
+                "peak_source": f"{peak_kind} hbm_gbs"}
+    kernels = None
     if kernel_launches:
-        avg_s = kernel_ms / kernel_launches / 1e3
-        achieved = ALG_BYTES_PER_BEAD_STEP * n / avg_s / 1e9
-    traffic = None  # DRAM bytes of one step's force + integrate passes, from the committed ncu summary
-    tf = os.path.join(ROOT, "profiles", "step_kernels_bilayer60k.md")
-    if os.path.exists(tf) and args.workload == "bilayer20k":
-        import re
-        m_ = re.search(r"traffic_bytes_per_bead_step\s*=\s*([0-9.]+)", open(tf).read())
-        if m_:
-            traffic = float(m_.group(1)) * n
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "kernel": "k_force + k_integ (one step's pair pass and CHAIN/Langevin/Verlet pass)",
-                "kernel_avg_us": 1e3 * kernel_ms / kernel_launches if kernel_launches else None,
-                "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_bead_step": ALG_BYTES_PER_BEAD_STEP}
+        avg_us = 1e3 * kernel_ms / kernel_launches
+        kernels = {"k_force + k_integ": {
+            "avg_us_per_md_step": avg_us, "achieved_gbs": ALG_BYTES_PER_BEAD_STEP * n / (avg_us * 1e3),
+            "frac": ALG_BYTES_PER_BEAD_STEP * n / (avg_us * 1e3) / peak, "launch_pairs": kernel_launches,
+            "share_of_step": avg_us / us_md_step}}
+    issue = None
+    if prof and clocks.get("sm_mhz"):
+        inst = prof["warp_inst_per_bead_step"] * n  # per MD step
+        bound_us = inst / (SMS * ISSUE_PER_SM_CLK * clocks["sm_mhz"] * 1e6) * 1e6
+        issue = {"warp_inst_per_md_step": inst, "issue_peak_warp_inst_per_s": SMS * ISSUE_PER_SM_CLK * clocks["sm_mhz"] * 1e6,
+                 "bound_us_per_md_step": bound_us, "measured_us_per_md_step": us_md_step,
+                 "frac": bound_us / us_md_step, "source": prof["source"]}
 
     base = None
+    force_err = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        f_ref = oracle_forces(ms, pos, boxes)
+        fscale = np.abs(f_ref).max()
+        force_err = {"max": float(np.abs(f_mixed - f_ref).max() / fscale),
+                     "rms": float(np.sqrt(np.mean((f_mixed - f_ref) ** 2)) / fscale),
+                     "plain_max": float(np.abs(f_plain - f_ref).max() / fscale),
+                     "reference": "FP64 oracle (the reference's computeForce + doChainForce + doBeadForce restated) "
+                                  "on the bench's final state, relative to max |F|"}
         threads = os.cpu_count() or 1
         # equilibrated state of (a sample of) the replicas, timed one after another
         sample = range(len(ms)) if len(ms) == 1 else range(0, len(ms), 16)
@@ -499,16 +601,18 @@ def main():
                 "sample": f"MD steps of {what} (equilibrated state), oracle port of MD.cpp with OpenMP"}
     s.close()
     if rank == 0:
-        cfg.update({"beads_per_gpu": n, "md_steps_per_bench_step": PERIOD,
-                    "l2": "flushed (256 MiB write) between timed steps",
-                    "skin": args.skin, "parallelism": f"replicas x{world}",
-                    "list_rebuilds_per_md_step": rebuilds / (K * PERIOD), "last_max_displacement": last_disp})
+        run = {"beads_per_gpu": n, "md_steps_per_bench_step": STEP_MD, "us_per_md_step": us_md_step,
+               "l2": "flushed (256 MiB write) between timed steps", "skin": args.skin,
+               "parallelism": (f"replicas split over {world} ranks" if args.workload == "batch64" and world > 1
+                               else f"replicas x{world}"),
+               "list_rebuilds_per_md_step": rebuilds / (K * STEP_MD), "last_max_displacement": last_disp}
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": max_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+i64 fixed-point forces, f64 integrate", "data": "synthetic", "config": cfg,
-            "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": launches,
+            "ms_per_step": max_ms / K, "higher_is_better": True,
+            "scaling": "strong" if args.workload == "batch64" and world > 1 else "weak", "vs_baseline": None,
+            "dtype": "f32+i64 fixed-point forces, f64 integrate", "data": "synthetic", "config": cfg, "run": run,
+            "roofline": roofline, "kernels": kernels, "issue": issue, "cpu_baseline": base, "e2e": e2e,
+            "clocks": clocks, "gpu_launches": launches,
             "plain_fp64": {"value": plain_value, "ms_per_step": plain_ms / kp,
                            "mixed_speedup": value / plain_value},
             "force_err": force_err,

@@ -238,6 +238,46 @@ long smd_rebuild_count(smd_system* h);
  * build (both in sigma; the list is rebuilt when their sum exceeds skin/2). */
 int smd_list_state(smd_system* h, double* max_disp, double* slack);
 
+/* Measurement of one measure step on the device (dataExtraction::compute,
+ * dataExtraction.h:827-1050, 1456-1650, and Kinetic::compute,
+ * include/algorithms/dataCollection.h:666-674), for handles stopped at a
+ * measure step (smd_advance with SMD_STOP_AT_MEASURE): the reductions the
+ * .dat files need, so that only these few numbers cross to the host.
+ * Single-system handles. */
+typedef struct smd_measurement {
+  double kinetic;          /* sum v^2/2 (kinetic_) */
+  double lo[3], hi[3];     /* smallest and largest coordinate per axis (flicker_) */
+  double bond_length_sum;  /* BOND residue bond lengths (lBond_) */
+  int n_bond;
+  double bend_cos_sum, bend_len0_sum, bend_len1_sum;  /* BEND residues (bend_) */
+  int n_bend;
+  int msd;                 /* 1: msd_sum holds the groups' sums (diffusion tracking on) */
+} smd_measurement;
+
+/* Fills *out and, while diffusion is tracked, msd_sum[n_groups] (may be NULL)
+ * with each group's sum of squared displacements since smd_start_diffusion;
+ * adds every bead's kinetic-energy bin int(0.5 v^2 / 1e-4)
+ * (dataExtraction.h:1509-1519) to the run's histogram on the device. */
+int smd_measure(smd_system* h, smd_measurement* out, double* msd_sum);
+
+/* The kinetic-energy histogram smd_measure has accumulated (the
+ * kEnergyDensity_ file written at the end of a run, dataExtraction.h:553-567):
+ * counts of bins of 1e-4 from 0; writes at most cap bins and stores the
+ * number of bins (the last non-empty bin + 1) in *n_bins. */
+int smd_ke_histogram(smd_system* h, long* counts, size_t cap, size_t* n_bins);
+
+/* dataExtraction::startDiffusion (dataExtraction.h:790-804, called by MD.cpp
+ * at the first measure step after 100 tau): from now on every drift adds
+ * v dt to each bead's displacement (nonzero types), as Verlet::first advances
+ * the absolute positions aP (include/algorithms/verlet.h:317-326); box moves
+ * do not rescale it (MD.cpp:555).  Calling it again restarts from zero. */
+int smd_start_diffusion(smd_system* h);
+
+/* The groups of meanSquareDisplacement_ (dataExtraction.h:1524-1650): group g
+ * averages the displacements of beads[offsets[g] .. offsets[g+1]) (file
+ * order; a bead may appear more than once, as the reference counts it). */
+int smd_set_msd_groups(smd_system* h, int n_groups, const int* offsets, const int* beads);
+
 /* Runs the synthetic generators (restating generate/liposome.cpp,
  * generate/bilayer.cpp and generate/continuumSphereAndLiposome.cpp) and
  * writes <path>. */
@@ -320,6 +360,25 @@ int smd_hessian_vector(smd_system* h, const double* w, double* kw);
  * initialTime into out_path (the store of MD.cpp:373-377). */
 int smd_mpd_update_state(const char* in_path, const char* out_path, const double* pos, const double* vel,
                          const double box[3], double time);
+
+/* Run settings of an .mpd that the descriptor does not carry. */
+typedef struct smd_mpd_run {
+  double initial_time, final_time, store_interval, measure_interval;
+  double initial_temp, final_temp, temp_step_interval;
+  int n_bead_residues;  /* BEAD and NANOCORE residues (beadPotential_ output) */
+  int per_type_gamma;   /* 1: gamma came from gammaType (entry 0 applies to every bead) */
+} smd_mpd_run;
+
+/* Reads <path> with the library's .mpd reader (Blob::input restated,
+ * include/system.h:589-1314, through Script::read, scriptFormat.h:79-94) and
+ * fills *desc with the system and every residue the device step runs,
+ * expanded as the `MD` executable expands them (CHAIN blocks, BOND and BEND
+ * terms, one BEAD or NANOCORE residue, external-field terms); run may be
+ * NULL.  The descriptor's arrays belong to *owner until smd_mpd_free(*owner).
+ * A residue type the device step does not run is refused (status 11), as is
+ * a file without gamma (12). */
+int smd_mpd_load(const char* path, smd_system_desc* desc, smd_mpd_run* run, void** owner);
+void smd_mpd_free(void* owner);
 
 /* Reads <name>.mpd and runs it exactly as `MD <name>` would, writing the
  * same .mpd / .xyz / .dat files (MD.cpp:72-755).  precision: smd_precision. */

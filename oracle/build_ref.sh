@@ -8,13 +8,13 @@
 #   _ref/ref_dump    oracle/ref_dump.cpp linked against the reference headers
 #   _ref/liposome    generate/liposome.cpp
 #   _ref/bilayer     generate/bilayer.cpp
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh reference_root   (or $SMD_REFERENCE_ROOT)
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${SMD_REFERENCE_ROOT:-}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
-if [ ! -f "$REF/MD.cpp" ]; then
-  echo "reference sources not found at $REF; nothing to build" >&2
+if [ -z "$REF" ] || [ ! -f "$REF/MD.cpp" ]; then
+  echo "reference sources not found (give their root as the argument or in SMD_REFERENCE_ROOT); nothing to build" >&2
   exit 0
 fi
 mkdir -p "$OUT"

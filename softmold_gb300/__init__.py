@@ -51,6 +51,13 @@ class Energy(C.Structure):
     _fields_ = [("pair", C.c_double), ("bonded", C.c_double), ("sphere", C.c_double), ("kinetic", C.c_double)]
 
 
+class Measurement(C.Structure):
+    _fields_ = [("kinetic", C.c_double), ("lo", C.c_double * 3), ("hi", C.c_double * 3),
+                ("bond_length_sum", C.c_double), ("n_bond", C.c_int),
+                ("bend_cos_sum", C.c_double), ("bend_len0_sum", C.c_double), ("bend_len1_sum", C.c_double),
+                ("n_bend", C.c_int), ("msd", C.c_int)]
+
+
 class McStats(C.Structure):
     _fields_ = [("trials", C.c_long), ("accepted", C.c_long), ("last_dU", C.c_double)]
 
@@ -110,6 +117,12 @@ _SIGS = {
     "smd_md_main": (C.c_int, [C.c_char_p, C.c_int]),
     "smd_pair_forces_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_int,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_mpd_load": (C.c_int, [C.c_char_p, C.POINTER(SystemDesc), C.c_void_p, C.POINTER(C.c_void_p)]),
+    "smd_mpd_free": (None, [C.c_void_p]),
+    "smd_measure": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "smd_ke_histogram": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "smd_start_diffusion": (C.c_int, [C.c_void_p]),
+    "smd_set_msd_groups": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -191,150 +204,53 @@ class Mpd:
     core_consts: np.ndarray | None = None   # (k,22)
 
 
+class MpdRun(C.Structure):
+    _fields_ = [("initial_time", C.c_double), ("final_time", C.c_double), ("store_interval", C.c_double),
+                ("measure_interval", C.c_double), ("initial_temp", C.c_double), ("final_temp", C.c_double),
+                ("temp_step_interval", C.c_double), ("n_bead_residues", C.c_int), ("per_type_gamma", C.c_int)]
+
+
 def read_mpd(path: str) -> Mpd:
-    """Parses the hot-path fields of an .mpd token stream (Blob::input,
-    include/system.h:589-1314)."""
-    toks = open(path).read().split()
-    i = 0
-    vals = {}
-    n_types = n_particles = n_mol = 0
-    pos = vel = typ = None
-    blocks, consts = [], []
-    bond_l, bond_c, bend_l, bend_c = [], [], [], []
-    sph_idx, sph_c = None, None
-    field_l, field_c = [], []
-    core_idx, core_c = None, None
-    fc = uc = None
+    """Reads an .mpd through the library's reader and residue expansion
+    (smd_mpd_load: Blob::input, include/system.h:589-1314, expanded into the
+    terms the device step takes exactly as the `MD` executable does)."""
+    d = SystemDesc()
+    run = MpdRun()
+    owner = C.c_void_p()
+    _check(lib().smd_mpd_load(path.encode(), C.byref(d), C.byref(run), C.byref(owner)), f"smd_mpd_load({path})")
+    try:
+        n, nT = d.n, d.n_types
 
-    def take(k=1):
-        nonlocal i
-        out = toks[i:i + k]
-        i += k
-        return out
+        def arr(ptr, count, dtype, shape=None):
+            if count <= 0 or not ptr:
+                return np.zeros(shape if shape else (0,), dtype)
+            a = np.ctypeslib.as_array(ptr, shape=(count,)).astype(dtype, copy=True)
+            return a.reshape(shape) if shape else a
 
-    layouts = {6: (2, 2), 7: (3, 2), 8: (3, 4), 9: (1, None), 10: (1, 1), 11: (1, 4), 12: (2, 5), 13: (1, 4),
-               14: (1, 4), 15: (1, None), 16: (3, 4), 17: (2, 2), 18: (1, None), 19: (2, 2)}
-    while i < len(toks):
-        kw = take()[0]
-        if kw == "end":
-            break
-        if kw in ("gamma", "initialTemp", "finalTemp", "cutoff", "initialTime", "finalTime", "deltaT",
-                  "storeInterval", "measureInterval", "deltaLXY", "removeSolvent", "tempStepInterval", "tension"):
-            vals[kw] = float(take()[0])
-        elif kw in ("seed", "nTypes", "nMolecules", "nParticles"):
-            vals[kw] = int(take()[0])
-            n_types = vals.get("nTypes", n_types)
-            n_particles = vals.get("nParticles", n_particles)
-            n_mol = vals.get("nMolecules", n_mol)
-        elif kw == "periodic":
-            take()
-        elif kw == "size":
-            vals["size"] = [float(x) for x in take(3)]
-        elif kw == "twoBodyFconst":
-            fc = np.array(take(6 * n_types * n_types), dtype=np.float64)
-        elif kw == "twoBodyUconst":
-            uc = np.array(take(6 * n_types * n_types), dtype=np.float64)
-        elif kw == "positions":
-            a = np.array(take(4 * n_particles), dtype=np.float64).reshape(-1, 4)
-            typ = a[:, 0].astype(np.int32)
-            pos = np.ascontiguousarray(a[:, 1:])
-        elif kw == "velocities":
-            vel = np.array(take(3 * n_particles), dtype=np.float64).reshape(-1, 3)
-        elif kw == "molecule":
-            for _ in range(n_mol):
-                mt = int(take()[0])
-                if mt not in layouts:
-                    take(4)
-                    continue
-                nb = int(take()[0])
-                nidx, ncon = layouts[mt]
-                if ncon is None:
-                    ncon = {9: 22 * n_types * n_types, 15: 6 * n_types, 18: 22 * nb}[mt]
-                c = np.array(take(ncon), dtype=np.float64)
-                b = np.array(take(nidx * nb), dtype=np.int64).reshape(nb, nidx)
-                if mt == 8:
-                    for row in b:
-                        blocks.append(row[:3])
-                        consts.append(c[:4])
-                elif mt == 6:
-                    bond_l.extend(b[:, :2].tolist())
-                    bond_c.extend([c[:2].tolist()] * nb)
-                elif mt == 7:
-                    bend_l.extend(b[:, :3].tolist())
-                    bend_c.extend([c[:2].tolist()] * nb)
-                elif mt == 9:
-                    sph_idx = b[:, 0].astype(np.int32)
-                    sph_c = c
-                elif mt in (11, 15, 16, 17, 19):
-                    field_terms(mt, b, c, typ, field_l, field_c)
-                elif mt == 18:
-                    core_idx = b[:, 0].astype(np.int32)
-                    core_c = c.reshape(nb, 22)
-        elif kw == "banana":
-            pass
-        elif kw == "solventGamma":
-            take(2)
-        elif kw == "gammaType":
-            vals["gammaType"] = [float(x) for x in take(n_types)]
-        else:
-            raise SmdError(f"unknown keyword {kw}")
-    gamma = vals.get("gamma", 0.0)
-    if not gamma > 0 and "gammaType" in vals:
-        gamma = vals["gammaType"][0]
-    return Mpd(n_types=n_types, pos=pos, vel=vel, type=typ, box=np.array(vals["size"]), cutoff=vals["cutoff"],
-               fconst=fc, uconst=uc,
-               chain_blocks=np.array(blocks, dtype=np.int32).reshape(-1, 3),
-               chain_consts=np.array(consts, dtype=np.float64).reshape(-1, 4),
-               dt=vals["deltaT"], gamma=gamma, temperature=vals["initialTemp"], seed=vals["seed"],
-               tension=vals.get("tension", 0.0), delta_lxy=vals.get("deltaLXY", 0.0),
-               initial_time=vals.get("initialTime", 0.0), final_time=vals.get("finalTime", 0.0),
-               sphere_index=sph_idx, sphere_consts=sph_c,
-               bonds=np.array(bond_l, np.int32).reshape(-1, 2) if bond_l else None,
-               bond_consts=np.array(bond_c, np.float64).reshape(-1, 2) if bond_c else None,
-               bends=np.array(bend_l, np.int32).reshape(-1, 3) if bend_l else None,
-               bend_consts=np.array(bend_c, np.float64).reshape(-1, 2) if bend_c else None,
-               fields=np.array(field_l, np.int32).reshape(-1, 3) if field_l else None,
-               field_consts=np.array(field_c, np.float64).reshape(-1, 8) if field_c else None,
-               core_index=core_idx, core_consts=core_c)
-
-
-def field_terms(mt, b, c, typ, out_l, out_c):
-    """Terms of one external-field residue (molecule type mt, index rows b,
-    constants c), in the order the reference applies them:
-      BOUNDARY 11 (Blob::doBoundaryForce, include/system.h:2335-2349): one
-        term per bead, constants {dim, centre, -, k};
-      FLOATING_BASE 15 (doFloatingBaseForce, :2403-2422): one term per bead,
-        the 6 constants of the bead's type, then the residue's first constant
-        (the potential's z offset, :2437);
-      ZTORQUE 16 (doZTorqueForce, :2626-2664): one term per bond (l, l+1) of
-        each chain but its last, constants {a, b, c, z0};
-      ZPOWERPOTENTIAL 17 (doZPowerForce, :2693-2716): one term per bead of each
-        {start, count} block, constants {c0, c1};
-      BALL 19 (doBallForce, :1937-1971): one term per bond (first of the
-        residue's first bond, this bond's second), constants {r0, k, this
-        bond's first} (the potential, :2750-2779, takes each bond's own first)."""
-    pad = lambda v: list(v) + [0.0] * (8 - len(v))  # noqa: E731
-    for row in b:
-        if mt == 11:
-            out_l.append((11, int(row[0]), -1))
-            out_c.append(pad(c[:4]))
-        elif mt == 15:
-            t = int(typ[int(row[0])])
-            out_l.append((15, int(row[0]), -1))
-            out_c.append(pad(list(c[6 * t:6 * t + 6]) + [c[0]]))
-        elif mt == 19:
-            out_l.append((19, int(b[0][0]), int(row[1])))
-            out_c.append(pad([c[0], c[1], float(row[0])]))
-        elif mt == 17:
-            for k in range(int(row[0]), int(row[0]) + int(row[1])):
-                out_l.append((17, k, -1))
-                out_c.append(pad(c[:2]))
-        else:
-            s0, nch, ln = int(row[0]), int(row[1]), int(row[2])
-            for k in range(s0, s0 + ln * nch, ln):
-                for l in range(k, k + ln - 2):
-                    out_l.append((16, l, l + 1))
-                    out_c.append(pad(c[:4]))
+        sph = arr(d.sphere_index, d.n_spheres, np.int32) if d.n_spheres > 0 else None
+        sph_c = None
+        if d.n_spheres > 0:
+            sph_c = arr(d.sphere_consts, 22 * (d.n_spheres if d.sphere_nanocore else nT * nT), np.float64)
+        return Mpd(n_types=nT, pos=arr(d.pos, 3 * n, np.float64, (n, 3)), vel=arr(d.vel, 3 * n, np.float64, (n, 3)),
+                   type=arr(d.type, n, np.int32), box=np.array(d.box[:]), cutoff=d.cutoff,
+                   fconst=arr(d.fconst, 6 * nT * nT, np.float64), uconst=arr(d.uconst, 6 * nT * nT, np.float64),
+                   chain_blocks=arr(d.chain_blocks, 3 * d.n_chain_blocks, np.int32, (d.n_chain_blocks, 3)),
+                   chain_consts=arr(d.chain_consts, 4 * d.n_chain_blocks, np.float64, (d.n_chain_blocks, 4)),
+                   dt=d.dt, gamma=d.gamma, temperature=d.temperature, seed=int(d.seed), tension=d.tension,
+                   delta_lxy=d.delta_lxy, initial_time=run.initial_time, final_time=run.final_time,
+                   sphere_index=None if d.sphere_nanocore else sph,
+                   sphere_consts=None if d.sphere_nanocore else sph_c,
+                   bonds=arr(d.bonds, 2 * d.n_bonds, np.int32, (d.n_bonds, 2)) if d.n_bonds else None,
+                   bond_consts=arr(d.bond_consts, 2 * d.n_bonds, np.float64, (d.n_bonds, 2)) if d.n_bonds else None,
+                   bends=arr(d.bends, 3 * d.n_bends, np.int32, (d.n_bends, 3)) if d.n_bends else None,
+                   bend_consts=arr(d.bend_consts, 2 * d.n_bends, np.float64, (d.n_bends, 2)) if d.n_bends else None,
+                   fields=arr(d.fields, 3 * d.n_fields, np.int32, (d.n_fields, 3)) if d.n_fields else None,
+                   field_consts=arr(d.field_consts, 8 * d.n_fields, np.float64, (d.n_fields, 8)) if d.n_fields
+                   else None,
+                   core_index=sph if d.sphere_nanocore else None,
+                   core_consts=sph_c.reshape(-1, 22) if d.sphere_nanocore else None)
+    finally:
+        lib().smd_mpd_free(owner)
 
 
 class System:
@@ -534,6 +450,35 @@ class System:
         s = McStats()
         _check(lib().smd_mc_stats_get(self.h, replica, C.byref(s)), "smd_mc_stats_get")
         return dict(trials=s.trials, accepted=s.accepted, last_dU=s.last_dU)
+
+    def measure(self, n_groups=0):
+        """smd_measure on a handle stopped at a measure step: the reductions
+        of the .dat files as a dict (and 'msd_sum' per group while diffusion
+        is tracked)."""
+        m = Measurement()
+        msd = np.zeros(max(n_groups, 1))
+        _check(lib().smd_measure(self.h, C.byref(m), msd.ctypes.data if n_groups else None), "smd_measure")
+        out = dict(kinetic=m.kinetic, lo=np.array(m.lo[:]), hi=np.array(m.hi[:]), bond_length_sum=m.bond_length_sum,
+                   n_bond=m.n_bond, bend_cos_sum=m.bend_cos_sum, bend_len0_sum=m.bend_len0_sum,
+                   bend_len1_sum=m.bend_len1_sum, n_bend=m.n_bend, msd=bool(m.msd))
+        if m.msd:
+            out["msd_sum"] = msd[:n_groups].copy()
+        return out
+
+    def ke_histogram(self):
+        n = C.c_size_t(0)
+        _check(lib().smd_ke_histogram(self.h, None, 0, C.byref(n)), "smd_ke_histogram")
+        out = np.zeros(max(n.value, 1), np.int64)
+        _check(lib().smd_ke_histogram(self.h, out.ctypes.data, n.value, C.byref(n)), "smd_ke_histogram")
+        return out[:n.value]
+
+    def start_diffusion(self):
+        _check(lib().smd_start_diffusion(self.h), "smd_start_diffusion")
+
+    def set_msd_groups(self, offsets, beads):
+        o = np.ascontiguousarray(offsets, np.int32)
+        b = np.ascontiguousarray(beads, np.int32)
+        _check(lib().smd_set_msd_groups(self.h, len(o) - 1, o.ctypes.data, b.ctypes.data), "smd_set_msd_groups")
 
     def launches(self):
         return self.timing()[2]

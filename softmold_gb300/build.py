@@ -23,7 +23,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_OUT = os.path.join(ORACLE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-HOST_SRC = ["mpd_io.cpp", "observables.cpp", "synth.cpp", "md_driver.cpp", "abi_host.cpp"]
+HOST_SRC = ["mpd_io.cpp", "mpd_desc.cpp", "observables.cpp", "synth.cpp", "md_driver.cpp", "abi_host.cpp"]
 CU_SRC = ["smd_api.cu", "smd_static.cu"]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 
@@ -101,11 +101,22 @@ def build_oracle(force: bool = False) -> str:
     return lib
 
 
-def build_reference_tools(ref_root: str = "/root/reference") -> bool:
+def reference_root(ref_root: str | None = None) -> str | None:
+    """The reference checkout: the argument, else $SMD_REFERENCE_ROOT, else a
+    directory named `reference` beside this repository; None when none of
+    them holds the reference's MD.cpp."""
+    for cand in (ref_root, os.environ.get("SMD_REFERENCE_ROOT"), os.path.join(os.path.dirname(ROOT), "reference")):
+        if cand and os.path.exists(os.path.join(cand, "MD.cpp")):
+            return cand
+    return None
+
+
+def build_reference_tools(ref_root: str | None = None) -> bool:
     """Compiles the reference's own tools into oracle/_ref (only where present)."""
-    if not os.path.exists(os.path.join(ref_root, "MD.cpp")):
+    root = reference_root(ref_root)
+    if root is None:
         return False
-    _run(["bash", os.path.join(ORACLE, "build_ref.sh"), ref_root])
+    _run(["bash", os.path.join(ORACLE, "build_ref.sh"), root])
     return True
 
 

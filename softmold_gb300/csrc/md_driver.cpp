@@ -6,16 +6,28 @@
 // measurements every measureInterval, the temperature ramp, and the MC box
 // move every 8 steps; at the end resizeHist_<name>.dat, the acceptance ratio on
 // stderr and kEnergyDensity_<name>.dat.  The device advances in chunks between
-// those events; the state is read back only at stores and measurements.
+// those events.  The state is read back only at stores: a measurement reads
+// back the device's reductions (smd_measure, smd_compute_energy), and from the
+// first measurement after 100 tau on the device tracks each bead's
+// displacement for meanSquareDisplacement_<name>.dat (MD.cpp:64, 538-539).
+//
+// SMD_REFERENCE_NOISE=1 (a test mode, one step per call, slow) drives the
+// Langevin term with the noise of a one-thread reference run, 2 u - 1 with u
+// from MTRand(seed).rand53() for each bead's x, y, z in turn
+// (include/algorithms/langevin.h:284-331), through smd_set_noise_once, so
+// that a run can be compared with the reference's output files line by line.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <ctime>
 #include <iostream>
 #include <string>
 #include <vector>
 
 #include "../../include/softmold_gb300.h"
+#include "mpd_desc.h"
 #include "mpd_io.h"
+#include "mt19937.h"
 #include "observables.h"
 
 namespace {
@@ -31,47 +43,6 @@ int die(const std::string& what) {
   return 1;
 }
 
-// Terms of one external-field residue, in the order the reference applies
-// them (kind = the molecule type; 8 constants each):
-//   BOUNDARY (Blob::doBoundaryForce, include/system.h:2335-2349): one term per
-//     bead, constants {dim, centre, -, k};
-//   FLOATING_BASE (doFloatingBaseForce, :2403-2422): one term per bead, the 6
-//     constants of the bead's type, then the residue's first constant (the
-//     potential's z offset, doFloatingBasePotential :2437);
-//   ZTORQUE (doZTorqueForce, :2626-2664): one term per bond (l, l+1) of each
-//     chain but its last, constants {a, b, c, z0};
-//   ZPOWERPOTENTIAL (doZPowerForce, :2693-2716): one term per bead of each
-//     {start, count} block, constants {c0, c1};
-//   BALL (doBallForce, :1937-1971): one term per bond (the residue's first
-//     bond's first bead, this bond's second), constants {r0, k, this bond's
-//     first} (the potential, doBallPotential :2750-2779, takes each bond's
-//     own first).
-void field_terms(const smd::Molecule& m, const std::vector<int>& type, std::vector<int>& idx,
-                 std::vector<double>& cs) {
-  auto push = [&](int a, int b, std::initializer_list<double> c) {
-    idx.insert(idx.end(), {m.type, a, b});
-    std::vector<double> v(c);
-    v.resize(8, 0.0);
-    cs.insert(cs.end(), v.begin(), v.end());
-  };
-  const std::vector<double>& C = m.constants;
-  for (const auto& b : m.bonds) {
-    if (m.type == smd::MOL_BOUNDARY) {
-      push(b[0], -1, {C[0], C[1], C[2], C[3]});
-    } else if (m.type == smd::MOL_FLOATING_BASE) {
-      const double* t = C.data() + 6 * type[b[0]];
-      push(b[0], -1, {t[0], t[1], t[2], t[3], t[4], t[5], C[0]});
-    } else if (m.type == smd::MOL_ZPOWERPOTENTIAL) {
-      for (int k = b[0]; k < b[0] + b[1]; ++k) push(k, -1, {C[0], C[1]});
-    } else if (m.type == smd::MOL_BALL) {
-      push(m.bonds[0][0], b[1], {C[0], C[1], (double)b[0]});
-    } else {
-      for (int k = b[0]; k < b[0] + b[2] * b[1]; k += b[2])
-        for (int l = k; l < k + b[2] - 2; ++l) push(l, l + 1, {C[0], C[1], C[2], C[3]});
-    }
-  }
-}
-
 }  // namespace
 
 extern "C" int smd_md_main(const char* name_c, int precision) {
@@ -82,61 +53,14 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
     std::cout << err << "\n";
     return 1;
   }
-  // residues on the device path
-  std::vector<int> blocks;
-  std::vector<double> consts;
-  std::vector<int> sphere_idx, bond_idx, bend_idx;
-  std::vector<double> bond_c, bend_c;
-  std::vector<int> field_idx;
-  std::vector<double> field_c;
-  const std::vector<double>* sphere_consts = nullptr;
-  bool nanocore = false;
-  int n_bead_res = 0;  // BEAD and NANOCORE residues: the beadPotential_ output (dataExtraction.h:1031-1040)
-  for (const smd::Molecule& m : S.mol) {
-    if (m.type == smd::MOL_CHAIN) {
-      for (const auto& b : m.bonds) {
-        blocks.insert(blocks.end(), {b[0], b[1], b[2]});
-        consts.insert(consts.end(), m.constants.begin(), m.constants.begin() + 4);
-      }
-    } else if (m.type == smd::MOL_BOND) {
-      for (const auto& b : m.bonds) {
-        bond_idx.insert(bond_idx.end(), {b[0], b[1]});
-        bond_c.insert(bond_c.end(), m.constants.begin(), m.constants.begin() + 2);
-      }
-    } else if (m.type == smd::MOL_BEND) {
-      for (const auto& b : m.bonds) {
-        bend_idx.insert(bend_idx.end(), {b[0], b[1], b[2]});
-        bend_c.insert(bend_c.end(), m.constants.begin(), m.constants.begin() + 2);
-      }
-    } else if (m.type == smd::MOL_BEAD || m.type == smd::MOL_NANOCORE) {
-      if (sphere_consts) {
-        std::cout << "Error(MD): more than one BEAD or NANOCORE residue is not supported on the GPU step\n";
-        return 1;
-      }
-      for (const auto& b : m.bonds) sphere_idx.push_back(b[0]);
-      sphere_consts = &m.constants;
-      nanocore = (m.type == smd::MOL_NANOCORE);
-      ++n_bead_res;
-    } else if (m.type == smd::MOL_BOUNDARY || m.type == smd::MOL_FLOATING_BASE || m.type == smd::MOL_ZTORQUE ||
-               m.type == smd::MOL_ZPOWERPOTENTIAL || m.type == smd::MOL_BALL) {
-      field_terms(m, S.type, field_idx, field_c);
-    } else if (m.type != smd::MOL_SOLID) {
-      std::cout << "Error(MD): molecule type " << m.type
-                << " is not supported on the GPU step (supported: CHAIN, BOND, BEND, BEAD, NANOCORE, "
-                   "BOUNDARY, FLOATING_BASE, ZTORQUE, ZPOWERPOTENTIAL, BALL)\n";
-      return 1;
-    }
+  // residues on the device path, expanded as smd_mpd_load expands them
+  smd::MpdResidues res;
+  if (int rc = smd::mpd_residues(S, res, err)) {
+    std::cout << err << "\n";
+    return rc == 2 ? 0 : 1;  // the reference exits with status 0 when gamma is missing
   }
-  double gamma = S.gamma;
-  bool perTypeGamma = false;
-  if (!(S.gamma > 0)) {
-    if (!S.present[smd::CMD_GAMMATYPE]) {
-      std::cout << "Error(main): No gamma available!\n";
-      return 0;
-    }
-    gamma = S.gammaType[0];  // the reference applies entry 0 to every bead
-    perTypeGamma = true;
-  }
+  const int n_bead_res = res.n_bead_res;
+  const bool perTypeGamma = res.per_type_gamma;
   const int N = S.nParticles;
   const int endInt = int(S.finalTime / S.deltaT + 0.0000001);
   const int startInt = int(S.initialTime / S.deltaT + 0.0000001);
@@ -153,40 +77,8 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
     return 1;
   }
 
-  smd_system_desc d{};
-  d.n = N;
-  d.n_types = S.nTypes;
-  d.pos = S.pos.data();
-  d.vel = S.vel.data();
-  d.type = S.type.data();
-  for (int k = 0; k < 3; ++k) d.box[k] = S.size[k];
-  d.cutoff = S.cutoff;
-  d.fconst = S.twoBodyFconst.data();
-  d.uconst = S.twoBodyUconst.data();
-  d.n_chain_blocks = (int)blocks.size() / 3;
-  d.chain_blocks = blocks.data();
-  d.chain_consts = consts.data();
-  d.n_spheres = (int)sphere_idx.size();
-  d.sphere_index = sphere_idx.data();
-  d.sphere_consts = sphere_consts ? sphere_consts->data() : nullptr;
-  d.sphere_nanocore = nanocore ? 1 : 0;
-  d.n_bonds = (int)bond_idx.size() / 2;
-  d.bonds = bond_idx.data();
-  d.bond_consts = bond_c.data();
-  d.n_bends = (int)bend_idx.size() / 3;
-  d.bends = bend_idx.data();
-  d.bend_consts = bend_c.data();
-  d.n_fields = (int)field_idx.size() / 3;
-  d.fields = field_idx.data();
-  d.field_consts = field_c.data();
-  d.dt = S.deltaT;
-  d.gamma = gamma;
-  d.temperature = S.initialTemp;
-  d.seed = (uint32_t)S.seed;
-  d.tension = S.tension;
-  d.delta_lxy = S.deltaLXY;
-  d.resize_rate = 8;
-  d.first_step = startInt;
+  smd_system_desc d;
+  smd::mpd_descriptor(S, res, d);
   smd_system* h = nullptr;
   if (smd_create(&d, precision, &h)) return die("smd_create");
 
@@ -194,10 +86,26 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   const std::string frames = "frames_" + name + ".xyz";
   std::vector<double> pos(3 * (size_t)N), vel(3 * (size_t)N);
   double box[3];
+  std::vector<int> msd_off, msd_beads;
+  smd::msd_groups(S, msd_off, msd_beads);
+  if (smd_set_msd_groups(h, (int)S.mol.size(), msd_off.data(), msd_beads.data())) return die("smd_set_msd_groups");
+  std::vector<double> msd_sum(S.mol.size() + 1, 0.0);
+  bool diffusion = false;
+
+  const char* rn = std::getenv("SMD_REFERENCE_NOISE");
+  const bool ref_noise = rn && rn[0] == '1';
+  smd::Mt19937 lang((uint32_t)S.seed);
+  std::vector<double> psi(ref_noise ? 3 * (size_t)N : 0);
+  auto feed_noise = [&]() -> int {  // one step's draws, bead by bead, x y z
+    if (!ref_noise) return 0;
+    for (double& q : psi) q = 2.0 * lang.rand53() - 1.0;
+    return smd_set_noise_once(h, psi.data());
+  };
 
   // start-up (MD.cpp:186-308)
   smd_energy e0;
   const bool t0 = (S.initialTime == 0);
+  if (feed_noise()) return die("smd_set_noise_once");
   if (smd_prepare(h, t0 ? 0 : 1, t0 ? &e0 : nullptr)) return die("smd_prepare");
   if (t0) {
     obs.compute(S, S.initialTime, S.pos.data(), S.vel.data(), S.pos.data(), e0.pair + e0.bonded + e0.sphere,
@@ -231,7 +139,8 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
     }
     // next iteration that needs the host before its force pass
     long long next = it + 1;
-    while (next <= endInt && !is_store(next) && !is_temp(next)) ++next;
+    while (!ref_noise && next <= endInt && !is_store(next) && !is_temp(next)) ++next;
+    if (feed_noise()) return die("smd_set_noise_once");
     long long m = it;
     while (m < next && !is_measure(m)) ++m;
     if (m < next && m <= endInt) {
@@ -240,12 +149,31 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
       const time_t last = current;
       current = time(NULL);
       std::cerr << S.initialTime << '\t' << current - last << std::endl;
+      // dataCollection.startDiffusion() before compute() (MD.cpp:538-539)
+      if (S.initialTime > 100.0 && !diffusion) {
+        if (smd_start_diffusion(h)) return die("smd_start_diffusion");
+        diffusion = true;
+      }
       smd_energy e;
-      if (smd_get_state(h, pos.data(), vel.data()) || smd_get_box(h, 0, box) || smd_compute_energy(h, &e))
+      smd_measurement dm;
+      if (smd_get_box(h, 0, box) || smd_compute_energy(h, &e) || smd_measure(h, &dm, msd_sum.data()))
         return die("measure");
       for (int k = 0; k < 3; ++k) S.size[k] = box[k];
-      obs.compute(S, S.initialTime, pos.data(), vel.data(), pos.data(), e.pair + e.bonded + e.sphere, e.sphere,
-                  n_bead_res);
+      smd::Measurement mm;
+      mm.kinetic = dm.kinetic;
+      for (int k = 0; k < 3; ++k) {
+        mm.lo[k] = dm.lo[k];
+        mm.hi[k] = dm.hi[k];
+      }
+      mm.lbond = dm.bond_length_sum;
+      mm.n_bond = dm.n_bond;
+      mm.cos_bend = dm.bend_cos_sum;
+      mm.l_bend0 = dm.bend_len0_sum;
+      mm.l_bend1 = dm.bend_len1_sum;
+      mm.n_bend = dm.n_bend;
+      mm.msd = dm.msd != 0;
+      if (mm.msd) mm.msd_sum.assign(msd_sum.begin(), msd_sum.begin() + S.mol.size());
+      obs.write(S, S.initialTime, e.pair + e.bonded + e.sphere, e.sphere, n_bead_res, mm);
       current = time(NULL);
       if (smd_advance(h, 0, 0)) return die("smd_advance");
       it = m + 1;
@@ -281,6 +209,15 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
     }
   }
   std::cerr << "Resize acceptance ratio: " << (double)st.accepted / (double)st.trials << std::endl;
+  // the measurements' kinetic-energy bins: the t = 0 measurement's (host) and
+  // the loop's (device)
+  size_t nb = 0;
+  if (smd_ke_histogram(h, nullptr, 0, &nb)) return die("smd_ke_histogram");
+  std::vector<long> dev_hist(nb);
+  if (nb > 0 && smd_ke_histogram(h, dev_hist.data(), nb, &nb)) return die("smd_ke_histogram");
+  std::vector<long>& hist = obs.ke_histogram();
+  if (hist.size() < nb) hist.resize(nb, 0);
+  for (size_t k = 0; k < nb; ++k) hist[k] += dev_hist[k];
   obs.finish();
   smd_destroy(h);
   return 0;

@@ -11,16 +11,37 @@ void Observables::append(const std::string& prefix, const std::string& line) {
   f << line;
 }
 
+void msd_groups(const MpdSystem& sys, std::vector<int>& offsets, std::vector<int>& beads) {
+  offsets.assign(1, 0);
+  beads.clear();
+  for (const Molecule& m : sys.mol) {
+    if (m.type == MOL_BOND) {
+      for (const auto& b : m.bonds) beads.insert(beads.end(), {b[0], b[1]});
+    } else if (m.type == MOL_BEND) {
+      for (const auto& b : m.bonds) beads.insert(beads.end(), {b[0], b[1], b[2]});
+    } else if (m.type == MOL_CHAIN) {
+      for (const auto& b : m.bonds)
+        for (int j = b[0]; j < b[0] + b[2] * b[1]; ++j) beads.push_back(j);
+    } else if (m.type == MOL_BEAD || m.type == MOL_NANOCORE) {
+      for (const auto& b : m.bonds) beads.push_back(b[0]);
+    }
+    offsets.push_back((int)beads.size());
+  }
+}
+
 void Observables::compute(const MpdSystem& sys, double time, const double* p, const double* v,
                           const double* ap, double pot, double bead_pot, int n_bead_res) {
+  Measurement m;
+  aggregate(sys, p, v, ap, m);
+  write(sys, time, pot, bead_pot, n_bead_res, m);
+}
+
+void Observables::aggregate(const MpdSystem& sys, const double* p, const double* v, const double* ap,
+                            Measurement& out) {
   const int n = sys.nParticles;
   const double* s = sys.size;
   // BOND lengths and BEND angles (dataExtraction.h:860-940); CHAIN residues
   // contribute to neither.
-  double lBond = 0;
-  int nBond = 0;
-  double cosBend = 0, lBend0 = 0, lBend1 = 0;
-  int nBend = 0;
   auto wrap = [&](double& d, double L) {
     if (d >= L / 2.0) d -= L;
     if (d <= -L / 2.0) d += L;
@@ -36,8 +57,8 @@ void Observables::compute(const MpdSystem& sys, double time, const double* p, co
         wrap(dz, s[2]);
         priv += std::sqrt(dx * dx + dy * dy + dz * dz);
       }
-      lBond += priv;
-      nBond += (int)m.bonds.size();
+      out.lbond += priv;
+      out.n_bond += (int)m.bonds.size();
     } else if (m.type == MOL_BEND) {
       for (const auto& b : m.bonds) {
         double da[3], db[3];
@@ -49,13 +70,59 @@ void Observables::compute(const MpdSystem& sys, double time, const double* p, co
         for (int d = 0; d < 3; ++d) wrap(db[d], s[d]);
         const double ra = std::sqrt(da[0] * da[0] + da[1] * da[1] + da[2] * da[2]);
         const double rb = std::sqrt(db[0] * db[0] + db[1] * db[1] + db[2] * db[2]);
-        lBend0 += ra;
-        lBend1 += rb;
-        cosBend += (da[0] * db[0] + da[1] * db[1] + da[2] * db[2]) / (ra * rb);
+        out.l_bend0 += ra;
+        out.l_bend1 += rb;
+        out.cos_bend += (da[0] * db[0] + da[1] * db[1] + da[2] * db[2]) / (ra * rb);
       }
-      nBend += (int)m.bonds.size();
+      out.n_bend += (int)m.bonds.size();
     }
   }
+  // Kinetic<T>::compute (include/algorithms/dataCollection.h:666-674)
+  out.kinetic = 0;
+  for (int i = 0; i < n; ++i)
+    out.kinetic += ((v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]) / 2.0);
+  // bounding box (dataExtraction.h:1456-1488)
+  for (int d = 0; d < 3; ++d) {
+    out.lo[d] = s[d];
+    out.hi[d] = 0;
+  }
+  for (int i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      if (p[3 * i + d] < out.lo[d]) out.lo[d] = p[3 * i + d];
+      if (p[3 * i + d] > out.hi[d]) out.hi[d] = p[3 * i + d];
+    }
+  if (ap) {
+    // per-bead kinetic-energy histogram (dataExtraction.h:1509-1519)
+    for (int i = 0; i < n; ++i) {
+      const int part = (int)(0.5 * (v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] +
+                                    v[3 * i + 2] * v[3 * i + 2]) /
+                             0.0001);
+      while ((int)ke_hist_.size() <= part) ke_hist_.push_back(0);
+      ke_hist_[part]++;
+    }
+  }
+  out.msd = ap && !msd_start_.empty();
+  if (out.msd) {
+    // mean square displacement per residue (dataExtraction.h:1524-1650), in
+    // the reference's order within each molecule
+    if (msd_off_.empty()) msd_groups(sys, msd_off_, msd_beads_);
+    out.msd_sum.assign(msd_off_.size() - 1, 0.0);
+    for (size_t g = 0; g + 1 < msd_off_.size(); ++g) {
+      double msd = 0;
+      for (int k = msd_off_[g]; k < msd_off_[g + 1]; ++k) {
+        const int j = msd_beads_[k];
+        const double dx = ap[3 * j] - msd_start_[3 * j], dy = ap[3 * j + 1] - msd_start_[3 * j + 1],
+                     dz = ap[3 * j + 2] - msd_start_[3 * j + 2];
+        msd += dx * dx + dy * dy + dz * dz;
+      }
+      out.msd_sum[g] = msd;
+    }
+  }
+}
+
+void Observables::write(const MpdSystem& sys, double time, double pot, double bead_pot, int n_bead_res,
+                        const Measurement& m) {
+  const double* s = sys.size;
   {
     std::ostringstream o;
     o << time << '\t' << pot << '\n';
@@ -68,13 +135,14 @@ void Observables::compute(const MpdSystem& sys, double time, const double* p, co
   }
   {
     std::ostringstream o;
-    o << time << '\t' << (lBond / (double)nBond) << '\n';
+    o << time << '\t' << (m.lbond / (double)m.n_bond) << '\n';
     append("lBond_", o.str());
   }
-  if (nBend > 1) {
-    cosBend /= (double)nBend;
-    lBend0 /= (double)nBend;
-    lBend1 /= (double)nBend;
+  double cosBend = m.cos_bend, lBend0 = m.l_bend0, lBend1 = m.l_bend1;
+  if (m.n_bend > 1) {
+    cosBend /= (double)m.n_bend;
+    lBend0 /= (double)m.n_bend;
+    lBend1 /= (double)m.n_bend;
   }
   {
     std::ostringstream o;
@@ -92,71 +160,23 @@ void Observables::compute(const MpdSystem& sys, double time, const double* p, co
     append("temp_", o.str());
   }
   {
-    // Kinetic<T>::compute (include/algorithms/dataCollection.h:666-674)
-    double ke = 0;
-    for (int i = 0; i < n; ++i)
-      ke += ((v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]) / 2.0);
     std::ostringstream o;
-    o << time << '\t' << ke << '\n';
+    o << time << '\t' << m.kinetic << '\n';
     append("kinetic_", o.str());
   }
   {
-    // bounding box extents (dataExtraction.h:1456-1488)
-    double mn[3] = {s[0], s[1], s[2]}, mx[3] = {0, 0, 0};
-    for (int i = 0; i < n; ++i)
-      for (int d = 0; d < 3; ++d) {
-        if (p[3 * i + d] < mn[d]) mn[d] = p[3 * i + d];
-        if (p[3 * i + d] > mx[d]) mx[d] = p[3 * i + d];
-      }
     std::ostringstream o;
-    o << time << '\t' << mx[0] - mn[0] << '\t' << mx[1] - mn[1] << '\t' << mx[2] - mn[2] << '\n';
+    o << time << '\t' << m.hi[0] - m.lo[0] << '\t' << m.hi[1] - m.lo[1] << '\t' << m.hi[2] - m.lo[2] << '\n';
     append("flicker_", o.str());
   }
-  if (ap) {
-    // per-bead kinetic-energy histogram (dataExtraction.h:1509-1519)
-    for (int i = 0; i < n; ++i) {
-      const int part = (int)(0.5 * (v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] +
-                                    v[3 * i + 2] * v[3 * i + 2]) /
-                             0.0001);
-      while ((int)ke_hist_.size() <= part) ke_hist_.push_back(0);
-      ke_hist_[part]++;
-    }
-  }
-  if (ap && !msd_start_.empty()) {
-    // mean square displacement per residue (dataExtraction.h:1524-1650)
+  if (m.msd) {
+    std::vector<int> off, beads;
+    msd_groups(sys, off, beads);
     std::ostringstream o;
     o << time;
-    auto sq = [&](int j) {
-      const double dx = ap[3 * j] - msd_start_[3 * j], dy = ap[3 * j + 1] - msd_start_[3 * j + 1],
-                   dz = ap[3 * j + 2] - msd_start_[3 * j + 2];
-      return dx * dx + dy * dy + dz * dz;
-    };
-    for (const Molecule& m : sys.mol) {
-      double msd = 0;
-      int np = 0;
-      if (m.type == MOL_BOND) {
-        for (const auto& b : m.bonds) {
-          msd += sq(b[0]);
-          msd += sq(b[1]);
-        }
-        np += (int)m.bonds.size() * 2;
-      } else if (m.type == MOL_BEND) {
-        for (const auto& b : m.bonds) {
-          msd += sq(b[0]);
-          msd += sq(b[1]);
-          msd += sq(b[2]);
-        }
-        np += (int)m.bonds.size() * 3;
-      } else if (m.type == MOL_CHAIN) {
-        for (const auto& b : m.bonds) {
-          for (int j = b[0]; j < b[0] + b[2] * b[1]; ++j) msd += sq(j);
-          np += b[2] * b[1];
-        }
-      } else if (m.type == MOL_BEAD || m.type == MOL_NANOCORE) {
-        for (const auto& b : m.bonds) msd += sq(b[0]);
-        np += (int)m.bonds.size();
-      }
-      if (np != 0) o << '\t' << (msd / (double)np);
+    for (size_t g = 0; g + 1 < off.size() && g < m.msd_sum.size(); ++g) {
+      const int np = off[g + 1] - off[g];
+      if (np != 0) o << '\t' << (m.msd_sum[g] / (double)np);
     }
     o << '\n';
     append("meanSquareDisplacement_", o.str());

@@ -16,20 +16,55 @@
 
 namespace smd {
 
+// Aggregates of one measurement, from which the .dat lines are written: the
+// host computes them from the state it holds (the oracle), the device from its
+// own arrays (the GPU driver reads back only these).
+struct Measurement {
+  double kinetic = 0;                      // sum v^2/2 (Kinetic::compute)
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // smallest and largest coordinate per axis
+  double lbond = 0;                        // sum of BOND residue bond lengths
+  int n_bond = 0;
+  double cos_bend = 0, l_bend0 = 0, l_bend1 = 0;  // BEND residue sums
+  int n_bend = 0;
+  bool msd = false;                        // diffusion started: write a meanSquareDisplacement_ line
+  std::vector<double> msd_sum;             // per molecule: sum of squared displacements of its entries
+};
+
+// Bead entries whose displacements meanSquareDisplacement_ averages, per
+// molecule in file order (dataExtraction.h:1524-1650): both beads of every
+// BOND, the three of every BEND, every bead of every CHAIN block, each bead
+// of a BEAD or NANOCORE residue; a bead listed twice counts twice.  Other
+// molecule types have no entries (no column).  offsets has nMolecules + 1
+// entries.
+void msd_groups(const MpdSystem& sys, std::vector<int>& offsets, std::vector<int>& beads);
+
 class Observables {
  public:
   explicit Observables(const std::string& name) : name_(name) {}
 
-  // One measurement.  pos/vel: N*3 (current state), abs_pos: unwrapped
-  // positions (may be null: no diffusion tracking), time: current time.
-  // pot: total potential (pair + bonded + BEAD); bead_pot: BEAD part;
-  // n_bead_res: number of BEAD residues.
+  // One measurement from the state.  pos/vel: N*3 (current state), abs_pos:
+  // unwrapped positions (may be null: no diffusion tracking and no
+  // kinetic-energy histogram), time: current time.  pot: total potential
+  // (pair + bonded + BEAD); bead_pot: BEAD part; n_bead_res: number of BEAD
+  // residues.
   void compute(const MpdSystem& sys, double time, const double* pos, const double* vel,
                const double* abs_pos, double pot, double bead_pot, int n_bead_res);
+
+  // The aggregates compute() writes from (and the kinetic-energy histogram
+  // update when abs_pos is given).
+  void aggregate(const MpdSystem& sys, const double* pos, const double* vel, const double* abs_pos,
+                 Measurement& m);
+
+  // Appends the measurement's lines to the .dat files.
+  void write(const MpdSystem& sys, double time, double pot, double bead_pot, int n_bead_res,
+             const Measurement& m);
 
   // dataExtraction::startDiffusion (dataExtraction.h:790-804).
   void start_diffusion(const MpdSystem& sys, const double* abs_pos);
   bool diffusion_started() const { return !msd_start_.empty(); }
+
+  // The per-bead kinetic-energy histogram in bins of 1e-4 (its counts so far).
+  std::vector<long>& ke_histogram() { return ke_hist_; }
 
   // Writes kEnergyDensity_<name>.dat (dataExtraction.h:553-567).
   void finish();
@@ -39,6 +74,7 @@ class Observables {
   std::string name_;
   std::vector<long> ke_hist_;
   std::vector<double> msd_start_;
+  std::vector<int> msd_off_, msd_beads_;
 };
 
 }  // namespace smd

@@ -62,6 +62,17 @@ struct smd_system {
     AdjAcc* acc = nullptr;
     AdjTables* tab = nullptr;
   } adj;
+  // measurement on the device (smd_measure, smd_start_diffusion)
+  struct Meas {
+    MeasureAcc* acc = nullptr;
+    unsigned int* hist = nullptr;  // kinetic-energy bins of the run so far
+    int cap = 0;
+    int* off = nullptr;            // meanSquareDisplacement_ groups
+    int* beads = nullptr;
+    int n_groups = 0, max_group = 0;
+    double* msd = nullptr;
+    bool tracking = false;         // the drifts add to P.disp
+  } meas;
   int cur = 0;
   long long it = 0;         // current loop step
   bool at_measure = false;  // stopped after the second half-kick of step `it`
@@ -320,6 +331,13 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   if (kLoopStep && h->profile) {
     if (int rc = prof_mark(h)) return rc;
   }
+  // diffusion tracking: the drift of a step that ran through
+  if constexpr (kLoopStep && (FL & F_STOP) == 0) {
+    if (h->meas.tracking) {
+      if (h->mixed) SMD_LAUNCH(h, k_track<true><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur));
+      else SMD_LAUNCH(h, k_track<false><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur));
+    }
+  }
   return 0;
 }
 
@@ -341,6 +359,10 @@ int launch_finish(smd_system* h, int mode, int apply_mc, StepEnd se) {
     SMD_LAUNCH(h, k_finish<true><<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur, mode, apply_mc, se));
   else
     SMD_LAUNCH(h, k_finish<false><<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur, mode, apply_mc, se));
+  if (h->meas.tracking) {  // k_finish drifts
+    if (h->mixed) SMD_LAUNCH(h, k_track<true><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur));
+    else SMD_LAUNCH(h, k_track<false><<<h->grid(), kBlock, 0, h->stream>>>(P, h->cur));
+  }
   h->cur ^= 1;
   return 0;
 }
@@ -1528,6 +1550,135 @@ long smd_rebuild_count(smd_system* h) {
   if (cudaMemcpyAsync(&g, h->P.g, sizeof(Global), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) return -1;
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return -1;
   return (long)g.n_rebuilds;
+}
+
+int smd_start_diffusion(smd_system* h) {
+  if (!h) return fail(1, "null handle");
+  auto& M = h->meas;
+  if (!h->P.disp) {
+    double* d = nullptr;
+    if (int rc = h->alloc(&d, 3 * (size_t)h->n)) return rc;
+    h->P.disp = d;
+  }
+  SMD_CUDA(cudaMemsetAsync(h->P.disp, 0, 3 * sizeof(double) * (size_t)h->n, h->stream));
+  if (!M.tracking) {
+    M.tracking = true;
+    drop_graphs(h);  // the captured periods have no tracking kernel
+  }
+  return 0;
+}
+
+int smd_set_msd_groups(smd_system* h, int n_groups, const int* offsets, const int* beads) {
+  if (!h) return fail(1, "null handle");
+  if (n_groups < 0 || (n_groups > 0 && !offsets)) return fail(1, "bad measurement groups");
+  auto& M = h->meas;
+  const int total = n_groups > 0 ? offsets[n_groups] : 0;
+  if (n_groups > 0 && (offsets[0] != 0 || total < 0 || (total > 0 && !beads)))
+    return fail(1, "measurement group offsets must start at 0");
+  int widest = 0;
+  for (int g = 0; g < n_groups; ++g) {
+    if (offsets[g + 1] < offsets[g]) return fail(1, "measurement group offsets must not decrease");
+    widest = std::max(widest, offsets[g + 1] - offsets[g]);
+  }
+  for (int k = 0; k < total; ++k)
+    if (beads[k] < 0 || beads[k] >= h->n) return fail(1, "measurement group bead index out of range");
+  if (n_groups > 0) {
+    int* off = nullptr;
+    int* bd = nullptr;
+    double* out = nullptr;
+    if (int rc = h->alloc(&off, (size_t)n_groups + 1)) return rc;
+    if (int rc = h->alloc(&bd, (size_t)std::max(total, 1))) return rc;
+    if (int rc = h->alloc(&out, (size_t)n_groups)) return rc;
+    SMD_CUDA(cudaMemcpy(off, offsets, sizeof(int) * ((size_t)n_groups + 1), cudaMemcpyHostToDevice));
+    if (total > 0) SMD_CUDA(cudaMemcpy(bd, beads, sizeof(int) * (size_t)total, cudaMemcpyHostToDevice));
+    M.off = off;
+    M.beads = bd;
+    M.msd = out;
+  }
+  M.n_groups = n_groups;
+  M.max_group = widest;
+  return 0;
+}
+
+int smd_measure(smd_system* h, smd_measurement* out, double* msd_sum) {
+  if (!h || !out) return fail(1, "bad arguments");
+  if (h->n_rep != 1) return fail(1, "smd_measure runs on single-system handles");
+  auto& M = h->meas;
+  auto& P = h->P;
+  if (!M.acc) {
+    if (int rc = h->alloc(&M.acc, 1)) return rc;
+    M.cap = 1 << 20;  // kinetic energies below 104.8576 per bead
+    if (int rc = h->alloc(&M.hist, (size_t)M.cap)) return rc;
+  }
+  MeasureAcc a{};
+  for (int d = 0; d < 3; ++d) {
+    a.lo[d] = ~0ull;
+    a.hi[d] = 0ull;
+  }
+  a.max_bin = -1;
+  SMD_CUDA(cudaMemcpyAsync(M.acc, &a, sizeof a, cudaMemcpyHostToDevice, h->stream));
+  SMD_LAUNCH(h, k_measure<<<h->grid(), kBlock, 0, h->stream>>>(P, M.acc, M.hist, M.cap));
+  const bool msd = M.tracking && M.n_groups > 0 && msd_sum;
+  if (msd) {
+    SMD_CUDA(cudaMemsetAsync(M.msd, 0, sizeof(double) * (size_t)M.n_groups, h->stream));
+    const dim3 grid((unsigned)std::max(1, (M.max_group + kMsdChunk - 1) / kMsdChunk), (unsigned)M.n_groups);
+    SMD_LAUNCH(h, k_msd<<<grid, kBlock, 0, h->stream>>>(P, M.off, M.beads, M.msd));
+  }
+  SMD_CUDA(cudaMemcpyAsync(&a, M.acc, sizeof a, cudaMemcpyDeviceToHost, h->stream));
+  if (msd)
+    SMD_CUDA(cudaMemcpyAsync(msd_sum, M.msd, sizeof(double) * (size_t)M.n_groups, cudaMemcpyDeviceToHost,
+                             h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if (a.max_bin >= M.cap) {  // grow the histogram and add the bins that did not fit
+    constexpr int kMaxBins = 1 << 26;
+    if (a.max_bin >= kMaxBins)
+      return fail(10, "a bead's kinetic energy exceeds the measurement histogram (" +
+                          std::to_string(kMaxBins / 10000) + " per bead): the run has blown up");
+    int cap = M.cap;
+    while (cap <= a.max_bin) cap *= 2;
+    unsigned int* nh = nullptr;
+    if (int rc = h->alloc(&nh, (size_t)cap)) return rc;
+    SMD_CUDA(cudaMemcpyAsync(nh, M.hist, sizeof(unsigned int) * (size_t)M.cap, cudaMemcpyDeviceToDevice, h->stream));
+    SMD_LAUNCH(h, k_measure_bins<<<h->grid(), kBlock, 0, h->stream>>>(P, nh, M.cap, cap));
+    SMD_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto& q : h->allocs)
+      if (q == (void*)M.hist) {
+        cudaFree(q);
+        q = nullptr;
+      }
+    M.hist = nh;
+    M.cap = cap;
+  }
+  out->kinetic = a.kinetic;
+  for (int d = 0; d < 3; ++d) {
+    std::memcpy(&out->lo[d], &a.lo[d], sizeof(double));
+    std::memcpy(&out->hi[d], &a.hi[d], sizeof(double));
+  }
+  out->bond_length_sum = a.lbond;
+  out->n_bond = a.n_bond;
+  out->bend_cos_sum = a.cos_bend;
+  out->bend_len0_sum = a.l_bend0;
+  out->bend_len1_sum = a.l_bend1;
+  out->n_bend = a.n_bend;
+  out->msd = msd ? 1 : 0;
+  return 0;
+}
+
+int smd_ke_histogram(smd_system* h, long* counts, size_t cap, size_t* n_bins) {
+  if (!h || !n_bins) return fail(1, "bad arguments");
+  auto& M = h->meas;
+  *n_bins = 0;
+  if (!M.hist) return 0;
+  std::vector<unsigned int> hc((size_t)M.cap);
+  SMD_CUDA(cudaMemcpyAsync(hc.data(), M.hist, sizeof(unsigned int) * hc.size(), cudaMemcpyDeviceToHost,
+                           h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  size_t nb = hc.size();
+  while (nb > 0 && hc[nb - 1] == 0) --nb;
+  *n_bins = nb;
+  if (counts)
+    for (size_t k = 0; k < std::min(cap, nb); ++k) counts[k] = (long)hc[k];
+  return 0;
 }
 
 }  // extern "C"

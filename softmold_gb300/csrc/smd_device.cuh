@@ -171,6 +171,18 @@ struct Tables {  // force/potential tables (float and double) in constant-like m
   double fieldD[kMaxFieldSets][kFieldConst];  // external-field term constants (FP64)
 };
 
+// Reductions of one measure step (single-system handles): positions enter as
+// the bit patterns of non-negative doubles, which order as unsigned integers.
+struct MeasureAcc {
+  double kinetic;
+  unsigned long long lo[3], hi[3];
+  double lbond;
+  double cos_bend, l_bend0, l_bend1;
+  int n_bond, n_bend;
+  int max_bin;  // largest kinetic-energy bin beyond the histogram's capacity (-1: none)
+  int pad;
+};
+
 // All device pointers of one handle.
 struct DevPtrs {
   int n, npad, n_rep, kmax, n_cells_total;
@@ -200,6 +212,7 @@ struct DevPtrs {
   double* ext_noise; // n*3 noise in sorted order (test hook)
   double* force_out; // n*3 scratch for host reads (file order)
   int* key_out;
+  double* disp;      // n*3 displacement since diffusion tracking started (file order; null: not tracking)
   // BOND / BEND residue terms of each bead, file order: entries
   // terms[term_off[o] .. term_off[o+1]) of bead o; an entry is {kind | role<<1
   // | set<<3, first, second, third} (kind 0 bond, 1 bend; role = the bead's

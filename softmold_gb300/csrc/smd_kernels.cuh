@@ -2485,4 +2485,143 @@ __global__ void __launch_bounds__(kBlock) k_pairs(DevPtrs P, int* out, long long
   }
 }
 
+// ------------------------------------------------------------ measurement
+// Displacement since diffusion tracking started, file order: the reference's
+// absolute positions aP advance by v dt in every first() for beads of nonzero
+// type (include/algorithms/verlet.h:317-326) and box moves do not rescale
+// them (MD.cpp:555), so aP - aPStart (dataExtraction.h:790-800, 1524-1650) is
+// the sum of the drifts since the start.  Runs after every drift while
+// tracking: v is the half-step velocity the drift used.
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_track(DevPtrs P, int cur) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= P.n) return;
+  int ti;
+  if constexpr (MIXED) ti = P.m4[cur][i].w & 0xff; else ti = __double_as_longlong(P.d4[cur][i].w) & 0xff;
+  if (ti == 0) return;
+  const double dt = P.rp[rep_of(P, i)].dt;
+  double* d = P.disp + 3 * (size_t)P.orig[i];
+  d[0] = __dadd_rn(d[0], __dmul_rn(P.vx[i], dt));
+  d[1] = __dadd_rn(d[1], __dmul_rn(P.vy[i], dt));
+  d[2] = __dadd_rn(d[2], __dmul_rn(P.vz[i], dt));
+}
+
+__device__ __forceinline__ double measure_wrap(double d, double L) {
+  if (d >= L / 2.0) d -= L;
+  if (d <= -L / 2.0) d += L;
+  return d;
+}
+__device__ __forceinline__ double dot_rn(const double a[3], const double b[3]) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
+}
+
+// One measure step's reductions on the stopped state (positions of the step,
+// velocities after its second half-kick), with the reference's expressions
+// rounded alike (no contraction into FMA): sum v^2/2 (Kinetic::compute,
+// include/algorithms/dataCollection.h:666-674), the smallest and largest
+// coordinate per axis (dataExtraction.h:1456-1488), BOND lengths and BEND
+// angles of the BOND / BEND residues (dataExtraction.h:860-940), and each
+// bead's kinetic-energy bin int(0.5 v^2 / 1e-4) into the run's histogram
+// (dataExtraction.h:1509-1519).  Single-system handles.
+__global__ void __launch_bounds__(kBlock) k_measure(DevPtrs P, MeasureAcc* acc, unsigned int* hist, int cap) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  double ke = 0.0, lb = 0.0, cb = 0.0, l0 = 0.0, l1 = 0.0;
+  int nb = 0, ne = 0;
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+  if (i < P.n) {
+    const double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+    const double v2 = dot_rn(v, v);
+    ke = __ddiv_rn(v2, 2.0);
+    const int bin = (int)__ddiv_rn(__dmul_rn(0.5, v2), 0.0001);
+    if (bin >= 0 && bin < cap) atomicAdd(hist + bin, 1u);
+    else atomicMax(&acc->max_bin, bin < 0 ? 0x7fffffff : bin);
+    const double x[3] = {P.x[i], P.y[i], P.z[i]};
+    for (int d = 0; d < 3; ++d) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(x[d] + 0.0);  // -0 -> +0
+      lo[d] = b;
+      hi[d] = b;
+    }
+    const RepState& rs = P.rs[0];
+    const int o = P.orig[i];
+    if (P.n_terms > 0) {
+      for (int k = P.term_off[o]; k < P.term_off[o + 1]; ++k) {
+        const int4 t = P.terms[k];
+        if (term_role(t.x) != 0) continue;
+        const int kind = term_kind(t.x);
+        if (kind != kTermBond && kind != kTermBend) continue;
+        const int a = P.inv[t.y], b = P.inv[t.z];
+        const double pa[3] = {P.x[a], P.y[a], P.z[a]}, pb[3] = {P.x[b], P.y[b], P.z[b]};
+        double da[3];
+        for (int d = 0; d < 3; ++d) da[d] = measure_wrap(pa[d] - pb[d], rs.box[d]);
+        if (kind == kTermBond) {
+          lb += sqrt(dot_rn(da, da));
+          ++nb;
+        } else {
+          const int c = P.inv[t.w];
+          const double pc[3] = {P.x[c], P.y[c], P.z[c]};
+          double db[3];
+          for (int d = 0; d < 3; ++d) db[d] = measure_wrap(pb[d] - pc[d], rs.box[d]);
+          const double ra = sqrt(dot_rn(da, da)), rb = sqrt(dot_rn(db, db));
+          l0 += ra;
+          l1 += rb;
+          cb += __ddiv_rn(dot_rn(da, db), __dmul_rn(ra, rb));
+          ++ne;
+        }
+      }
+    }
+  }
+  // block reductions, then one atomic per block and quantity
+  __shared__ double sh[kBlock / 32];
+  block_sum_atomic(ke, &acc->kinetic, sh);
+  if (P.n_terms > 0) {
+    block_sum_atomic(lb, &acc->lbond, sh);
+    block_sum_atomic(cb, &acc->cos_bend, sh);
+    block_sum_atomic(l0, &acc->l_bend0, sh);
+    block_sum_atomic(l1, &acc->l_bend1, sh);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nb += __shfl_xor_sync(0xffffffffu, nb, o);
+    ne += __shfl_xor_sync(0xffffffffu, ne, o);
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+      hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (nb) atomicAdd(&acc->n_bond, nb);
+    if (ne) atomicAdd(&acc->n_bend, ne);
+    for (int d = 0; d < 3; ++d) {
+      atomicMin(&acc->lo[d], lo[d]);
+      atomicMax(&acc->hi[d], hi[d]);
+    }
+  }
+}
+
+// Kinetic-energy bins of a measure step that fell beyond the histogram's
+// previous capacity [from, cap), after the histogram has grown.
+__global__ void __launch_bounds__(kBlock) k_measure_bins(DevPtrs P, unsigned int* hist, int from, int cap) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= P.n) return;
+  const double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+  const int bin = (int)__ddiv_rn(__dmul_rn(0.5, dot_rn(v, v)), 0.0001);
+  if (bin >= from && bin < cap) atomicAdd(hist + bin, 1u);
+}
+
+// Sum of squared displacements of each measurement group (blockIdx.y): the
+// entries [off[g], off[g+1]) of file-order beads, kMsdChunk per block.
+constexpr int kMsdChunk = 4096;
+__global__ void __launch_bounds__(kBlock) k_msd(DevPtrs P, const int* off, const int* beads, double* out) {
+  const int g = blockIdx.y;
+  const int a = off[g] + blockIdx.x * kMsdChunk, e = min(off[g + 1], a + kMsdChunk);
+  double s = 0.0;
+  for (int k = a + (int)threadIdx.x; k < e; k += kBlock) {
+    const double* d = P.disp + 3 * (size_t)beads[k];
+    const double dd[3] = {d[0], d[1], d[2]};
+    s += dot_rn(dd, dd);
+  }
+  __shared__ double sh[kBlock / 32];
+  block_sum_atomic(s, out + g, sh);
+}
+
 }  // namespace smd

@@ -33,6 +33,12 @@ Fixtures
   restart_core/    stores at t = 0.48, extended to 0.96, and the sha256 of
                    every file the reference's continuation writes
                    (`--only-restart`; made after traj_bil and core200).
+  msd_bil/         the traj_bil bilayer entered as a checkpoint at t = 99.84
+                   and run to 100.8 (stores every 0.48, measurements every
+                   0.16): the reference starts diffusion tracking at its first
+                   measurement after 100 tau (MD.cpp:64, 538-539) and writes
+                   meanSquareDisplacement_bil.dat; sha256 of every file and the
+                   small ones verbatim (`--only-msd`).
   generators.json  sha256 of the reference generators' .mpd for a few seeds.
 Inputs are seeded synthetic membranes built in the reference generators' terms
 (softmold_gb300 synth_*, byte-identical to generate/liposome and bilayer).
@@ -334,6 +340,32 @@ def to_nanocore(path, sep):
     open(path, "w").write("\n".join(out))
 
 
+def make_msd(tmp):
+    """msd_bil/: a reference run that crosses 100 tau, so that it tracks
+    diffusion: the 200-lipid bilayer of traj_bil as a checkpoint at
+    initialTime 99.84, to finalTime 100.8."""
+    mdir = os.path.join(HERE, "msd_bil")
+    shutil.rmtree(mdir, ignore_errors=True)
+    os.makedirs(os.path.join(mdir, "out"))
+    path = os.path.join(mdir, "bil.mpd")
+    smd.synth_bilayer(path, 5, 200, 3.45, 16.0, 0.01, 0.0)
+    set_run(path, 100.8, 0.48, 0.16)
+    t = open(path).read()
+    t = re.sub(r"initialTime \S+", "initialTime 99.84", t)
+    open(path, "w").write(t)
+    run_dir = os.path.join(tmp, "msd")
+    os.makedirs(run_dir)
+    shutil.copy(path, run_dir)
+    run_ref_md(run_dir, "bil")
+    digests = {}
+    for f in sorted(glob.glob(os.path.join(run_dir, "*"))):
+        data = open(f, "rb").read()
+        digests[os.path.basename(f)] = hashlib.sha256(data).hexdigest()
+        if len(data) < 100_000:  # large histograms are kept as digests only
+            shutil.copy(f, os.path.join(mdir, "out"))
+    json.dump(digests, open(os.path.join(mdir, "digests.json"), "w"), indent=1)
+
+
 def run_ref_md(workdir, name):
     env = dict(os.environ, OMP_NUM_THREADS="1")
     subprocess.run([os.path.join(REF, "MD"), name], cwd=workdir, env=env, check=True,
@@ -419,6 +451,13 @@ def main():
     if not os.path.exists(os.path.join(REF, "ref_dump")):
         sys.exit("oracle/_ref is missing: run oracle/build_ref.sh first")
     tmp = tempfile.mkdtemp(prefix="smd_golden_")
+    if "--only-msd" in sys.argv:  # the diffusion-tracking fixture alone
+        try:
+            make_msd(tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        print("msd fixture written to", HERE)
+        return
     if "--only-restart" in sys.argv:  # the checkpoint-continuation fixtures alone
         try:
             make_restart(tmp)

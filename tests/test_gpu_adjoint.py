@@ -268,3 +268,47 @@ def test_adjoint_rejects_barostat(built, tmp_path):
     s = smd.System(smd.read_mpd(p), precision=smd.MIXED)
     with pytest.raises(smd.SmdError, match="barostat"):
         s.adjoint(10, 5)
+
+
+@pytest.fixture(scope="module")
+def bilayer10k(tmp_path_factory):
+    """The benchmarked adjoint workload: the 10,000-lipid flat bilayer of the
+    bench (29,400 beads, the generator's square lattice per leaflet), barostat
+    off, after 200 mixed steps from the lattice."""
+    p = str(tmp_path_factory.mktemp("adj10k") / "b.mpd")
+    smd.synth_bilayer(p, 1000, 10000, 3.45, 15.0, 0.0, 0.0)
+    m = smd.read_mpd(p)
+    s = smd.System(m, precision=smd.MIXED)
+    s.prepare()
+    s.advance(200)
+    start = s.state()
+    s.close()
+    return m, start, 200
+
+
+@pytest.fixture(scope="module")
+def fd_fp64_10k(bilayer10k):
+    """Central differences of the FP64 forward run of the 29,400-bead bilayer
+    over 20 steps at a 1e-3 relative step, Richardson-extrapolated with the
+    half step."""
+    m, start, it0 = bilayer10k
+    f1 = fd_gradient(m, start, it0, 20, smd.PLAIN_FP64, 1e-3)
+    f2 = fd_gradient(m, start, it0, 20, smd.PLAIN_FP64, 5e-4)
+    return (4.0 * f2 - f1) / 3.0
+
+
+@pytest.mark.parametrize("precision", PREC)
+def test_adjoint_of_the_benchmarked_workload(built, bilayer10k, fd_fp64_10k, precision):
+    """The adjoint at the size the bench times it: 20 steps in 4 recomputed
+    segments on 29,400 beads, both forms, against the FP64 differences at the
+    1e-3 relative step, and the mixed gradient against the FP64 adjoint."""
+    m, start, it0 = bilayer10k
+    res = adjoint_at(m, start, it0, precision, 20, 5)
+    j0 = mean_potential(m, start, it0, 20, precision)
+    assert abs(res["mean_potential"] - j0) <= (1e-7 if precision == smd.PLAIN_FP64 else 1e-6) * abs(j0)
+    rel = np.abs(res["grad"] - fd_fp64_10k) / np.abs(fd_fp64_10k)
+    print(f"29,400 beads, precision {precision}: adjoint {res['grad']}, FD {fd_fp64_10k}, rel err {rel}")
+    assert (rel < FD_1E3_TOL).all()
+    if precision == smd.MIXED:
+        ref = adjoint_at(m, start, it0, smd.PLAIN_FP64, 20, 5)["grad"]
+        assert (np.abs(res["grad"] - ref) / np.abs(ref) < 1e-3).all()

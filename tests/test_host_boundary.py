@@ -165,3 +165,32 @@ def test_md_executable_refuses_bad_input_files(built, tmp_path, case, message):
     assert r.returncode != 0
     assert message in r.stdout + r.stderr
     assert sorted(os.listdir(tmp_path)) == ([] if case == "missing" else ["bil.mpd"])
+
+
+def test_reader_is_the_md_executables():
+    """read_mpd goes through the library's reader and residue expansion
+    (smd_mpd_load), the code path of the `MD` executable: residues expand
+    into the device step's terms, run settings come with them, and files the
+    device step cannot run are refused with the executable's message."""
+    import softmold_gb300 as smd
+    from conftest import GOLDEN
+    net = smd.read_mpd(os.path.join(GOLDEN, "net200", "net.mpd"))
+    assert len(net.type) == 600 and net.chain_blocks.shape == (1, 3) and net.bonds.shape[1] == 2
+    assert net.bends is not None and net.fields is None and net.sphere_index is None
+    fld = smd.read_mpd(os.path.join(GOLDEN, "field200", "fld.mpd"))
+    assert set(np.unique(fld.fields[:, 0])) <= {11, 15, 16, 17, 19} and fld.field_consts.shape[1] == 8
+    core = smd.read_mpd(os.path.join(GOLDEN, "core200", "core.mpd"))
+    assert list(core.core_index) == [600, 601] and core.core_consts.shape == (2, 22) and core.sphere_index is None
+    msd = smd.read_mpd(os.path.join(GOLDEN, "msd_bil", "bil.mpd"))
+    assert msd.initial_time == 99.84 and msd.final_time == 100.8
+
+
+def test_reader_refusals(tmp_path):
+    import softmold_gb300 as smd
+    from conftest import GOLDEN
+    with pytest.raises(smd.SmdError):
+        smd.read_mpd(str(tmp_path / "missing.mpd"))
+    txt = open(os.path.join(GOLDEN, "traj_bil", "bil.mpd")).read()
+    (tmp_path / "cut.mpd").write_text(txt[:len(txt) // 2])
+    with pytest.raises(smd.SmdError):
+        smd.read_mpd(str(tmp_path / "cut.mpd"))

@@ -22,11 +22,13 @@ CORE = os.path.join(GOLDEN, "core200")
 MIX = os.path.join(GOLDEN, "mix200")
 RESTART_BIL = os.path.join(GOLDEN, "restart_bil")
 RESTART_CORE = os.path.join(GOLDEN, "restart_core")
+MSD = os.path.join(GOLDEN, "msd_bil")
 
 
 @pytest.mark.skipif(platform.machine() != "x86_64", reason="digests are of x86-64 glibc number formatting")
 @pytest.mark.parametrize("where,name", [(TRAJ, "bil"), (NET, "net"), (FIELD, "fld"), (CORE, "core"),
-                                        (MIX, "mix"), (RESTART_BIL, "bil"), (RESTART_CORE, "core")])
+                                        (MIX, "mix"), (RESTART_BIL, "bil"), (RESTART_CORE, "core"),
+                                        (MSD, "bil")])
 def test_md_oracle_matches_reference_outputs(oracle, tmp_path, where, name):
     """traj_bil: CHAIN lipids, barostat on; net200: the same with BOND and
     BEND residues over the heads; field200: with one residue of each
@@ -34,7 +36,9 @@ def test_md_oracle_matches_reference_outputs(oracle, tmp_path, where, name):
     BALL); core200: a vesicle with a two-core NANOCORE residue; mix200: a
     two-lipid bilayer (HEAD2/TAIL2, 8-type tables) under a temperature ramp;
     restart_bil / restart_core: continuations from the checkpoints the
-    reference stores at t = 0.48 (initialTime != 0, MD.cpp:274-308)."""
+    reference stores at t = 0.48 (initialTime != 0, MD.cpp:274-308);
+    msd_bil: a run from t = 99.84 across 100 tau, where the reference starts
+    tracking diffusion and writes meanSquareDisplacement_bil.dat."""
     from oracle_binding import MD
     shutil.copy(os.path.join(where, name + ".mpd"), tmp_path)
     env = dict(os.environ, OMP_NUM_THREADS="1")
