@@ -8,6 +8,11 @@
 #   _ref/ref_dump    oracle/ref_dump.cpp linked against the reference headers
 #   _ref/liposome    generate/liposome.cpp
 #   _ref/bilayer     generate/bilayer.cpp
+#   _ref/MDcuda      the reference's own FP32 CUDA driver MDcuda.cu, unmodified,
+#                    for sm_103a (C++17: CUDA 13's thrust requires it), when nvcc
+#                    is present.  It is built as a check that the reference GPU
+#                    port compiles for GB300; the binary is for this host's
+#                    architecture and cannot run where no reference sources are.
 # Usage: oracle/build_ref.sh reference_root   (or $SMD_REFERENCE_ROOT)
 set -euo pipefail
 REF="${1:-${SMD_REFERENCE_ROOT:-}}"
@@ -24,5 +29,9 @@ $CXX $FLAGS -fopenmp "$REF/MD.cpp" -o "$OUT/MD" &
 $CXX $FLAGS -fopenmp -I"$REF" "$HERE/ref_dump.cpp" -o "$OUT/ref_dump" &
 $CXX $FLAGS -I"$REF/generate" "$REF/generate/liposome.cpp" -o "$OUT/liposome" &
 $CXX $FLAGS -I"$REF/generate" "$REF/generate/bilayer.cpp" -o "$OUT/bilayer" &
+NVCC="$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)"
+if [ -x "$NVCC" ] && [ -f "$REF/MDcuda.cu" ]; then
+  (cd "$OUT" && "$NVCC" -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 "$REF/MDcuda.cu" -o "$OUT/MDcuda") &
+fi
 wait
 echo "built reference tools into $OUT"
