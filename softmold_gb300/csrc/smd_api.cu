@@ -292,6 +292,9 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
     if (int rc = prof_mark(h)) return rc;
   }
   const int gl = h->grid_lanes();
+  if constexpr ((FL & F_DU) != 0) {  // the reference-grid cells the size-change pass asks about
+    SMD_LAUNCH(h, k_ref_cells<<<h->grid(), kBlock, 0, h->stream>>>(P));
+  }
   if (h->mixed) {
     if constexpr (FL == 0 || FL == (F_STOP | F_DU)) {  // the loop's pair passes follow the tuner
       switch (h->tune.lanes) {
@@ -811,7 +814,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     if ((rc = h->alloc(&P.d4[0], total)) || (rc = h->alloc(&P.d4[1], total)) || (rc = h->alloc(&P.dt4, total)))
       return rc;
   }
-  if ((rc = h->alloc(&P.ref, total))) return rc;
+  if ((rc = h->alloc(&P.ref, total)) || (rc = h->alloc(&P.refcell, total))) return rc;
   int** ints[] = {&P.orig, &P.inv, &P.cinfo, &P.torig, &P.tcinfo, &P.key, &P.slot, &P.tkey, &P.nnbr, &P.key_out};
   for (int** q : ints)
     if ((rc = h->alloc(q, total))) return rc;

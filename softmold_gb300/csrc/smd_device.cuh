@@ -212,6 +212,8 @@ struct DevPtrs {
   double* ext_noise; // n*3 noise in sorted order (test hook)
   double* force_out; // n*3 scratch for host reads (file order)
   int* key_out;
+  unsigned long long* refcell;  // reference-grid cell of each bead (sorted order, x | y << 21 | z << 42),
+                                // set before each size-change pass
   double* disp;      // n*3 displacement since diffusion tracking started (file order; null: not tracking)
   // BOND / BEND residue terms of each bead, file order: entries
   // terms[term_off[o] .. term_off[o+1]) of bead o; an entry is {kind | role<<1
@@ -388,16 +390,6 @@ __device__ __forceinline__ R pair_mag(const R* c, R r) {
   R m = c[ci] - r;
   return ((c[ci + 1] - c[ci + 2] * m) * m) / r;
 }
-// The same force magnitude from r^2 without divisions: r and 1/r from one
-// reciprocal square root, and the table row chosen by r >= rm, which equals
-// int(r/rm) >= 1 for the positive values involved.
-__device__ __forceinline__ float pair_mag_rsqrt(const float* c, float r2) {
-  const float rinv = rsqrtf(r2), r = r2 * rinv;
-  const int ci = (r >= c[0]) ? 3 : 0;
-  const float m = c[ci] - r;
-  return ((c[ci + 1] - c[ci + 2] * m) * m) * rinv;
-}
-
 // Pair potential (include/MD.h:913-926).
 template <typename R>
 __device__ __forceinline__ R pair_pot(const R* c, R r) {
@@ -409,23 +401,34 @@ __device__ __forceinline__ R pair_pot(const R* c, R r) {
   return m * m * (c[4] - m * c[5]);
 }
 // U(r) - U(r') with r' = r + dr, written so that a small dr does not cancel:
-// each branch's polynomial difference is factored through dr.  rc2 bounds the
-// interaction range of both arguments.
+// each branch's polynomial difference is factored through dr.  rc bounds the
+// interaction range of both arguments.  Every operation is rounded
+// explicitly (no contraction left to the compiler), so a pair's term has the
+// same bits wherever it is evaluated.
+__device__ __forceinline__ float pot_f(const float* c, float r) {
+  if (r <= c[0]) {
+    const float m = __fsub_rn(c[0], r);
+    return __fmaf_rn(__fmul_rn(c[1], m), m, c[2]);
+  }
+  const float m = __fsub_rn(c[3], r);
+  return __fmul_rn(__fmul_rn(m, m), __fmaf_rn(-m, c[5], c[4]));
+}
 __device__ __forceinline__ float pair_dpot_f(const float* c, float r, float rn, float dr, float rc) {
   const bool in0 = r < rc, in1 = rn < rc;
   if (!in0 && !in1) return 0.f;
   if (in0 && in1 && ((r <= c[0]) == (rn <= c[0]))) {
     if (r <= c[0]) {
       // C1[(rm-r)^2-(rm-r')^2] = C1 dr (2 rm - r - r')
-      return c[1] * dr * (2.f * c[0] - r - rn);
+      return __fmul_rn(__fmul_rn(c[1], dr), __fsub_rn(__fsub_rn(__fmul_rn(2.f, c[0]), r), rn));
     }
-    const float m = c[3] - r, mn = c[3] - rn;  // mn = m - dr
+    const float m = __fsub_rn(c[3], r), mn = __fsub_rn(c[3], rn);  // mn = m - dr
     // m^2(C4 - C5 m) - mn^2(C4 - C5 mn) = dr[C4 (m+mn) - C5 (m^2 + m mn + mn^2)]
-    return dr * (c[4] * (m + mn) - c[5] * (m * m + m * mn + mn * mn));
+    const float sq = __fmaf_rn(mn, mn, __fmaf_rn(m, mn, __fmul_rn(m, m)));
+    return __fmul_rn(dr, __fmaf_rn(-c[5], sq, __fmul_rn(c[4], __fadd_rn(m, mn))));
   }
-  const float u0 = in0 ? pair_pot<float>(c, r) : 0.f;
-  const float u1 = in1 ? pair_pot<float>(c, rn) : 0.f;
-  return u0 - u1;
+  const float u0 = in0 ? pot_f(c, r) : 0.f;
+  const float u1 = in1 ? pot_f(c, rn) : 0.f;
+  return __fsub_rn(u0, u1);
 }
 
 // ------------------------------------------------------------------ BEAD

@@ -67,13 +67,18 @@ __device__ __forceinline__ float displacement(uint4 ref, unsigned int fx, unsign
 
 // ------------------------------------------------------------ list build
 // Verlet-list cell of bead i from its 32-bit fractional coordinates: the
-// cell index along an axis is floor(f * n / 2^32), always in [0, n).
+// cell index along an axis is floor(f * n / 2^32), always in [0, n).  The
+// beads are in the previous build's cell order, so the lanes of a warp mostly
+// share a few cells: the lanes of one cell take their slots from one atomic
+// add of the leader (the lowest lane), in lane order.
 __global__ void __launch_bounds__(kBeadBlock) k_bin(DevPtrs P, int cur, int mixed, int in_graph) {
   pdl_trigger();
   if (!P.g->rebuild) return;
   const int i = blockIdx.x * kBeadBlock + threadIdx.x;
   if (in_graph && i == 0) P.g->graph_builds++;
-  if (i >= P.n) return;
+  const bool active = i < P.n;
+  const unsigned int lanes = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
   const int r = rep_of(P, i);
   const RepState& rs = P.rs[r];
   unsigned int f[3];
@@ -91,7 +96,13 @@ __global__ void __launch_bounds__(kBeadBlock) k_bin(DevPtrs P, int cur, int mixe
   const int cx = __umulhi(f[0], (unsigned)n0), cy = __umulhi(f[1], (unsigned)n1), cz = __umulhi(f[2], (unsigned)n2);
   const int key = P.rp[r].cell_begin + cx + n0 * (cy + n1 * cz);
   P.key[i] = key;
-  P.slot[i] = atomicAdd(&P.cell_count[key], 1);
+  const unsigned int same = __match_any_sync(lanes, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(same) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&P.cell_count[key], __popc(same));
+  base = __shfl_sync(same, base, leader);
+  P.slot[i] = base + __popc(same & ((1u << lane) - 1u));
 }
 
 // Exclusive scan of cell_count into cell_start in three passes: tile sums,
@@ -1567,6 +1578,47 @@ __device__ __forceinline__ Vec3<typename std::conditional<MIXED, float, double>:
 // minimum image.  Writes the per-bead pair force (fixed point or FP64) and,
 // with F_DU / F_ENERGY, the replica's pair U(x)-U(s x) / pair energy.
 constexpr int kGather = 4;  // neighbour gathers in flight per lane (mixed pair pass)
+// Cells of the reference's grid (nCells = int(L/rc) per axis, at least 3)
+// for every bead before a size-change pass: CellOpt::computeDPotential visits
+// only pairs of one cell and its 26 neighbours
+// (include/algorithms/cellOpt.h:1043-1180), so a pair farther than one cell
+// apart that the box rescale would bring within rc adds nothing to the
+// reference's difference.  The cell of each axis is the reference's
+// int(x / cellSize) with the x >= n -> n-1 correction, packed in 21 bits.
+__global__ void __launch_bounds__(kBlock) k_ref_cells(DevPtrs P) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= P.n) return;
+  const RepState& rs = P.rs[rep_of(P, i)];
+  const double rc = P.tab->rc;
+  const double x[3] = {P.x[i], P.y[i], P.z[i]};
+  unsigned long long key = 0;
+  for (int d = 0; d < 3; ++d) {
+    const int n = int(rs.box[d] / rc);
+    key |= (unsigned long long)(cell_coord(x[d], rs.box[d] / n, n) & 0x1fffff) << (21 * d);
+  }
+  P.refcell[i] = key;
+}
+
+// Whether beads a and b (sorted indices) lie in the same or neighbouring
+// cells of the reference's grid (periodic).  The size-change passes ask this
+// only for pairs beyond rc at the current positions (pairs within rc are
+// always neighbours).
+__device__ __forceinline__ bool ref_cells_adjacent(const DevPtrs& P, int a, int b, const int n[3]) {
+  const unsigned long long ka = P.refcell[a], kb = P.refcell[b];
+  bool adj = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int dd = (int)((ka >> (21 * d)) & 0x1fffff) - (int)((kb >> (21 * d)) & 0x1fffff);
+    dd = dd < 0 ? -dd : dd;
+    adj = adj && (dd <= 1 || dd == n[d] - 1);
+  }
+  return adj;
+}
+// The reference grid's cells per axis of a replica.
+__device__ __forceinline__ void ref_grid(const DevPtrs& P, const RepState& rs, int n[3]) {
+  for (int d = 0; d < 3; ++d) n[d] = int(rs.box[d] / P.tab->rc);
+}
+
 // Mixed-form pair sums of bead i over its Verlet list, lane `sub` of its G
 // lanes: each pair force rounded to fixed point and summed in int32 per lane
 // (flushed to int64 every 32 terms), with F_DU the size-change difference
@@ -1606,6 +1658,18 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
     ay += __float2int_rn(dy * mag);
     az += __float2int_rn(dz * mag);
   };
+  // distances and size-change terms rounded explicitly: a pair gives the
+  // same bits in every unrolled copy of the loop and in the second pass below
+  auto dist2 = [](float dx, float dy, float dz) { return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))); };
+  auto dscale = [&](float dx, float dy, float dz) {  // sum (s_d^2 - 1) d_d^2
+    return __fmaf_rn(sq2, __fmul_rn(dz, dz), __fmaf_rn(sq1, __fmul_rn(dy, dy), __fmul_rn(sq0, __fmul_rn(dx, dx))));
+  };
+  auto du_q = [&](float r2, float q, float rn2, int tj) -> long long {
+    const float rr = __fmul_rn(r2, rsqrtf(r2)), rs2 = __fmul_rn(rn2, rsqrtf(rn2));
+    return f2ll_rn(__fmul_rn(pair_dpot_f(rowU + 6 * tj, rr, rs2, __fdividef(q, __fadd_rn(rs2, rr)), T.rcf),
+                             4294967296.0f));
+  };
+  bool entered = false;  // a pair beyond rc that the scale brings within rc
   int k = sub;
   int rounds = 0;
   // kGather independent gathers in flight per lane
@@ -1621,15 +1685,14 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
     for (int u = 0; u < kGather; ++u) {
       const uint4 o = og[u];
       const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
-      const float r2 = dx * dx + dy * dy + dz * dz;
+      const float r2 = dist2(dx, dy, dz);
       if constexpr ((FL & F_DU) != 0) {
         // each pair once, from its lower-index bead (the term is even in d)
-        const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
-        const float rn2 = r2 + q;
+        const float q = dscale(dx, dy, dz);
+        const float rn2 = __fadd_rn(r2, q);
         if (jg[u] > i && (r2 < rc2 || rn2 < rc2)) {
-          const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
-          dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
-                        4294967296.0f);
+          dq += du_q(r2, q, rn2, o.w & 0xff);
+          entered = entered || !(r2 < rc2);
         }
       }
       if constexpr ((FL & F_ENERGY) == 0) {
@@ -1650,14 +1713,13 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
     const int j = __ldg(nb + k);
     const uint4 o = P.m4[cur][j];
     const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
-    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float r2 = dist2(dx, dy, dz);
     if constexpr ((FL & F_DU) != 0) {
-      const float q = sq0 * dx * dx + sq1 * dy * dy + sq2 * dz * dz;
-      const float rn2 = r2 + q;
+      const float q = dscale(dx, dy, dz);
+      const float rn2 = __fadd_rn(r2, q);
       if (j > i && (r2 < rc2 || rn2 < rc2)) {
-        const float rr = r2 * rsqrtf(r2), rn = rn2 * rsqrtf(rn2);
-        dq += f2ll_rn(pair_dpot_f(rowU + 6 * (o.w & 0xff), rr, rn, __fdividef(q, rn + rr), T.rcf) *
-                      4294967296.0f);
+        dq += du_q(r2, q, rn2, o.w & 0xff);
+        entered = entered || !(r2 < rc2);
       }
     }
     if constexpr ((FL & F_ENERGY) == 0) {
@@ -1669,6 +1731,24 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
   qx += ax;
   qy += ay;
   qz += az;
+  if constexpr ((FL & F_DU) != 0) {
+    // Rare second pass: of the pairs that only the scale brings within rc,
+    // the reference counts those in neighbouring cells of its grid
+    // (ref_cells_adjacent); take the others' terms back out, bit for bit.
+    if (entered) {
+      int refn[3];
+      ref_grid(P, rs, refn);
+      for (int k2 = sub; k2 < nn; k2 += G) {
+        const int j = __ldg(nb + k2);
+        const uint4 o = P.m4[cur][j];
+        const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
+        const float r2 = dist2(dx, dy, dz);
+        const float q = dscale(dx, dy, dz);
+        const float rn2 = __fadd_rn(r2, q);
+        if (j > i && !(r2 < rc2) && rn2 < rc2 && !ref_cells_adjacent(P, i, j, refn)) dq -= du_q(r2, q, rn2, o.w & 0xff);
+      }
+    }
+  }
 }
 
 template <bool MIXED, int FL, int G>
@@ -1711,6 +1791,8 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
       const double* rowU = sU + 6 * ti * nT;
       const double rc2 = T.rc2;
       const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
+      int rgrid[3] = {0, 0, 0};
+      if constexpr ((FL & F_DU) != 0) ref_grid(P, rs, rgrid);
       for (int k = sub; k < nn; k += G) {
         const int j = __ldg(nb + k);
         const double4 o = P.d4[cur][j];
@@ -1741,7 +1823,8 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
           const double nx = dx * rs.scale[0], ny = dy * rs.scale[1], nz = dz * rs.scale[2];
           const double rn2 = nx * nx + ny * ny + nz * nz;
           const double u0 = r2 < rc2 ? pair_pot<double>(rowU + 6 * tj, sqrt(r2)) : 0.0;
-          const double u1 = rn2 < rc2 ? pair_pot<double>(rowU + 6 * tj, sqrt(rn2)) : 0.0;
+          const double u1 = (rn2 < rc2 && (r2 < rc2 || ref_cells_adjacent(P, i, j, rgrid)))
+                                ? pair_pot<double>(rowU + 6 * tj, sqrt(rn2)) : 0.0;
           dU += 0.5 * (u0 - u1);
         }
       }
