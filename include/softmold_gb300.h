@@ -46,7 +46,9 @@ typedef struct smd_system_desc {
   int n_chain_blocks;           /* CHAIN residue blocks */
   const int* chain_blocks;      /* n_chain_blocks*3: start, nChains, length */
   const double* chain_consts;   /* n_chain_blocks*4: l0, kbond, abend, kbend */
-  int n_spheres;                /* beads of one BEAD residue (0 = none) */
+  int n_spheres;                /* beads of one BEAD residue (0 = none, at most 256); up to 20 a
+                                   sphere's force leaves out the other spheres, above 20 it takes
+                                   them (Blob::doBeadForce's two branches, system.h:2104-2210) */
   const int* sphere_index;      /* n_spheres bead indices */
   const double* sphere_consts;  /* 22*n_types^2 BEAD constants */
   double dt;                    /* deltaT */

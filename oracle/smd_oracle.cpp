@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -763,6 +764,56 @@ double orc_bend_dpotential(const double* pos, const double box[3], int nb, const
   return bend_energy(pos, box, nb, list, c, scale);
 }
 
+}  // extern "C"
+
+namespace {
+
+// The hash-cell search of the many-sphere branches (Blob::doBeadForce above
+// 20 beads, include/system.h:2104-2163; doNanoCoreForce from 50 cores,
+// :2264-2318), with the cell helpers of analysis/cellInclude/cell.h:
+// int(L / (2 r)) cells per axis of side L / n (getCell floors p / side),
+// each cell's beads in reverse index order (createIMap pushes to the front of
+// a list), and the 27 neighbours of the sphere's cell with periodic wrap,
+// x offset outermost (neighIndices).  With fewer than three cells along an
+// axis a neighbour repeats, and its beads are visited again, as in the
+// reference.
+struct HashCells {
+  int n[3];
+  double side[3];
+  std::unordered_map<int, std::vector<int>> members;  // in index order; visited back to front
+
+  HashCells(int np, const double* pos, const double box[3], double range) {
+    for (int a = 0; a < 3; ++a) {
+      n[a] = int(box[a] / (range * 2.0));
+      side[a] = box[a] / n[a];
+    }
+    for (int i = 0; i < np; ++i) members[hash_of(pos + 3 * i)].push_back(i);
+  }
+  int hash_of(const double* p) const {
+    const int c[3] = {int(std::floor(p[0] / side[0])), int(std::floor(p[1] / side[1])),
+                      int(std::floor(p[2] / side[2]))};
+    return c[0] + c[1] * n[0] + c[2] * n[0] * n[1];
+  }
+  template <class F>
+  void visit(const double* p, F&& f) const {
+    const int h = hash_of(p);
+    const int cx = h % n[0], cy = (h / n[0]) % n[1], cz = (h / (n[0] * n[1])) % n[2];
+    for (int i = -1; i < 2; ++i)
+      for (int j = -1; j < 2; ++j)
+        for (int k = -1; k < 2; ++k) {
+          const int key = (cx + i + n[0]) % n[0] + ((cy + j + n[1]) % n[1]) * n[0] +
+                          ((cz + k + n[2]) % n[2]) * n[0] * n[1];
+          const auto it = members.find(key);
+          if (it == members.end()) continue;
+          for (auto b = it->second.rbegin(); b != it->second.rend(); ++b) f(*b);
+        }
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
 void orc_bead_force(int n, const double* pos, const int* type, const double box[3], int nT, int nb,
                     const int* idx, const double* C, double* acc) {
   // bead-bead pairs (include/system.h:2072-2098); with a single residue the
@@ -783,6 +834,30 @@ void orc_bead_force(int n, const double* pos, const int* type, const double box[
   }
   const double cutR = C[0];
   const double cut2R = cutR * cutR;
+  if (nb > 20) {
+    // hash-cell branch: every other bead, the other spheres included
+    const HashCells cells(n, pos, box, cutR);
+    for (int j = 0; j < nb; ++j) {
+      const int f = idx[j];
+      double ax = 0, ay = 0, az = 0;
+      cells.visit(pos + 3 * f, [&](int k) {
+        if (k == f) return;
+        const V3 d = diff(pos, f, k, box);
+        V3 ab{0, 0, 0};
+        V3 a2 = accv(acc, k);
+        const int ci = 22 * ((type[f] * nT) + type[k]);
+        bead_force_fn(d, ab, a2, &C[ci], cut2R);
+        setv(acc, k, a2);
+        ax += ab.x;
+        ay += ab.y;
+        az += ab.z;
+      });
+      acc[3 * f] += ax;
+      acc[3 * f + 1] += ay;
+      acc[3 * f + 2] += az;
+    }
+    return;
+  }
   // brute-force branch for <= 20 beads (include/system.h:2165-2210)
   for (int j = 0; j < nb; ++j) {
     const int f = idx[j];
@@ -807,10 +882,16 @@ void orc_bead_force(int n, const double* pos, const int* type, const double box[
   }
 }
 
+// doBeadPotential sums each bead's inner loop under an OpenMP reduction
+// (include/system.h:2967, 2999): a private sum from zero, added to the total
+// at the loop's end; doBeadDPotential's pragmas are commented out, so its
+// terms go straight into the total.
 static double bead_energy(int n, const double* pos, const int* type, const double box[3], int nT,
                           int nb, const int* idx, const double* C, const double* scale) {
   double total = 0;
   for (int j = 0; j < nb; ++j) {
+    double part = 0;
+    double& sum = scale ? total : part;
     for (int k = j + 1; k < nb; ++k) {
       const int f = idx[j], s = idx[k];
       V3 d = diff(pos, f, s, box);
@@ -820,33 +901,37 @@ static double bead_energy(int n, const double* pos, const int* type, const doubl
       const int ci = 22 * ((type[f] * nT) + type[s]);
       const double oldP = beadbead_potential_fn(d, &C[ci], cut2);
       if (!scale) {
-        total += oldP;
+        sum += oldP;
         continue;
       }
       d.x *= scale[0];
       d.y *= scale[1];
       d.z *= scale[2];
-      total += oldP - beadbead_potential_fn(d, &C[ci], cut2);
+      sum += oldP - beadbead_potential_fn(d, &C[ci], cut2);
     }
+    if (!scale) total += part;
   }
   const double cutR = C[0];
   const double cut2R = cutR * cutR;
   for (int j = 0; j < nb; ++j) {
     const int f = idx[j];
+    double part = 0;
+    double& sum = scale ? total : part;
     for (int k = 0; k < n; ++k) {
       if (k == f) continue;
       V3 d = diff(pos, f, k, box);
       const int ci = 22 * ((type[f] * nT) + type[k]);
       const double oldP = bead_potential_fn(d, &C[ci], cut2R);
       if (!scale) {
-        total += oldP;
+        sum += oldP;
         continue;
       }
       d.x *= scale[0];
       d.y *= scale[1];
       d.z *= scale[2];
-      total += oldP - bead_potential_fn(d, &C[ci], cut2R);
+      sum += oldP - bead_potential_fn(d, &C[ci], cut2R);
     }
+    if (!scale) total += part;
   }
   return total;
 }
@@ -1032,6 +1117,34 @@ double orc_ball_potential(const double* pos, const double box[3], int nb, const 
 
 void orc_nanocore_force(int n, const double* pos, const double box[3], int nb, const int* idx, const double* C,
                         double* acc) {
+  if (nb >= 50) {
+    // hash-cell branch: cells from the largest range, truncated to an int
+    int range = 0;
+    for (int j = 0; j < nb; ++j)
+      if (C[22 * j] > range) range = int(C[22 * j]);
+    const HashCells cells(n, pos, box, (double)range);
+    for (int j = 0; j < nb; ++j) {
+      const int f = idx[j];
+      const double* Cj = C + 22 * j;
+      const double cut2 = Cj[0] * Cj[0];
+      double ax = 0, ay = 0, az = 0;
+      cells.visit(pos + 3 * f, [&](int k) {
+        if (k == f) return;
+        const V3 d = diff(pos, f, k, box);
+        V3 ab{0, 0, 0};
+        V3 a2 = accv(acc, k);
+        bead_force_fn(d, ab, a2, Cj, cut2);
+        setv(acc, k, a2);
+        ax += ab.x;
+        ay += ab.y;
+        az += ab.z;
+      });
+      acc[3 * f] += ax;
+      acc[3 * f + 1] += ay;
+      acc[3 * f + 2] += az;
+    }
+    return;
+  }
   for (int j = 0; j < nb; ++j) {
     const int f = idx[j];
     const double* Cj = C + 22 * j;
@@ -1055,6 +1168,8 @@ void orc_nanocore_force(int n, const double* pos, const double box[3], int nb, c
   }
 }
 
+// Each core's loop is an OpenMP reduction (include/system.h:3049): a private
+// sum from zero, added to the total at its end.
 double orc_nanocore_potential(int n, const double* pos, const double box[3], int nb, const int* idx,
                               const double* C) {
   double potential = 0;
@@ -1063,10 +1178,12 @@ double orc_nanocore_potential(int n, const double* pos, const double box[3], int
     const double* Cj = C + 22 * j;
     const double cutoffRad = Cj[0];
     const double cut2 = cutoffRad * cutoffRad;
+    double part = 0;
     for (int k = 0; k < n; ++k) {
       if (k == f) continue;
-      potential += bead_potential_fn(diff(pos, f, k, box), Cj, cut2);
+      part += bead_potential_fn(diff(pos, f, k, box), Cj, cut2);
     }
+    potential += part;
   }
   return potential;
 }

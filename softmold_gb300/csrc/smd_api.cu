@@ -51,6 +51,8 @@ struct smd_system {
   bool mixed = true;
   int n = 0, n_rep = 0, npad = 0, kmax = 0, n_cells = 0, n_tiles = 0;
   int n_sph = 0;  // BEAD sphere beads
+  int sph_threads = 32;  // k_sphere block: the spheres rounded up to whole warps
+  size_t sph_stage = 0;  // k_integ's dynamic shared memory: the spheres' copy
   int n_terms = 0;  // BOND / BEND and external-field term entries
   bool has_fields = false;  // any external-field term entry
   long long n_chains = 0;  // CHAIN molecules (lipids)
@@ -172,18 +174,23 @@ int check_launch(smd_system* h) {
 // results on the device).  Kernel nodes captured this way keep the
 // programmatic edge in the graph.
 template <typename... KArgs, typename... Args>
-cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+cudaError_t launch_pdl_smem(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st,
+                            Args... args) {
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cfg.attrs = at;
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+  return launch_pdl_smem(kern, grid, block, 0, st, args...);
 }
 
 #define SMD_LAUNCH(h, ...)               \
@@ -196,6 +203,15 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t
 #define SMD_PDL(h, ...)                                                                          \
   do {                                                                                           \
     const cudaError_t e_ = launch_pdl(__VA_ARGS__);                                              \
+    if (e_ != cudaSuccess) return fail(200 + (int)e_, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    int rc_ = check_launch(h);                                                                   \
+    if (rc_) return rc_;                                                                         \
+  } while (0)
+
+// k_integ: the spheres' shared-memory copy when the system has any
+#define SMD_PDL_INTEG(h, kern)                                                                   \
+  do {                                                                                           \
+    const cudaError_t e_ = launch_pdl_smem(kern, h->bead_grid(), kBeadBlock, h->sph_stage, h->stream, P, h->cur, se); \
     if (e_ != cudaSuccess) return fail(200 + (int)e_, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
     int rc_ = check_launch(h);                                                                   \
     if (rc_) return rc_;                                                                         \
@@ -312,24 +328,24 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
     }
     if constexpr (kHot) {
       if (!h->has_fields)
-        SMD_PDL(h, k_integ<true, FL>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+        SMD_PDL_INTEG(h, (k_integ<true, FL>));
       else
-        SMD_PDL(h, k_integ<true, FL | F_FIELDS>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+        SMD_PDL_INTEG(h, (k_integ<true, FL | F_FIELDS>));
     } else {
-      SMD_PDL(h, k_integ<true, FL | F_FIELDS>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+      SMD_PDL_INTEG(h, (k_integ<true, FL | F_FIELDS>));
     }
-    if (h->n_sph) SMD_LAUNCH(h, (k_sphere<true, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
+    if (h->n_sph) SMD_LAUNCH(h, (k_sphere<true, FL><<<1, h->sph_threads, 0, h->stream>>>(P, h->cur, se)));
   } else {
     SMD_LAUNCH(h, (k_force<false, FL, kLanes><<<gl, kBlock, 0, h->stream>>>(P, h->cur)));
     if constexpr (kHot) {
       if (!h->has_fields)
-        SMD_PDL(h, k_integ<false, FL>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+        SMD_PDL_INTEG(h, (k_integ<false, FL>));
       else
-        SMD_PDL(h, k_integ<false, FL | F_FIELDS>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+        SMD_PDL_INTEG(h, (k_integ<false, FL | F_FIELDS>));
     } else {
-      SMD_PDL(h, k_integ<false, FL | F_FIELDS>, h->bead_grid(), kBeadBlock, h->stream, P, h->cur, se);
+      SMD_PDL_INTEG(h, (k_integ<false, FL | F_FIELDS>));
     }
-    if (h->n_sph) SMD_LAUNCH(h, (k_sphere<false, FL><<<1, 32, 0, h->stream>>>(P, h->cur, se)));
+    if (h->n_sph) SMD_LAUNCH(h, (k_sphere<false, FL><<<1, h->sph_threads, 0, h->stream>>>(P, h->cur, se)));
   }
   if (kLoopStep && h->profile) {
     if (int rc = prof_mark(h)) return rc;
@@ -489,6 +505,20 @@ int read_error(smd_system* h) {
   return 0;
 }
 
+// Range of the reference's hash cells for a residue above the brute-force
+// size (cells of side >= twice it): a BEAD residue's C[0]; for NANOCORE the
+// largest C[0] of its cores, truncated to an integer as the reference's
+// int accumulator does (include/system.h:2265-2271).
+double sphere_grid_range(const smd_system_desc& d) {
+  if (!d.sphere_nanocore) return d.sphere_consts[0];
+  int r = 0;
+  for (int k = 0; k < d.n_spheres; ++k) {
+    const double c = d.sphere_consts[kBeadConst * k];
+    if (c > r) r = c < 2147483647.0 ? (int)c : 2147483647;
+  }
+  return (double)r;
+}
+
 int validate(const smd_system_desc& d, std::string& why) {
   if (d.n <= 0) return why = "n must be positive", 1;
   if (d.n_types <= 0 || d.n_types > kMaxTypes) return why = "n_types must be in 1..8", 1;
@@ -538,6 +568,13 @@ int validate(const smd_system_desc& d, std::string& why) {
         if (!(d.sphere_consts[kBeadConst * k + kBeadRadiusConst] > 0)) return why = "NANOCORE radius must be positive", 1;
     } else if (!(d.sphere_consts[kBeadRadiusConst] > 0)) {
       return why = "BEAD radius must be positive", 1;
+    }
+    const bool grid = d.sphere_nanocore ? d.n_spheres > kCoreBrute : d.n_spheres > kBeadBrute;
+    if (grid) {
+      // the reference's cell count int(L / 2r) must be at least one per axis
+      const double len = 2.0 * sphere_grid_range(d);
+      if (!(len > 0) || !(d.box[0] >= len && d.box[1] >= len && d.box[2] >= len))
+        return why = "box below one hash cell (twice the sphere range) of the many-sphere branch", 1;
     }
   }
   if (d.n_bonds < 0 || d.n_bends < 0) return why = "negative BOND / BEND term count", 1;
@@ -860,6 +897,10 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     }
     const double R = d0.sphere_consts[kBeadRadiusConst];
     sd.bb_cut2 = (R + R + 2.0) * (R + R + 2.0);
+    // the reference's branch for this residue size (brute force or hash cells)
+    sd.all_partners = (sd.nanocore || sd.n > kBeadBrute) ? 1 : 0;
+    sd.grid = sd.nanocore ? (sd.n > kCoreBrute ? 1 : 0) : (sd.n > kBeadBrute ? 1 : 0);
+    sd.grid_len = 2.0 * sphere_grid_range(d0);
     SMD_CUDA(cudaMemcpy(P.sph, &sd, sizeof sd, cudaMemcpyHostToDevice));
     SMD_CUDA(cudaMemcpy(dC, d0.sphere_consts, nc * sizeof(double), cudaMemcpyHostToDevice));
     SMD_CUDA(cudaMemcpy(fC, cf.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
@@ -867,6 +908,8 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     P.sphCf = fC;
     P.n_sph = sd.n;
     h->n_sph = sd.n;
+    h->sph_threads = (sd.n + 31) / 32 * 32;
+    h->sph_stage = sphere_stage_bytes(sd.n, h->mixed);
   }
   // ---- BOND / BEND term entries
   {

@@ -46,7 +46,9 @@ constexpr int kBlock = 256;
 constexpr int kBeadBlock = 128;
 constexpr int kScanTile = 2048;  // cells per scan block (256 threads x 8)
 constexpr int kLanes = 8;        // lanes per bead in the list build and the pair pass
-constexpr int kMaxSpheres = 16;  // BEAD beads of one handle (the reference's brute-force branch takes <= 20)
+constexpr int kMaxSpheres = 256; // BEAD or NANOCORE beads of one handle (one k_sphere block)
+constexpr int kBeadBrute = 20;   // BEAD residues up to this size take the brute-force branch
+constexpr int kCoreBrute = 49;   // NANOCORE residues up to this size take the brute-force branch
 constexpr int kBeadConst = 22;   // constants per ordered type pair of a BEAD residue (nBEADCONST)
 constexpr int kBeadBeadOff = 11; // BEADBEADOFFSET: bead-bead constants within a row
 
@@ -73,9 +75,23 @@ struct RepParams {  // per replica, fixed
 // the sums of the other beads' reactions on each sphere, gathered during
 // k_integ and used by k_sphere.  MIXED sums are int64 in units of 2^-32
 // (order-independent).
+//
+// Which partners a sphere's force takes follows the reference's two branches.
+// Brute force (BEAD up to 20 beads, NANOCORE up to 49 cores): every bead
+// except the residue's own spheres (BEAD, system.h:2165-2210) or except the
+// core itself (NANOCORE, :2221-2261).  Hash cells (more beads or cores,
+// :2104-2163 and :2264-2318): every bead except the sphere itself, found
+// through cells of side box / int(box / grid_len) and their 27 periodic
+// neighbours, so that along an axis of one cell every neighbour is the same
+// cell (visited 3 times) and along an axis of two cells the other cell is
+// visited twice.  Energies and size-change differences take every bead except
+// the sphere itself in both branches (:2936-3074, 3584-3700).
 struct SphereDev {
   int n;
   int nanocore;     // 1: a NANOCORE residue (per-sphere rows, no sphere-sphere term, no dU)
+  int all_partners; // 1: forces between spheres as bead partners (NANOCORE; BEAD hash-cell branch)
+  int grid;         // 1: the hash-cell branch, whose repeated neighbour cells multiply terms
+  double grid_len;  // cell side floor: BEAD 2 C[0]; NANOCORE 2 int(max C[0]) (system.h:2265-2277)
   int orig[kMaxSpheres];
   double mass[kMaxSpheres];   // 4 pi R^2 of each sphere
   double cut2[kMaxSpheres];   // bead-sphere range of each sphere (its row's constant 0, squared)

@@ -1233,15 +1233,81 @@ __device__ __forceinline__ void warp_atomic_add_q(long long v, long long* dst, i
     atomicAdd((unsigned long long*)dst, (unsigned long long)acc);
 }
 
-// Sphere <-> bead terms of bead i for every BEAD sphere (Blob::doBeadForce
-// brute-force branch, include/system.h:2165-2210, and doBeadPotential /
-// doBeadDPotential): the force on the bead into fs, and the reaction on each
-// sphere summed over the warp into the sphere's accumulator (MIXED: int64 in
-// units of 2^-32, exact in any order).  Energies and size-change differences
-// include every bead k != sphere, forces exclude the other spheres, as the
-// reference does.  The separation d = x_sphere - x_bead takes the minimum
+// Hash-cell counts of the reference's many-sphere branches for the current
+// box: int(box / grid_len) per axis, at least 1 (the reference divides by
+// zero below that; smd_create refuses such a box).
+__device__ __forceinline__ void sphere_grid_dims(const SphereDev* S, const double box[3], int n[3]) {
+  for (int a = 0; a < 3; ++a) {
+    const double q = box[a] / S->grid_len;
+    n[a] = q >= 1.0 ? (q < 1048576.0 ? (int)q : 1048576) : 1;
+  }
+}
+
+// How often the reference's 27 neighbour cells visit the cell of a partner
+// (getCell and neighIndices, analysis/cellInclude/cell.h:36-101): along an
+// axis of one cell all three offsets land on it, along an axis of two cells
+// the other cell is reached by two offsets and the own cell by one, and with
+// three or more cells a partner in range lies in exactly one neighbour.
+// Cells are packed 10 bits per axis and computed only for axes below three.
+__device__ __forceinline__ int sphere_cells(const double x[3], const double box[3], const int n[3]) {
+  int packed = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (n[a] != 2) continue;
+    const double c = floor(x[a] / (box[a] / n[a]));
+    packed |= (c >= 1.0 ? 1 : 0) << (10 * a);
+  }
+  return packed;
+}
+__device__ __forceinline__ int sphere_multiplicity(int cell_a, int cell_b, const int n[3]) {
+  int m = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (n[a] == 1) m *= 3;
+    else if (n[a] == 2) m *= (((cell_a >> (10 * a)) & 1) == ((cell_b >> (10 * a)) & 1)) ? 1 : 2;
+  }
+  return m;
+}
+
+// Per-block copy of the spheres, in dynamic shared memory of
+// sphere_stage_bytes(n, MIXED): the position word (MIXED: the 32-bit
+// fractional uint4, PLAIN: the double4) of each sphere, then its file index
+// and hash cell.  One dependent load chain per block instead of one per
+// sphere and warp.
+__host__ __device__ constexpr size_t sphere_stage_bytes(int n, bool mixed) {
+  return (size_t)n * ((mixed ? sizeof(uint4) : sizeof(double4)) + sizeof(int2));
+}
+extern __shared__ uint4 smd_sphere_stage[];
+
+template <bool MIXED>
+__device__ __forceinline__ void stage_spheres(const DevPtrs& P, int cur, const double box[3], const int gn[3]) {
+  const SphereDev* S = P.sph;
+  const int n = P.n_sph;
+  int2* info = reinterpret_cast<int2*>(reinterpret_cast<unsigned char*>(smd_sphere_stage) +
+                                        (size_t)n * (MIXED ? sizeof(uint4) : sizeof(double4)));
+  for (int s = threadIdx.x; s < n; s += blockDim.x) {
+    const int os = S->orig[s], js = P.inv[os];
+    if constexpr (MIXED) smd_sphere_stage[s] = P.m4[cur][js];
+    else reinterpret_cast<double4*>(smd_sphere_stage)[s] = P.d4[cur][js];
+    int cell = 0;
+    if (S->grid) {
+      const double x[3] = {P.x[js], P.y[js], P.z[js]};
+      cell = sphere_cells(x, box, gn);
+    }
+    info[s] = make_int2(os, cell);
+  }
+  __syncthreads();
+}
+
+// Sphere <-> bead terms of bead i for every sphere of a BEAD or NANOCORE
+// residue (Blob::doBeadForce, include/system.h:2043-2212, doNanoCoreForce,
+// :2216-2318, and doBeadPotential / doBeadDPotential / doNanoCorePotential):
+// the force on the bead into fs, and the reaction on each sphere summed over
+// the warp into the sphere's accumulator (MIXED: int64 in units of 2^-32,
+// exact in any order).  Energies and size-change differences take every bead
+// k != sphere; forces take the partners of the reference's branch for the
+// residue's size (SphereDev), each term repeated as often as the hash-cell
+// branch visits it.  The separation d = x_sphere - x_bead takes the minimum
 // image (MIXED: exact from the 32-bit fractional mirror; PLAIN: the
-// reference's half-box shift).  Called by whole warps.
+// reference's half-box shift).  Called by whole blocks after stage_spheres.
 template <bool MIXED, int FL>
 __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, bool active, Vec3<double>& fs,
                                              double& e_sph, double& du_sph) {
@@ -1249,8 +1315,15 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
   const int nT = P.tab->nT;
   const RepState& rs = P.rs[0];
   const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
+  int gn[3] = {3, 3, 3};
+  if (S->grid) sphere_grid_dims(S, box, gn);
+  stage_spheres<MIXED>(P, cur, box, gn);
+  const int n_sph = P.n_sph;
+  const int2* info = reinterpret_cast<const int2*>(reinterpret_cast<const unsigned char*>(smd_sphere_stage) +
+                                                   (size_t)n_sph * (MIXED ? sizeof(uint4) : sizeof(double4)));
   const bool me_sphere = active && (P.cinfo[i] < 0) && (P.cinfo[i] & 0x40000000);
-  int ti = 0;
+  const bool repeats = S->grid && (gn[0] < 3 || gn[1] < 3 || gn[2] < 3);
+  int ti = 0, my_cell = 0;
   uint4 mu = make_uint4(0, 0, 0, 0);
   double4 md = make_double4(0, 0, 0, 0);
   if (active) {
@@ -1261,21 +1334,22 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
       md = P.d4[cur][i];
       ti = __double_as_longlong(md.w) & 0xff;
     }
+    if (repeats) {
+      const double x[3] = {P.x[i], P.y[i], P.z[i]};
+      my_cell = sphere_cells(x, box, gn);
+    }
   }
   const int o = active ? P.orig[i] : -1;
-  for (int s = 0; s < P.n_sph; ++s) {
-    const int os = S->orig[s];
+  const bool force_partner = !me_sphere || S->all_partners;
+  for (int s = 0; s < n_sph; ++s) {
+    const int2 si = info[s];
     double r[3] = {0.0, 0.0, 0.0};
-    // BEAD: a sphere bead meets the other spheres only through the
-    // sphere-sphere term (k_sphere); NANOCORE: every core is an ordinary
-    // partner of the others
-    if (active && o != os && (!me_sphere || S->nanocore)) {
-      const int js = P.inv[os];
+    if (active && o != si.x) {
       double d[3];
       int ts;
       bool near;
       if constexpr (MIXED) {
-        const uint4 ms = P.m4[cur][js];
+        const uint4 ms = smd_sphere_stage[s];
         ts = ms.w & 0xff;
         // FP32 range test first; FP64 from the exact fractional differences
         const float fx = frac_delta(ms.x, mu.x, rs.len_per_frac[0]);
@@ -1288,7 +1362,7 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
           d[2] = frac_delta_d(ms.z, mu.z, box[2] * (1.0 / 4294967296.0));
         }
       } else {
-        const double4 ms = P.d4[cur][js];
+        const double4 ms = reinterpret_cast<const double4*>(smd_sphere_stage)[s];
         ts = __double_as_longlong(ms.w) & 0xff;
         d[0] = ms.x - md.x;
         d[1] = ms.y - md.y;
@@ -1312,8 +1386,9 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
           }
         }
         if constexpr ((FL & F_ENERGY) == 0) {
-          {
-            const double mag = bead_mag(dr2, row, cut2);
+          if (force_partner) {
+            double mag = bead_mag(dr2, row, cut2);
+            if (repeats) mag *= (double)sphere_multiplicity(my_cell, si.y, gn);
             for (int a = 0; a < 3; ++a) r[a] = d[a] * mag;
             fs.x -= r[0];
             fs.y -= r[1];
@@ -1345,10 +1420,10 @@ __device__ __forceinline__ void sphere_terms(const DevPtrs& P, int cur, int i, b
       }
     }
   }
-  // NANOCORE: a core's share of the other cores' terms (their reactions on it)
-  // joins its own sum, which k_sphere integrates
+  // a sphere's terms as the other spheres' partner (their reactions on it)
+  // join its own sum, which k_sphere integrates
   if constexpr ((FL & F_ENERGY) == 0) {
-    if (me_sphere && S->nanocore) {
+    if (me_sphere && S->all_partners) {
       const int me = P.cinfo[i] & 0xffff;
       const double f[3] = {fs.x, fs.y, fs.z};
       for (int a = 0; a < 3; ++a) {
@@ -2279,17 +2354,26 @@ __global__ void __launch_bounds__(kBeadBlock) k_finish(DevPtrs P, int cur, int m
   finalize_step(P, bm, se);
 }
 
-// BEAD spheres and NANOCORE cores after k_integ (one warp, one sphere per
-// lane): the total force on each sphere (its non-bonded force, the reactions
+// BEAD spheres and NANOCORE cores after k_integ (one block, one sphere per
+// thread): the total force on each sphere (its non-bonded force, the reactions
 // gathered in k_integ and the BEAD sphere-sphere terms,
 // include/system.h:2072-2098, or the cores' terms on each other), its
 // Langevin term, the mass division of MD.cpp:480-509 and, in a loop step, both half-kicks,
 // the drift and the wrap; then the step's list-rebuild decision.  The same
 // flags as k_integ select the variant.
 template <bool MIXED, int FL>
-__global__ void __launch_bounds__(32) k_sphere(DevPtrs P, int cur, StepEnd se) {
+__global__ void __launch_bounds__(kMaxSpheres) k_sphere(DevPtrs P, int cur, StepEnd se) {
   SphereDev* S = P.sph;
   const int s = threadIdx.x;
+  // every sphere's position word, so that the sphere-sphere loop reads
+  // shared memory instead of a dependent load chain per partner
+  using Word = typename std::conditional<MIXED, uint4, double4>::type;
+  __shared__ Word pos_s[kMaxSpheres];
+  if (s < S->n) {
+    const int js = P.inv[S->orig[s]];
+    if constexpr (MIXED) pos_s[s] = P.m4[cur][js]; else pos_s[s] = P.d4[cur][js];
+  }
+  __syncthreads();
   const long long it = P.g->it;
   const Tables& T = *P.tab;
   const RepParams& rp = P.rp[0];
@@ -2300,7 +2384,7 @@ __global__ void __launch_bounds__(32) k_sphere(DevPtrs P, int cur, StepEnd se) {
   if (s < S->n) {
     const int o = S->orig[s], j = P.inv[o];
     int ti;
-    if constexpr (MIXED) ti = P.m4[cur][j].w & 0xff; else ti = __double_as_longlong(P.d4[cur][j].w) & 0xff;
+    if constexpr (MIXED) ti = pos_s[s].w & 0xff; else ti = __double_as_longlong(pos_s[s].w) & 0xff;
     double F[3] = {0.0, 0.0, 0.0};
     if constexpr ((FL & F_ENERGY) == 0) {
       for (int d = 0; d < 3; ++d) {
@@ -2317,17 +2401,16 @@ __global__ void __launch_bounds__(32) k_sphere(DevPtrs P, int cur, StepEnd se) {
     if constexpr ((FL & F_PAIRONLY) == 0) {
       for (int t = 0; t < S->n && !S->nanocore; ++t) {  // BEAD sphere-sphere terms
         if (t == s) continue;
-        const int jt = P.inv[S->orig[t]];
         double d[3];
         int tt;
         if constexpr (MIXED) {
-          const uint4 a = P.m4[cur][j], b = P.m4[cur][jt];
+          const uint4 a = pos_s[s], b = pos_s[t];
           tt = b.w & 0xff;
           d[0] = frac_delta_d(a.x, b.x, box[0] * (1.0 / 4294967296.0));
           d[1] = frac_delta_d(a.y, b.y, box[1] * (1.0 / 4294967296.0));
           d[2] = frac_delta_d(a.z, b.z, box[2] * (1.0 / 4294967296.0));
         } else {
-          const double4 a = P.d4[cur][j], b = P.d4[cur][jt];
+          const double4 a = pos_s[s], b = pos_s[t];
           tt = __double_as_longlong(b.w) & 0xff;
           d[0] = a.x - b.x;
           d[1] = a.y - b.y;
@@ -2404,41 +2487,63 @@ __global__ void __launch_bounds__(32) k_sphere(DevPtrs P, int cur, StepEnd se) {
         const unsigned int fx = to_frac(x[0], rs.frac_per_len[0]), fy = to_frac(x[1], rs.frac_per_len[1]),
                            fz = to_frac(x[2], rs.frac_per_len[2]);
         vmax = displacement(P.ref[j], fx, fy, fz, rs);
-        if constexpr (MIXED) {
-          const uint4 me = P.m4[cur][j];
-          P.m4[cur ^ 1][j] = make_uint4(fx, fy, fz, me.w);
-        } else {
-          const double4 me = P.d4[cur][j];
-          P.d4[cur ^ 1][j] = make_double4(x[0], x[1], x[2], me.w);
-        }
+        if constexpr (MIXED) P.m4[cur ^ 1][j] = make_uint4(fx, fy, fz, pos_s[s].w);
+        else P.d4[cur ^ 1][j] = make_double4(x[0], x[1], x[2], pos_s[s].w);
       }
     }
   }
-  __syncwarp();
-  // every lane has read its accumulator: clear them for the next pass
+  // each thread has read its own accumulator: clear it for the next pass
   if (s < S->n)
     for (int d = 0; d < 3; ++d) {
       S->fq[s][d] = 0;
       S->fd[s][d] = 0.0;
     }
+  // block sums in a fixed order (warps, then warp 0 over them)
+  __shared__ double red_d[kMaxSpheres / 32];
+  __shared__ long long red_q[kMaxSpheres / 32];
+  __shared__ float red_f[kMaxSpheres / 32];
+  const int lane = s & 31, warp = s >> 5, nw = blockDim.x >> 5;
   if constexpr ((FL & F_ENERGY) != 0) {
     e = warp_sum(e);
-    if (s == 0 && e != 0.0) atomicAdd(&P.rs[0].e_sphere, e);
+    if (lane == 0) red_d[warp] = e;
+    __syncthreads();
+    if (s == 0) {
+      double t = 0.0;
+      for (int w = 0; w < nw; ++w) t += red_d[w];
+      if (t != 0.0) atomicAdd(&P.rs[0].e_sphere, t);
+    }
   }
   if constexpr ((FL & F_DU) != 0) {
     if constexpr (MIXED) {
       long long q = __double2ll_rn(du * 4294967296.0);
 #pragma unroll
       for (int w = 16; w > 0; w >>= 1) q += __shfl_xor_sync(0xffffffffu, q, w);
-      if (s == 0 && q != 0) atomicAdd((unsigned long long*)&P.rs[0].dUq_bond, (unsigned long long)q);
+      if (lane == 0) red_q[warp] = q;
+      __syncthreads();
+      if (s == 0) {
+        long long t = 0;
+        for (int w = 0; w < nw; ++w) t += red_q[w];
+        if (t != 0) atomicAdd((unsigned long long*)&P.rs[0].dUq_bond, (unsigned long long)t);
+      }
     } else {
       du = warp_sum(du);
-      if (s == 0 && du != 0.0) atomicAdd(&P.rs[0].dU_bond, du);
+      if (lane == 0) red_d[warp] = du;
+      __syncthreads();
+      if (s == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t += red_d[w];
+        if (t != 0.0) atomicAdd(&P.rs[0].dU_bond, t);
+      }
     }
   }
   if constexpr ((FL & (F_STOP | F_INIT | F_FORCES | F_ENERGY)) == 0) {
     vmax = warp_max(vmax);
-    finalize_step(P, vmax, se);
+    if (lane == 0) red_f[warp] = vmax;
+    __syncthreads();
+    float bm = 0.f;
+    if (s == 0)
+      for (int w = 0; w < nw; ++w) bm = fmaxf(bm, red_f[w]);
+    finalize_step(P, bm, se);
   }
 }
 

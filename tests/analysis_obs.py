@@ -6,6 +6,17 @@ height-fluctuation spectrum of a membrane from its frames_ and size_ files).
 That tool links FFTW, which this image does not have, so the restatement is
 checked against a direct discrete Fourier sum and an analytic mode instead of
 against the tool's own output.
+
+width_frames restates analysis/avgThicknessFrames.cpp (the membrane's width
+along one axis: the standard deviation of the selected beads' coordinate in
+columns of the other two axes, averaged over the columns and the frames).
+The tool's column index is broken as written (avgThicknessFrames.cpp:141-143
+assigns the x index twice, from the raw coordinate, and leaves the y index
+uninitialised, so its output is undefined), and its column count along the
+second axis is taken from the first axis's length (:131-132).  The
+restatement keeps the second quirk and computes the column index the tool
+evidently intends, floor(coordinate / column side); it is checked against a
+hand-worked case instead of the tool's output.
 """
 from __future__ import annotations
 
@@ -103,3 +114,39 @@ def structure_factor_frames(frames_path, size_path, store_interval, from_time, n
             lx.append(box[0])
     q = np.arange(1, nx // 2) * 2.0 * np.pi / np.mean(lx)
     return q, np.array(spectra)
+
+
+def frame_width(types, xyz, box, dimension, cutoff, select):
+    """One frame of avgThicknessFrames.cpp:127-170: columns of side
+    (Lx / int(Lx / cutoff), Ly / int(Lx / cutoff)) over the two axes after
+    `dimension`; in each column the selected beads' mean and mean square of
+    coordinate `dimension`; the square root of their difference summed over
+    the columns (0 for an empty one) and divided by the number of non-empty
+    columns."""
+    a1, a2 = (dimension + 1) % 3, (dimension + 2) % 3
+    nsx = int(box[0] / cutoff)
+    nsy = int(box[0] / cutoff)  # the tool's ns.y comes from size.x
+    csx, csy = box[0] / nsx, box[1] / nsy
+    keep = np.isin(types, select)
+    p = xyz[keep]
+    cx = np.minimum(np.floor(p[:, a1] / csx).astype(int), nsx - 1)
+    cy = np.minimum(np.floor(p[:, a2] / csy).astype(int), nsy - 1)
+    cell = cx + cy * nsx
+    cnt = np.bincount(cell, minlength=nsx * nsy).astype(float)
+    s1 = np.bincount(cell, weights=p[:, dimension], minlength=nsx * nsy)
+    s2 = np.bincount(cell, weights=p[:, dimension] ** 2, minlength=nsx * nsy)
+    filled = cnt != 0
+    avg = s1[filled] / cnt[filled]
+    avg2 = s2[filled] / cnt[filled]
+    total = np.sqrt(avg2 - avg * avg).sum()
+    return total / filled.sum() if filled.any() else 0.0
+
+
+def width_frames(frames_path, size_path, store_interval, from_time, dimension, cutoff, select):
+    """avgThicknessFrames.cpp as a whole: per-frame widths from `from_time` on
+    (the tool prints their mean and population standard deviation); frames
+    and boxes are paired as structureFactorFrames pairs them (:87-124)."""
+    frames = read_frames(frames_path)
+    times, boxes = frame_sizes(read_sizes(size_path), len(frames), store_interval)
+    return np.array([frame_width(types, xyz, box, dimension, cutoff, select)
+                     for (types, xyz), t, box in zip(frames, times, boxes) if t >= from_time])

@@ -340,6 +340,156 @@ def to_nanocore(path, sep):
     open(path, "w").write("\n".join(out))
 
 
+def to_many_spheres(path, count, seed, size=None, pair_gap=None):
+    """Adds spheres to the BEAD residue of a vesicle-and-sphere .mpd until it
+    holds `count` beads of the sphere's type: the generator's sphere, then
+    spheres at its distance from the vesicle's centre in other directions
+    (tangent to the vesicle like it), then (with `pair_gap`) two pairs in the
+    solvent `pair_gap` apart, then solvent spheres at least one range from
+    every lipid bead.  Spheres keep 2 radius + 1 between centres, except the
+    pairs.  `size` replaces the box first (beads stay put)."""
+    m = smd.read_mpd(path)
+    s0 = int(m.sphere_index[0])
+    ts, nT = int(m.type[s0]), m.n_types
+    rad, rng_c0 = float(m.sphere_consts[4]), float(m.sphere_consts[0])
+    box = np.array(size if size is not None else m.box, dtype=float)
+    lip = m.pos[np.arange(len(m.type)) != s0]
+    centre = lip.mean(0)
+    d0 = np.linalg.norm(m.pos[s0] - centre)
+    rng = np.random.default_rng(seed)
+
+    def mind(p, q):
+        d = q - p
+        d -= box * np.round(d / box)
+        return np.sqrt((d * d).sum(-1))
+
+    spheres = [m.pos[s0].copy()]
+    # tangent to the vesicle: Fibonacci directions, kept where far enough apart
+    k = 0
+    while len(spheres) < count and k < 400:
+        z = 1.0 - 2.0 * (k + 0.5) / 400
+        phi = k * np.pi * (3.0 - np.sqrt(5.0))
+        k += 7
+        p = centre + d0 * np.array([np.sqrt(1 - z * z) * np.cos(phi), np.sqrt(1 - z * z) * np.sin(phi), z])
+        p = np.mod(p, box)
+        if mind(p, np.array(spheres)).min() > 2 * rad + 1 and len(spheres) < max(2, count // 2):
+            spheres.append(p)
+    tries = 0
+
+    def free(p, sep):
+        return mind(p, lip).min() > rng_c0 + 0.5 and mind(p, np.array(spheres)).min() > sep
+
+    if pair_gap is not None:
+        for _ in range(2):
+            if len(spheres) + 2 > count:
+                break
+            while True:
+                tries += 1
+                p = rng.uniform(0, box)
+                u = rng.normal(size=3)
+                q = np.mod(p + pair_gap * u / np.linalg.norm(u), box)
+                if free(p, 2 * rad + 1) and free(q, 2 * rad + 1) and mind(p, q[None])[0] > 2 * rad + 1e-9:
+                    spheres += [p, q]
+                    break
+    while len(spheres) < count:
+        tries += 1
+        assert tries < 200000, "no room for the spheres"
+        p = rng.uniform(0, box)
+        if free(p, 2 * rad + 1):
+            spheres.append(p)
+    extra = spheres[1:]
+    n = len(m.type)
+    tok = open(path).read().split("\n")
+    out, i = [], 0
+    while i < len(tok):
+        ln = tok[i]
+        key = ln.strip()
+        if key.startswith("nParticles"):
+            out.append(f"nParticles {n + len(extra)} ")
+        elif key.startswith("size") and size is not None:
+            out.append("size %.17g %.17g %.17g " % tuple(box))
+        elif key == "positions":
+            out.extend(tok[i:i + 1 + n])
+            out.extend(" %d %.15g %.15g %.15g" % (ts, *p) for p in extra)
+            i += n + 1
+            continue
+        elif key == "velocities":
+            out.extend(tok[i:i + 1 + n])
+            out.extend(" 0 0 0" for _ in extra)
+            i += n + 1
+            continue
+        elif key.split() == ["9", "1"]:
+            # the BEAD block: header, its 22 nT^2 constants, then one index per
+            # bead; the sphere-sphere row becomes the head-sphere row, so that
+            # spheres in each other's range attract as bead partners too
+            out.append("9\t %d" % len(spheres))
+            i += 1
+            vals = []
+            while len(vals) < 22 * nT * nT:
+                vals += tok[i].split()
+                i += 1
+            C = np.array(vals, dtype=float).reshape(nT * nT, 22)
+            C[ts * nT + ts] = C[ts * nT + 2]
+            out.extend(" " + "  ".join("%.17g" % x for x in row) for row in C)
+            while not tok[i].split():
+                out.append(tok[i])
+                i += 1
+            out.append(tok[i])  # the generator's sphere
+            out.extend(f" {n + q}" for q in range(len(extra)))
+            i += 1
+            continue
+        else:
+            out.append(ln)
+        i += 1
+    open(path, "w").write("\n".join(out))
+
+
+def make_spheres(tmp):
+    """spheres24 / spheres6 / spheres21n2: BEAD residues of several beads on a
+    300-lipid vesicle, dumped by the reference (forces at the start
+    configuration, as sphere300).  spheres24 (radius 1.5, range 3.5) takes the
+    hash-cell branch with 5 cells per axis and holds two sphere pairs 3.25
+    apart, inside each other's range; spheres6 keeps six of its beads (the
+    generator's, three tangent ones and the first close pair), the
+    brute-force branch; spheres21n2 (radius 6, range 8) takes the hash-cell
+    branch in a 40 x 52 x 52 box, 2 x 3 x 3 cells, where the reference visits
+    the other cell along x twice.  The beads outside a residue keep the
+    sphere's type and interact through the pair table only."""
+    for name, count, R, size, gap in (("spheres24", 24, 2.5, None, 3.25), ("spheres6", 6, 2.5, None, 3.25),
+                                      ("spheres21n2", 21, 7.0, (40.0, 52.0, 52.0), None)):
+        f = os.path.join(tmp, name + ".mpd")
+        smd.synth_vesicle_sphere(f, 99, 300, 3.45, 40.0, R, -10.0, 10.0, 0.8)
+        if name == "spheres6":
+            shutil.copy(os.path.join(tmp, "spheres24.mpd"), f)
+            to_some_spheres(f, [0, 1, 2, 3, 12, 13])
+        else:
+            to_many_spheres(f, count, 5, size, gap)
+        dump_case(tmp, name, name)
+
+
+def to_some_spheres(path, keep):
+    """Keeps the beads of the BEAD residue at the list positions `keep` (the
+    others stay as ordinary beads of the sphere's type)."""
+    tok = open(path).read().split("\n")
+    mol = tok.index("molecule ")
+    out, i = tok[:mol], mol
+    while i < len(tok):
+        f = tok[i].split()
+        if len(f) == 2 and f[0] == "9":  # a molecule header: BEAD and its bead count
+            out.append("9\t %d" % len(keep))
+            i += 1
+            while len(tok[i].split()) != 1:  # constant rows and blank lines
+                out.append(tok[i])
+                i += 1
+            idx = tok[i:i + int(f[1])]
+            out.extend(idx[q] for q in keep)
+            i += int(f[1])
+            continue
+        out.append(tok[i])
+        i += 1
+    open(path, "w").write("\n".join(out))
+
+
 def make_msd(tmp):
     """msd_bil/: a reference run that crosses 100 tau, so that it tracks
     diffusion: the 200-lipid bilayer of traj_bil as a checkpoint at
@@ -478,6 +628,13 @@ def main():
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
         print("nanocore fixtures written to", HERE)
+        return
+    if "--only-spheres" in sys.argv:  # the many-sphere BEAD fixtures alone
+        try:
+            make_spheres(tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        print("sphere fixtures written to", HERE)
         return
     if "--only-fields" in sys.argv:  # the external-field fixtures alone
         try:

@@ -83,3 +83,39 @@ def test_frame_size_pairing():
     t, b = frame_sizes(sizes, 4, 1.0)
     assert np.allclose(t, [0.5, 1.5, 2.5, 3.5])
     assert np.allclose(b[:, 0], [11, 12, 14, 14])
+
+
+def test_width_of_two_flat_leaflets():
+    """Heads of two flat leaflets at z0 +- h in every column: each column's
+    standard deviation is h (equal counts), whatever the column grid."""
+    from analysis_obs import frame_width
+    rng = np.random.default_rng(1)
+    box = np.array([20.0, 20.0, 30.0])
+    n = 2000
+    x = rng.uniform(0, box[0], n)
+    y = rng.uniform(0, box[1], n)
+    z = np.where(np.arange(n) % 2 == 0, 15.0 + 2.5, 15.0 - 2.5)
+    types = np.full(n, 2)
+    xyz = np.stack([x, y, z], 1)
+    # pair each upper head with a lower one in the same column
+    xyz[1::2, :2] = xyz[0::2, :2]
+    w = frame_width(types, xyz, box, 2, 2.0, [2])
+    assert abs(w - 2.5) < 1e-9
+    # other types are ignored; along x the same beads have a uniform spread
+    types2 = types.copy()
+    types2[:10] = 3
+    assert frame_width(types2, xyz, box, 2, 2.0, [3]) > 0.0
+    wx = frame_width(types, xyz, box, 0, 4.0, [2])
+    assert 0.0 < wx < box[0] / np.sqrt(12.0) + 1e-9
+
+
+def test_width_columns_follow_the_tools_quirk():
+    """The second axis takes its column count from the first axis's length:
+    a 20 x 10 box with cutoff 2 has 10 x 10 columns of 2 x 1."""
+    from analysis_obs import frame_width
+    box = np.array([20.0, 10.0, 30.0])
+    # one column holds beads at y 0.2 and 0.7 (same 1-wide column) with z 10, 12
+    xyz = np.array([[1.0, 0.2, 10.0], [1.0, 0.7, 12.0], [1.0, 1.2, 20.0]])
+    types = np.array([2, 2, 2])
+    # columns: (0, 0) holds two beads (std 1), (0, 1) one bead (std 0)
+    assert abs(frame_width(types, xyz, box, 2, 2.0, [2]) - 0.5) < 1e-12

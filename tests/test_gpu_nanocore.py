@@ -106,3 +106,62 @@ def test_bead_and_core_residues_together_are_refused(built):
     m.sphere_index, m.sphere_consts = s["sphere_index"].astype(np.int32), s["sphere_consts"]
     with pytest.raises(smd.SmdError, match="BEAD and a NANOCORE"):
         smd.System(m)
+
+
+def _many_cores(g, count, range_=None, seed=3):
+    """core300 with `count` cores: the two of the fixture and more of the same
+    row in the solvent, at least 2 radius + 1 from the others and one range
+    from every lipid bead; `range_` replaces every core's constant 0."""
+    rng = np.random.default_rng(seed)
+    pos, typ, vel = g["pos"].copy(), g["type"].copy(), g["vel"].copy()
+    box = g["box"]
+    ci = list(g["core_index"])
+    rows = np.asarray(g["core_consts"]).reshape(-1, 22).copy()
+    rad, c0 = rows[0][4], rows[0][0]
+    lip = np.delete(pos, ci, axis=0)
+
+    def mind(p, q):
+        d = q - p
+        d -= box * np.round(d / box)
+        return np.sqrt((d * d).sum(-1))
+
+    cores = [pos[k] for k in ci]
+    while len(cores) < count:
+        p = rng.uniform(0, box)
+        if mind(p, lip).min() > c0 + 0.5 and mind(p, np.array(cores)).min() > 2 * rad + 1:
+            cores.append(p)
+    extra = np.array(cores[len(ci):])
+    n = len(typ)
+    pos = np.concatenate([pos, extra])
+    typ = np.concatenate([typ, np.full(len(extra), typ[ci[0]], typ.dtype)])
+    vel = np.concatenate([vel, np.zeros_like(extra)])
+    rows = np.concatenate([rows, np.repeat(rows[:1], len(extra), 0)])
+    if range_ is not None:
+        rows[:, 0] = range_
+    h = dict(g)
+    h.update(pos=pos, type=typ, vel=vel, core_index=np.array(ci + list(range(n, n + len(extra))), np.int32),
+             core_consts=rows)
+    return h
+
+
+@pytest.mark.parametrize("range_", [None, 7.5])
+@pytest.mark.parametrize("precision", PREC)
+def test_many_cores_against_oracle(built, oracle, precision, range_):
+    """50 cores take the reference's hash-cell branch (include/system.h:
+    2264-2318): with the fixture's range 4 the cells are 8 wide (5 per axis)
+    and every partner counts once; with range 7.5 the int-truncated range 7
+    gives cells 14 wide, 2 per axis, and partners in the other cell along an
+    axis count twice (four or eight times across two or three axes)."""
+    h = _many_cores(load_golden("core300"), 50, range_)
+    want = oracle.forces(h)
+    s = smd.System(mpd_from_golden(h), precision=precision)
+    f = s.forces()
+    err = np.abs(f - want).max() / np.abs(want).max()
+    print(f"range {range_} precision {precision}: max rel err {err:.3e}")
+    assert err <= FORCE_TOL[precision]
+    if range_ is not None:
+        # the repeated cells matter: 49 cores (brute force) give other forces
+        h49 = dict(h)
+        h49["core_index"] = h["core_index"][:49]
+        h49["core_consts"] = h["core_consts"][:49]
+        assert np.abs(oracle.forces(h49)[h["core_index"][:49]] - want[h["core_index"][:49]]).max() > 1e-6

@@ -5,8 +5,8 @@ reference from per-thread MT19937 streams, so trajectories differ sample by
 sample.  The GPU `MD` executable (mixed precision) and the oracle's
 restatement of the reference `MD` loop run the same 400-lipid bilayer with the
 constant-tension barostat on; after equilibration their time averages of
-temperature, area per lipid, potential energy per bead and bilayer thickness
-must agree within 4 combined standard errors (block averages) plus a 0.5 %
+temperature, area per lipid, potential energy per bead, bilayer thickness and
+the heads' width of the reference's avgThicknessFrames tool must agree within 4 combined standard errors (block averages) plus a 0.5 %
 allowance for the finite run.  A 2,048-lipid bilayer compares the
 height-fluctuation spectrum of the reference's structureFactorFrames tool.
 """
@@ -16,6 +16,7 @@ import subprocess
 
 import numpy as np
 import pytest
+from analysis_obs import width_frames
 
 import softmold_gb300 as smd
 
@@ -99,6 +100,9 @@ def test_observables_match_reference_statistics(built, tmp_path):
             "area_per_lipid": _block_mean(size[:, 1] * size[:, 2] / (N_LIPIDS / 2)),
             "potential_per_bead": _block_mean(pot / n_beads),
             "thickness": _block_mean(_thickness(d), blocks=5),
+            # avgThicknessFrames bil 20 z 2 2: the heads' width along z in 2-sigma columns
+            "head_width": _block_mean(width_frames(os.path.join(d, "frames_bil.xyz"), os.path.join(d, "size_bil.dat"),
+                                                   STORE_TAU, EQUIL_TAU, 2, 2.0, [2]), blocks=5),
         }
     for key in results["gpu"]:
         (mg, sg), (mc, sc) = results["gpu"][key], results["cpu"][key]

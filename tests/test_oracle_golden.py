@@ -7,7 +7,8 @@ import numpy as np
 import pytest
 from conftest import load_golden
 
-CASES = ["ves300", "bil400", "sphere300", "net400", "field400", "core300", "mix400"]
+CASES = ["ves300", "bil400", "sphere300", "net400", "field400", "core300", "mix400", "spheres6", "spheres24",
+         "spheres21n2"]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -54,3 +55,47 @@ def test_sphere_case_interacts():
     g = load_golden("sphere300")
     assert len(g["sphere_index"]) == 1
     assert g["energy"][2] != 0.0
+
+
+def _sphere_geometry(g):
+    idx = g["sphere_index"]
+    p = g["pos"][idx]
+    d = p[:, None, :] - p[None, :, :]
+    d -= g["box"] * np.round(d / g["box"])
+    r = np.sqrt((d * d).sum(-1))
+    np.fill_diagonal(r, np.inf)
+    return r, float(g["sphere_consts"][0])
+
+
+def test_many_sphere_cases_exercise_both_branches(oracle):
+    """spheres6 takes the brute-force branch (<= 20 beads) and spheres24 the
+    hash-cell branch; both hold sphere pairs within each other's bead range,
+    whose force the two branches treat differently.  spheres21n2 has two hash
+    cells along x, where the reference visits the other cell twice."""
+    for case, n in (("spheres6", 6), ("spheres24", 24), ("spheres21n2", 21)):
+        g = load_golden(case)
+        assert len(g["sphere_index"]) == n
+        assert g["energy"][2] != 0.0
+    for case in ("spheres6", "spheres24"):
+        r, rng = _sphere_geometry(load_golden(case))
+        assert (r < rng).sum() >= 2  # an ordered pair at least
+    g = load_golden("spheres21n2")
+    rng = float(g["sphere_consts"][0])
+    cells = (g["box"] / (2 * rng)).astype(int)
+    assert list(cells) == [2, 3, 3]
+    # head beads in a sphere's range but in the other cell along x: their
+    # terms count twice
+    cx = np.floor(g["pos"][:, 0] / (g["box"][0] / 2)).astype(int)
+    crossing = 0
+    for s in g["sphere_index"]:
+        d = g["pos"] - g["pos"][s]
+        d -= g["box"] * np.round(d / g["box"])
+        r = np.sqrt((d * d).sum(1))
+        crossing += int(((r > 0) & (r < rng) & (cx != cx[s])).sum())
+    assert crossing >= 1
+    # the same beads through the brute-force rule would give other forces
+    g6 = dict(load_golden("spheres24"))
+    f_hash = oracle.forces(g6)
+    g6["sphere_index"] = g6["sphere_index"][:20]
+    f_brute = oracle.forces(g6)
+    assert np.abs(f_hash - f_brute).max() > 0
