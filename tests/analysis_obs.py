@@ -10,10 +10,10 @@ against the tool's own output.
 width_frames restates analysis/avgThicknessFrames.cpp (the membrane's width
 along one axis: the standard deviation of the selected beads' coordinate in
 columns of the other two axes, averaged over the columns and the frames).
-The tool's column index is broken as written (avgThicknessFrames.cpp:141-143
+The tool's column index is broken as written (avgThicknessFrames.cpp:149-150
 assigns the x index twice, from the raw coordinate, and leaves the y index
 uninitialised, so its output is undefined), and its column count along the
-second axis is taken from the first axis's length (:131-132).  The
+second axis is taken from the first axis's length (:134-135).  The
 restatement keeps the second quirk and computes the column index the tool
 evidently intends, floor(coordinate / column side); it is checked against a
 hand-worked case instead of the tool's output.

@@ -39,6 +39,10 @@ Fixtures
                    measurement after 100 tau (MD.cpp:64, 538-539) and writes
                    meanSquareDisplacement_bil.dat; sha256 of every file and the
                    small ones verbatim (`--only-msd`).
+  spheres6.npz,    300-lipid vesicles with BEAD residues of 6, 24 and 21
+  spheres24.npz,   spheres (both force branches of Blob::doBeadForce, and
+  spheres21n2.npz  hash cells of two along x), dumped as the cases above
+                   (`--only-spheres`).
   generators.json  sha256 of the reference generators' .mpd for a few seeds.
 Inputs are seeded synthetic membranes built in the reference generators' terms
 (softmold_gb300 synth_*, byte-identical to generate/liposome and bilayer).
