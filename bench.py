@@ -82,6 +82,16 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+# Verlet-list skin per workload.  The list lives a whole number of steps,
+# mostly two, at kT 3 and dt 0.02: it is rebuilt once the fastest bead has
+# moved skin/2, about 0.19 sigma per step at 60,000 beads and more for more
+# beads (the largest of more Maxwell draws).  The smallest skin that still
+# keeps two steps is the fastest: 0.42 for the 15,000- and 60,000-bead
+# systems; the 240,001-bead vesicle and the 64-replica batch (up to 480,000
+# beads) rebuild after one step too often at 0.42 and keep the library's 0.5.
+SKIN_DEFAULT = {"bilayer20k": 0.42, "vesicle5k": 0.42}
+
+
 def workload(args, rank, tmpdir, world=1):
     """(paths, systems, config) of the benchmarked workload for one rank.
     The config dict describes the whole job and is the same in both arms."""
@@ -411,7 +421,8 @@ def main():
     ap.add_argument("--workload", default="bilayer20k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--skin", type=float, default=0.5)
+    ap.add_argument("--skin", type=float, default=None,
+                    help="Verlet-list skin in sigma (default: per workload, SKIN_DEFAULT)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the step kernels one by one (for profilers that cannot see kernels in graphs)")
     ap.add_argument("--profile-run", type=int, default=0, metavar="STEPS",
@@ -419,6 +430,8 @@ def main():
                          "configuration, run STEPS more MD steps and exit (no timing, no JSON line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.skin is None:
+        args.skin = SKIN_DEFAULT.get(args.workload, 0.5)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

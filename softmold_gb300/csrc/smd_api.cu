@@ -947,7 +947,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
       const double one[3] = {1.0, 1.0, 1.0};
       for (int k = 0; k < 3; ++k) rs[r].box[k] = d.box[k];
       set_scale(rs[r], one);
-      derive_box(rs[r], h->rp[r].cell_cap, T.list_cut);
+      derive_box(rs[r], h->rp[r].cell_cap, T.list_cut, T.rc);
       for (int i = 0; i < d.n; ++i, ++b) {
         hx[b] = d.pos[3 * i];
         hy[b] = d.pos[3 * i + 1];
@@ -1105,7 +1105,7 @@ int smd_set_box(smd_system* h, int replica, const double box[3]) {
   SMD_CUDA(cudaMemcpyAsync(&rs, h->P.rs + replica, sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
   for (int k = 0; k < 3; ++k) rs.box[k] = box[k];
-  derive_box(rs, h->rp[replica].cell_cap, h->tab.list_cut);
+  derive_box(rs, h->rp[replica].cell_cap, h->tab.list_cut, h->tab.rc);
   SMD_CUDA(cudaMemcpyAsync(h->P.rs + replica, &rs, sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
   if (h->mixed)
     SMD_LAUNCH(h, k_mirror<true><<<h->grid(), kBlock, 0, h->stream>>>(h->P, h->cur));

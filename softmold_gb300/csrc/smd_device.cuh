@@ -116,7 +116,11 @@ struct RepState {  // per replica, updated on the device
   long long n_trial, n_accept;
   int accept;
   int ncell[3];
+  int refn[3];       // the reference's cells per axis, int(L / rc) (the size-change passes' grid)
   int pad;
+  double ref_cs[3];  // its cell sides L / refn
+  float ref_inv_cs[3];
+  float pad_r;
 };
 
 // Sets a replica's trial scale and its FP32 factors s^2 - 1 (one rounding of
@@ -285,16 +289,21 @@ __device__ __forceinline__ unsigned int to_frac(double x, double frac_per_len) {
   return (unsigned int)(long long)(x * frac_per_len);
 }
 
-// Derived box quantities of a replica: fractional scales and the Verlet-list
-// grid (cells of at least list_cut, at most cap cells).  Computed on the host
+// Derived box quantities of a replica: fractional scales, the Verlet-list
+// grid (cells of at least list_cut, at most cap cells) and the reference's
+// cell grid (cells of at least rc).  Computed on the host
 // at creation and on the device when a box move is accepted; the same IEEE
 // arithmetic gives the same grid on both.
-__host__ __device__ inline void derive_box(RepState& rs, int cap, double list_cut) {
+__host__ __device__ inline void derive_box(RepState& rs, int cap, double list_cut, double rc) {
   for (int d = 0; d < 3; ++d) {
     rs.frac_per_len[d] = 4294967296.0 / rs.box[d];
     rs.len_per_frac[d] = (float)(rs.box[d] * (1.0 / 4294967296.0));
     int n = int(rs.box[d] / list_cut);
     rs.ncell[d] = n < 1 ? 1 : n;
+    const int m = int(rs.box[d] / rc);
+    rs.refn[d] = m < 1 ? 1 : m;
+    rs.ref_cs[d] = rs.box[d] / rs.refn[d];
+    rs.ref_inv_cs[d] = (float)(1.0 / rs.ref_cs[d]);
   }
   while ((long long)rs.ncell[0] * rs.ncell[1] * rs.ncell[2] > cap) {
     int m = 0;

@@ -1660,16 +1660,27 @@ constexpr int kGather = 4;  // neighbour gathers in flight per lane (mixed pair 
 // apart that the box rescale would bring within rc adds nothing to the
 // reference's difference.  The cell of each axis is the reference's
 // int(x / cellSize) with the x >= n -> n-1 correction, packed in 21 bits.
+// The quotient is formed in FP32 from a reciprocal: three roundings of
+// 2^-24 put it within 1.8e-7 q of x / cs, below 7.4e-4 for q < 4096, so a
+// quotient more than 1e-3 from an integer has the reference's integer part;
+// the others (and larger quotients) take the FP64 division.
+__device__ __forceinline__ int ref_cell_coord(double x, double cs, float inv_cs, int n) {
+  const float q = (float)x * inv_cs;
+  const float fr = q - floorf(q);
+  if (fr < 1e-3f || fr > 1.f - 1e-3f || !(q < 4096.f)) return cell_coord(x, cs, n);
+  const int c = (int)q;
+  return c >= n ? n - 1 : (c < 0 ? 0 : c);
+}
 __global__ void __launch_bounds__(kBlock) k_ref_cells(DevPtrs P) {
   const int i = blockIdx.x * kBlock + threadIdx.x;
   if (i >= P.n) return;
   const RepState& rs = P.rs[rep_of(P, i)];
-  const double rc = P.tab->rc;
   const double x[3] = {P.x[i], P.y[i], P.z[i]};
   unsigned long long key = 0;
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const int n = int(rs.box[d] / rc);
-    key |= (unsigned long long)(cell_coord(x[d], rs.box[d] / n, n) & 0x1fffff) << (21 * d);
+    const int n = rs.refn[d];
+    key |= (unsigned long long)(ref_cell_coord(x[d], rs.ref_cs[d], rs.ref_inv_cs[d], n) & 0x1fffff) << (21 * d);
   }
   P.refcell[i] = key;
 }
@@ -1678,20 +1689,16 @@ __global__ void __launch_bounds__(kBlock) k_ref_cells(DevPtrs P) {
 // cells of the reference's grid (periodic).  The size-change passes ask this
 // only for pairs beyond rc at the current positions (pairs within rc are
 // always neighbours).
-__device__ __forceinline__ bool ref_cells_adjacent(const DevPtrs& P, int a, int b, const int n[3]) {
+__device__ __forceinline__ bool ref_cells_adjacent(const DevPtrs& P, const RepState& rs, int a, int b) {
   const unsigned long long ka = P.refcell[a], kb = P.refcell[b];
   bool adj = true;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     int dd = (int)((ka >> (21 * d)) & 0x1fffff) - (int)((kb >> (21 * d)) & 0x1fffff);
     dd = dd < 0 ? -dd : dd;
-    adj = adj && (dd <= 1 || dd == n[d] - 1);
+    adj = adj && (dd <= 1 || dd == rs.refn[d] - 1);
   }
   return adj;
-}
-// The reference grid's cells per axis of a replica.
-__device__ __forceinline__ void ref_grid(const DevPtrs& P, const RepState& rs, int n[3]) {
-  for (int d = 0; d < 3; ++d) n[d] = int(rs.box[d] / P.tab->rc);
 }
 
 // Mixed-form pair sums of bead i over its Verlet list, lane `sub` of its G
@@ -1811,8 +1818,6 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
     // the reference counts those in neighbouring cells of its grid
     // (ref_cells_adjacent); take the others' terms back out, bit for bit.
     if (entered) {
-      int refn[3];
-      ref_grid(P, rs, refn);
       for (int k2 = sub; k2 < nn; k2 += G) {
         const int j = __ldg(nb + k2);
         const uint4 o = P.m4[cur][j];
@@ -1820,7 +1825,7 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
         const float r2 = dist2(dx, dy, dz);
         const float q = dscale(dx, dy, dz);
         const float rn2 = __fadd_rn(r2, q);
-        if (j > i && !(r2 < rc2) && rn2 < rc2 && !ref_cells_adjacent(P, i, j, refn)) dq -= du_q(r2, q, rn2, o.w & 0xff);
+        if (j > i && !(r2 < rc2) && rn2 < rc2 && !ref_cells_adjacent(P, rs, i, j)) dq -= du_q(r2, q, rn2, o.w & 0xff);
       }
     }
   }
@@ -1866,8 +1871,6 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
       const double* rowU = sU + 6 * ti * nT;
       const double rc2 = T.rc2;
       const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
-      int rgrid[3] = {0, 0, 0};
-      if constexpr ((FL & F_DU) != 0) ref_grid(P, rs, rgrid);
       for (int k = sub; k < nn; k += G) {
         const int j = __ldg(nb + k);
         const double4 o = P.d4[cur][j];
@@ -1898,7 +1901,7 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
           const double nx = dx * rs.scale[0], ny = dy * rs.scale[1], nz = dz * rs.scale[2];
           const double rn2 = nx * nx + ny * ny + nz * nz;
           const double u0 = r2 < rc2 ? pair_pot<double>(rowU + 6 * tj, sqrt(r2)) : 0.0;
-          const double u1 = (rn2 < rc2 && (r2 < rc2 || ref_cells_adjacent(P, i, j, rgrid)))
+          const double u1 = (rn2 < rc2 && (r2 < rc2 || ref_cells_adjacent(P, rs, i, j)))
                                 ? pair_pot<double>(rowU + 6 * tj, sqrt(rn2)) : 0.0;
           dU += 0.5 * (u0 - u1);
         }
@@ -2268,7 +2271,7 @@ __global__ void k_mc(DevPtrs P) {
       shift = fmax(shift, fabs(rs.scale[d] - 1.0) * P.tab->list_cut);
       rs.box[d] = rs.trial_box[d];
     }
-    derive_box(rs, rp.cell_cap, P.tab->list_cut);
+    derive_box(rs, rp.cell_cap, P.tab->list_cut, P.tab->rc);
     rs.accept = 1;
     rs.n_accept++;
     P.accept_log[(size_t)trial * P.n_rep + r] = 1;
