@@ -1791,23 +1791,37 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
       rounds = 0;
     }
   }
-  for (; k < nn; k += G) {
-    const int j = __ldg(nb + k);
-    const uint4 o = P.m4[cur][j];
-    const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
-    const float r2 = dist2(dx, dy, dz);
-    if constexpr ((FL & F_DU) != 0) {
-      const float q = dscale(dx, dy, dz);
-      const float rn2 = __fadd_rn(r2, q);
-      if (j > i && (r2 < rc2 || rn2 < rc2)) {
-        dq += du_q(r2, q, rn2, o.w & 0xff);
-        entered = entered || !(r2 < rc2);
-      }
+  if (k < nn) {
+    // the last entries (fewer than kGather): their gathers issued together,
+    // then the terms in list order (an int32 sum holds at most 31 terms here)
+    uint4 og[kGather - 1];
+    int jg[kGather - 1];
+#pragma unroll
+    for (int u = 0; u < kGather - 1; ++u) {
+      const bool ok = k + u * G < nn;
+      jg[u] = ok ? __ldg(nb + k + u * G) : -1;
+      og[u] = P.m4[cur][ok ? jg[u] : i];
     }
-    if constexpr ((FL & F_ENERGY) == 0) {
-      pair_force_q(dx, dy, dz, r2, o.w & 0xff);
-    } else {
-      if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
+#pragma unroll
+    for (int u = 0; u < kGather - 1; ++u) {
+      if (jg[u] < 0) break;
+      const int j = jg[u];
+      const uint4 o = og[u];
+      const float dx = frac_delta(me.x, o.x, s0), dy = frac_delta(me.y, o.y, s1), dz = frac_delta(me.z, o.z, s2);
+      const float r2 = dist2(dx, dy, dz);
+      if constexpr ((FL & F_DU) != 0) {
+        const float q = dscale(dx, dy, dz);
+        const float rn2 = __fadd_rn(r2, q);
+        if (j > i && (r2 < rc2 || rn2 < rc2)) {
+          dq += du_q(r2, q, rn2, o.w & 0xff);
+          entered = entered || !(r2 < rc2);
+        }
+      }
+      if constexpr ((FL & F_ENERGY) == 0) {
+        pair_force_q(dx, dy, dz, r2, o.w & 0xff);
+      } else {
+        if (r2 < rc2) eacc += pair_pot<float>(rowU + 6 * (o.w & 0xff), sqrtf(r2));
+      }
     }
   }
   qx += ax;
