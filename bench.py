@@ -68,7 +68,7 @@ ISSUE_PER_SM_CLK = 4  # warp instructions issued per SM and clock (four schedule
 # the per-kernel table are in profiles/step_traffic_bilayer60k.md).  Traffic
 # is a named constant because ncu cannot run inside the timed region.
 STEP_PROFILE = {
-    "bilayer20k": {"dram_bytes_per_bead_step": 819.0, "warp_inst_per_bead_step": 622.0,
+    "bilayer20k": {"dram_bytes_per_bead_step": 773.0, "warp_inst_per_bead_step": 620.0,
                    "source": "profiles/step_traffic_bilayer60k.md (ncu, cold caches: an upper bound on the bench's "
                              "L2-resident DRAM traffic)"},
 }
