@@ -62,15 +62,21 @@ STEP_MD = 8 * PERIOD  # MD steps per bench step
 SMS = 152          # GB300 streaming multiprocessors
 ISSUE_PER_SM_CLK = 4  # warp instructions issued per SM and clock (four schedulers)
 # DRAM bytes and warp instructions per bead and MD step of the mixed step,
-# summed over every kernel of the step with its launches per MD step, from one
-# ncu capture of the workload (metrics dram__bytes_read.sum,
-# dram__bytes_write.sum, smsp__inst_executed.sum per kernel; the command and
-# the per-kernel table are in profiles/step_traffic_bilayer60k.md).  Traffic
-# is a named constant because ncu cannot run inside the timed region.
+# summed over every kernel of the step with its launches per MD step, from ncu
+# captures of the workload (metrics dram__bytes_read.sum, dram__bytes_write.sum,
+# smsp__inst_executed.sum per kernel).  "warm": one pass per launch with the
+# caches as the previous kernels left them (--cache-control none), the traffic
+# of the bench's L2-resident loop; "cold": every launch after an L2 flush, each
+# kernel's whole working set from DRAM (an upper bound).  The commands and the
+# per-kernel tables are in profiles/step_traffic_warm_bilayer60k.md and
+# profiles/step_traffic_bilayer60k.md.  Traffic is a named constant because ncu
+# cannot run inside the timed region.
 STEP_PROFILE = {
-    "bilayer20k": {"dram_bytes_per_bead_step": 773.0, "warp_inst_per_bead_step": 620.0,
-                   "source": "profiles/step_traffic_bilayer60k.md (ncu, cold caches: an upper bound on the bench's "
-                             "L2-resident DRAM traffic)"},
+    "bilayer20k": {"dram_bytes_per_bead_step": 61.1, "dram_bytes_per_bead_step_cold": 773.0,
+                   "warp_inst_per_bead_step": 620.0,
+                   "source": "profiles/step_traffic_warm_bilayer60k.md (ncu --cache-control none: the bench's "
+                             "L2-resident loop) and profiles/step_traffic_bilayer60k.md (ncu, caches flushed "
+                             "per launch: an upper bound; instructions)"},
 }
 
 
@@ -567,7 +573,9 @@ def main():
     prof = STEP_PROFILE.get(args.workload)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": prof["dram_bytes_per_bead_step"] * n if prof else None,
-                "traffic_per": "MD step, every kernel of the step (DRAM read + write)",
+                "traffic_cold": prof["dram_bytes_per_bead_step_cold"] * n if prof else None,
+                "traffic_per": "MD step, every kernel of the step (DRAM read + write); traffic with the caches "
+                               "as the step leaves them, traffic_cold with L2 flushed before every launch",
                 "alg_bytes_per_bead_step": ALG_BYTES_PER_BEAD_STEP, "alg_bytes_per_md_step": ALG_BYTES_PER_BEAD_STEP * n,
                 "kernel": "the whole MD step (every kernel, list builds and barostat passes included)",
                 "peak_source": f"{peak_kind} hbm_gbs"}

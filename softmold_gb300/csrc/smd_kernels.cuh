@@ -1754,14 +1754,26 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
   bool entered = false;  // a pair beyond rc that the scale brings within rc
   int k = sub;
   int rounds = 0;
-  // kGather independent gathers in flight per lane
-  for (; k + (kGather - 1) * G < nn; k += kGather * G) {
+  // kGather independent gathers in flight per lane; the next batch's list
+  // entries are loaded one batch ahead, so a gather waits only on itself
+  int jn[kGather];
+  bool more = k + (kGather - 1) * G < nn;
+  if (more) {
+#pragma unroll
+    for (int u = 0; u < kGather; ++u) jn[u] = __ldg(nb + k + u * G);
+  }
+  for (; more; k += kGather * G) {
     uint4 og[kGather];
     int jg[kGather];
 #pragma unroll
     for (int u = 0; u < kGather; ++u) {
-      jg[u] = __ldg(nb + k + u * G);
+      jg[u] = jn[u];
       og[u] = P.m4[cur][jg[u]];
+    }
+    more = k + (2 * kGather - 1) * G < nn;
+    if (more) {
+#pragma unroll
+      for (int u = 0; u < kGather; ++u) jn[u] = __ldg(nb + k + (kGather + u) * G);
     }
 #pragma unroll
     for (int u = 0; u < kGather; ++u) {
