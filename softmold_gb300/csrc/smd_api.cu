@@ -309,7 +309,8 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
   }
   const int gl = h->grid_lanes();
   if constexpr ((FL & F_DU) != 0) {  // the reference-grid cells the size-change pass asks about
-    SMD_LAUNCH(h, k_ref_cells<<<h->grid(), kBlock, 0, h->stream>>>(P));
+    // (and, in the loop's barostat step, the replicas' trial)
+    SMD_LAUNCH(h, k_ref_cells<<<h->grid(), kBlock, 0, h->stream>>>(P, (FL & F_STOP) != 0 ? 1 : 0));
   }
   if (h->mixed) {
     if constexpr (FL == 0 || FL == (F_STOP | F_DU)) {  // the loop's pair passes follow the tuner
@@ -1273,8 +1274,7 @@ int capture_period(smd_system* h, int cur0) {
       const bool last = (k == G - 1);
       const StepEnd se{last ? 0ull : (unsigned long long)cond[k + 1], last ? 0 : 1, 1, 0, 0};
       if (last && h->barostat) {
-        SMD_LAUNCH(h, k_trial<<<(h->n_rep + 63) / 64, 64, 0, st>>>(P));
-        if (int r = launch_step<F_STOP | F_DU>(h)) return r;
+        if (int r = launch_step<F_STOP | F_DU>(h)) return r;  // the trial is drawn in its first kernel
         SMD_LAUNCH(h, k_mc<<<(h->n_rep + 63) / 64, 64, 0, st>>>(P));
         if (int r = launch_finish(h, 2, 1, StepEnd{0, 0, 1, 1, 0})) return r;
       } else {
@@ -1460,7 +1460,6 @@ int smd_advance(smd_system* h, int steps, int flags) {
       }
       if (trial) {
         h->trials_used++;
-        SMD_LAUNCH(h, k_trial<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P));
         rc = ext ? launch_step<F_STOP | F_DU | F_EXTNOISE>(h) : launch_step<F_STOP | F_DU>(h);
       } else {
         rc = ext ? launch_step<F_STOP | F_EXTNOISE>(h) : launch_step<F_STOP>(h);

@@ -5,7 +5,7 @@
 //   k_force<MIXED>                         non-bonded forces, G lanes per bead
 //   k_integ<MIXED>                         CHAIN + Langevin + both half-kicks + drift
 // and on barostat steps
-//   k_trial, k_force<DU>, k_integ<STOP|DU>, k_mc, k_finish.
+//   k_ref_cells (with the trial), k_force<DU>, k_integ<STOP|DU>, k_mc, k_finish.
 #pragma once
 
 #include "smd_device.cuh"
@@ -1671,8 +1671,14 @@ __device__ __forceinline__ int ref_cell_coord(double x, double cs, float inv_cs,
   const int c = (int)q;
   return c >= n ? n - 1 : (c < 0 ? 0 : c);
 }
-__global__ void __launch_bounds__(kBlock) k_ref_cells(DevPtrs P) {
+__device__ __forceinline__ void trial_replica(const DevPtrs& P, int r);
+
+// trial = 1: also the barostat trial of every replica (trial box, scale
+// factors and cleared size-change sums, one thread per replica), so that the
+// barostat step launches one kernel for both; the cells do not depend on it.
+__global__ void __launch_bounds__(kBlock) k_ref_cells(DevPtrs P, int trial) {
   const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (trial && i < P.n_rep) trial_replica(P, i);
   if (i >= P.n) return;
   const RepState& rs = P.rs[rep_of(P, i)];
   const double x[3] = {P.x[i], P.y[i], P.z[i]};
@@ -2250,11 +2256,9 @@ __global__ void __launch_bounds__(kBeadBlock) k_integ(DevPtrs P, int cur, StepEn
   }
 }
 
-// Barostat trial box for every replica (MD.cpp:593-611).
-__global__ void k_trial(DevPtrs P) {
+// Barostat trial box of replica r (MD.cpp:593-611), drawn by k_ref_cells.
+__device__ __forceinline__ void trial_replica(const DevPtrs& P, int r) {
   const int trial = P.g->trial_slot;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= P.n_rep) return;
   RepState& rs = P.rs[r];
   rs.dU_pair = 0.0;
   rs.dU_bond = 0.0;
@@ -2287,11 +2291,12 @@ __global__ void k_mc(DevPtrs P) {
   if (rp.dlxy == 0) return;
   double dPot = rep_dU(rs);
   if (rp.tension != 0) dPot += rp.tension * ((rs.trial_box[0] * rs.trial_box[1]) - (rs.box[0] * rs.box[1]));
-  const double D = exp(dPot / rp.kT);
   const double u2 = P.trial_u[((size_t)trial * P.n_rep + r) * 2 + 1];
   rs.last_dU = dPot;
   rs.n_trial++;
-  if (D >= u2 || -dPot <= 0) {
+  // MD.cpp's test D >= u2 || -dPot <= 0 with D = exp(dPot / kT); the
+  // exponential is needed only when the second clause fails
+  if (-dPot <= 0 || exp(dPot / rp.kT) >= u2) {
     double shift = 0.0;  // pair distances within rc + skin change by at most this
     for (int d = 0; d < 3; ++d) {
       shift = fmax(shift, fabs(rs.scale[d] - 1.0) * P.tab->list_cut);
