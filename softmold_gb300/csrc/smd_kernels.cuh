@@ -1760,27 +1760,12 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
   bool entered = false;  // a pair beyond rc that the scale brings within rc
   int k = sub;
   int rounds = 0;
-  // kGather independent gathers in flight per lane; the next batch's list
-  // entries are loaded one batch ahead, so a gather waits only on itself
-  int jn[kGather];
-  bool more = k + (kGather - 1) * G < nn;
-  if (more) {
-#pragma unroll
-    for (int u = 0; u < kGather; ++u) jn[u] = __ldg(nb + k + u * G);
-  }
-  for (; more; k += kGather * G) {
-    uint4 og[kGather];
-    int jg[kGather];
-#pragma unroll
-    for (int u = 0; u < kGather; ++u) {
-      jg[u] = jn[u];
-      og[u] = P.m4[cur][jg[u]];
-    }
-    more = k + (2 * kGather - 1) * G < nn;
-    if (more) {
-#pragma unroll
-      for (int u = 0; u < kGather; ++u) jn[u] = __ldg(nb + k + (kGather + u) * G);
-    }
+  // kGather independent gathers in flight per lane; batch() takes the terms
+  // of one batch in list order.  The force pass loads the next batch's list
+  // entries one batch ahead, so a gather waits only on itself; the
+  // size-change pass does not (the registers this takes would cost it a CTA
+  // per SM and spill)
+  auto batch = [&](const uint4 (&og)[kGather], const int (&jg)[kGather]) {
 #pragma unroll
     for (int u = 0; u < kGather; ++u) {
       const uint4 o = og[u];
@@ -1807,6 +1792,40 @@ __device__ __forceinline__ void pair_sum_q(const DevPtrs& P, int cur, int i, int
       qz += az;
       ax = ay = az = 0;
       rounds = 0;
+    }
+  };
+  if constexpr ((FL & F_DU) == 0) {
+    int jn[kGather];
+    bool more = k + (kGather - 1) * G < nn;
+    if (more) {
+#pragma unroll
+      for (int u = 0; u < kGather; ++u) jn[u] = __ldg(nb + k + u * G);
+    }
+    for (; more; k += kGather * G) {
+      uint4 og[kGather];
+      int jg[kGather];
+#pragma unroll
+      for (int u = 0; u < kGather; ++u) {
+        jg[u] = jn[u];
+        og[u] = P.m4[cur][jg[u]];
+      }
+      more = k + (2 * kGather - 1) * G < nn;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < kGather; ++u) jn[u] = __ldg(nb + k + (kGather + u) * G);
+      }
+      batch(og, jg);
+    }
+  } else {
+    for (; k + (kGather - 1) * G < nn; k += kGather * G) {
+      uint4 og[kGather];
+      int jg[kGather];
+#pragma unroll
+      for (int u = 0; u < kGather; ++u) {
+        jg[u] = __ldg(nb + k + u * G);
+        og[u] = P.m4[cur][jg[u]];
+      }
+      batch(og, jg);
     }
   }
   if (k < nn) {
