@@ -1998,12 +1998,12 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
 // start-up, force-only and energy-only variants.
 // One bead's part of the per-bead pass: bonded terms, the total force, the
 // Langevin term and the velocity-Verlet updates, the next mirror and the
-// displacement from the list build.  q is the bead's pair force in fixed
-// point (mixed form; the plain form reads P.fp), fs its sphere force; the
-// energy and size-change sums and the displacement accumulate into the
-// caller's variables.
+// displacement from the list build.  The bead's pair force (P.fq in fixed
+// point in the mixed form, P.fp in the plain form) is read after pdl_wait;
+// fs is its sphere force; the energy and size-change sums and the
+// displacement accumulate into the caller's variables.
 template <bool MIXED, int FL>
-__device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int r, long long it, const long long q[3],
+__device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int r, long long it,
                                            const Vec3<double>& fs, double& dU_bond, double& e_bond, double& e_kin,
                                            float& vmax) {
   const Tables& T = *P.tab;
@@ -2117,23 +2117,31 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
     const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
     e_kin = (vx * vx + vy * vy + vz * vz) / 2.0;
   } else {
-    double F[3];
-    if constexpr (MIXED) {
-      F[0] = (double)q[0] * T.inv_fscale + (double)fb.x;
-      F[1] = (double)q[1] * T.inv_fscale + (double)fb.y;
-      F[2] = (double)q[2] * T.inv_fscale + (double)fb.z;
-    } else {
-      F[0] = P.fp[i] + fb.x;
-      F[1] = P.fp[i + P.n] + fb.y;
-      F[2] = P.fp[i + 2 * P.n] + fb.z;
-    }
-    if (P.n_sph > 0) {
-      F[0] += fs.x;
-      F[1] += fs.y;
-      F[2] += fs.z;
-    }
+    // The pair pass's forces are read only from here on, after the wait for
+    // that kernel (this one is its programmatic dependent): the bonded
+    // terms, the noise and the state loads above and below run while the
+    // pair pass's last CTAs still do.
+    auto total_force = [&](double F[3]) {
+      pdl_wait();
+      if constexpr (MIXED) {
+        F[0] = (double)P.fq[i] * T.inv_fscale + (double)fb.x;
+        F[1] = (double)P.fq[i + P.n] * T.inv_fscale + (double)fb.y;
+        F[2] = (double)P.fq[i + 2 * P.n] * T.inv_fscale + (double)fb.z;
+      } else {
+        F[0] = P.fp[i] + fb.x;
+        F[1] = P.fp[i + P.n] + fb.y;
+        F[2] = P.fp[i + 2 * P.n] + fb.z;
+      }
+      if (P.n_sph > 0) {
+        F[0] += fs.x;
+        F[1] += fs.y;
+        F[2] += fs.z;
+      }
+    };
     if constexpr ((FL & F_FORCES) != 0) {
       if (!sphere) {
+        double F[3];
+        total_force(F);
         const int o = P.orig[i];
         P.force_out[3 * o] = F[0];
         P.force_out[3 * o + 1] = F[1];
@@ -2142,6 +2150,12 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
     } else if (!sphere) {
       const int o = P.orig[i];
       double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+      double x0[3] = {0.0, 0.0, 0.0};
+      if constexpr ((FL & (F_STOP | F_INIT)) == 0) {  // the drift's positions, loaded before the wait
+        x0[0] = P.x[i];
+        x0[1] = P.y[i];
+        x0[2] = P.z[i];
+      }
       double a[3];
       if constexpr (MIXED && (FL & F_EXTNOISE) == 0) {
         // CHAIN force and noise summed in FP32 (both force terms of the
@@ -2155,6 +2169,8 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
           e[1] += fs.y;
           e[2] += fs.z;
         }
+        pdl_wait();
+        const long long q[3] = {P.fq[i], P.fq[i + P.n], P.fq[i + 2 * P.n]};
         for (int d = 0; d < 3; ++d)
           a[d] = fma(-rp.gamma, v[d], fma((double)q[d], T.inv_fscale, e[d]));
       } else {
@@ -2164,6 +2180,8 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
         } else {
           langevin_noise(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31, noise);
         }
+        double F[3];
+        total_force(F);
         for (int d = 0; d < 3; ++d) a[d] = fma(-rp.gamma, v[d], F[d]) + noise[d];
       }
       if constexpr ((FL & (F_STOP | F_INIT)) != 0) {
@@ -2179,7 +2197,7 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
           }
         }
       } else {
-        double x[3] = {P.x[i], P.y[i], P.z[i]};
+        double x[3] = {x0[0], x0[1], x0[2]};
         if (ti != 0) {
           if constexpr (MIXED) {
             // second() of this step and first() of the next, rounded as the
@@ -2226,7 +2244,8 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
 
 template <bool MIXED, int FL>
 __global__ void __launch_bounds__(kBeadBlock) k_integ(DevPtrs P, int cur, StepEnd se) {
-  pdl_wait();  // the pair pass's forces
+  // No wait here: integ_bead waits for the pair pass right before it reads
+  // the pair forces, and every thread waits before the step's sums.
   const long long it = P.g->it;
   const int i = blockIdx.x * kBeadBlock + threadIdx.x;
   const bool active = i < P.n;
@@ -2240,15 +2259,8 @@ __global__ void __launch_bounds__(kBeadBlock) k_integ(DevPtrs P, int cur, StepEn
     if (P.n_sph > 0) sphere_terms<MIXED, FL>(P, cur, i, active, fs, e_sph, du_sph);
   }
   dU_bond += du_sph;
-  if (active) {
-    long long q[3] = {0, 0, 0};
-    if constexpr (MIXED && (FL & F_ENERGY) == 0) {
-      q[0] = P.fq[i];
-      q[1] = P.fq[i + P.n];
-      q[2] = P.fq[i + 2 * P.n];
-    }
-    integ_bead<MIXED, FL>(P, cur, i, r, it, q, fs, dU_bond, e_bond, e_kin, vmax);
-  }
+  if (active) integ_bead<MIXED, FL>(P, cur, i, r, it, fs, dU_bond, e_bond, e_kin, vmax);
+  pdl_wait();  // returns at once where integ_bead has waited
   if constexpr ((FL & F_DU) != 0) {
     if constexpr (MIXED) warp_atomic_add_q(__double2ll_rn(dU_bond * 4294967296.0), &P.rs[r].dUq_bond, r);
     else warp_atomic_add(dU_bond, &P.rs[r].dU_bond, r);
