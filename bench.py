@@ -72,8 +72,8 @@ ISSUE_PER_SM_CLK = 4  # warp instructions issued per SM and clock (four schedule
 # profiles/step_traffic_bilayer60k.md.  Traffic is a named constant because ncu
 # cannot run inside the timed region.
 STEP_PROFILE = {
-    "bilayer20k": {"dram_bytes_per_bead_step": 52.0, "dram_bytes_per_bead_step_cold": 773.0,
-                   "warp_inst_per_bead_step": 617.0,
+    "bilayer20k": {"dram_bytes_per_bead_step": 61.0, "dram_bytes_per_bead_step_cold": 773.0,
+                   "warp_inst_per_bead_step": 619.0,
                    "source": "profiles/step_traffic_warm_bilayer60k.md (ncu --cache-control none: the bench's "
                              "L2-resident loop; traffic and instructions) and profiles/step_traffic_bilayer60k.md "
                              "(ncu, caches flushed per launch: an upper bound on traffic)"},

@@ -2,8 +2,12 @@
 //
 // One MD loop iteration (MD.cpp:335-729) in the steady state is
 //   [k_bin, k_scan_*, k_reorder, k_nbr]   only when the Verlet list is stale
-//   k_force<MIXED>                         non-bonded forces, G lanes per bead
-//   k_integ<MIXED>                         CHAIN + Langevin + both half-kicks + drift
+//   k_pre                                  CHAIN + Langevin terms (mixed form,
+//                                          systems without spheres or fields)
+//   k_force<MIXED>                         non-bonded forces, G lanes per bead,
+//                                          beside k_pre
+//   k_integ<MIXED>                         both half-kicks + drift (and the CHAIN
+//                                          + Langevin terms where k_pre does not run)
 // and on barostat steps
 //   k_ref_cells (with the trial), k_force<DU>, k_integ<STOP|DU>, k_mc, k_finish.
 #pragma once
