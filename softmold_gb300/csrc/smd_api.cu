@@ -219,6 +219,14 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t
 
 __global__ void k_set_rebuild(Global* g, int v) { g->rebuild = v; }
 
+// Clears every replica's energy sums before an energy pass.
+__global__ void k_clear_energy(DevPtrs P) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= P.n_rep) return;
+  RepState& rs = P.rs[r];
+  rs.e_pair = rs.e_bond = rs.e_kin = rs.e_sphere = 0.0;
+}
+
 __global__ void k_set_counters(Global* g, long long it, int set_it, int slot, int set_slot) {
   if (set_it) g->it = it;
   if (set_slot) g->trial_slot = slot;
@@ -1097,8 +1105,7 @@ int smd_set_state(smd_system* h, const double* pos, const double* vel) {
       if (int rc = grow_list(h, need)) return rc;
     }
   }
-  SMD_CUDA(cudaStreamSynchronize(h->stream));
-  return read_error(h);
+  return read_error(h);  // synchronises the stream
 }
 
 int smd_get_box(smd_system* h, int replica, double box[3]) {
@@ -1147,21 +1154,19 @@ int smd_compute_energy(smd_system* h, smd_energy* e) {
   if (!h || !e) return fail(1, "bad arguments");
   int rc = rebuild_if_needed(h, true);
   if (rc) return rc;
+  // the energy sums are cleared on the device: no host round trip before the pass
+  SMD_LAUNCH(h, k_clear_energy<<<(h->n_rep + 63) / 64, 64, 0, h->stream>>>(h->P));
+  if ((rc = launch_step<F_ENERGY>(h))) return rc;
   std::vector<RepState> rs(h->n_rep);
   SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaStreamSynchronize(h->stream));
-  for (auto& s : rs) s.e_pair = s.e_bond = s.e_kin = s.e_sphere = 0;
-  SMD_CUDA(cudaMemcpyAsync(h->P.rs, rs.data(), h->n_rep * sizeof(RepState), cudaMemcpyHostToDevice, h->stream));
-  if ((rc = launch_step<F_ENERGY>(h))) return rc;
-  SMD_CUDA(cudaMemcpyAsync(rs.data(), h->P.rs, h->n_rep * sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
-  SMD_CUDA(cudaStreamSynchronize(h->stream));
+  if ((rc = read_error(h))) return rc;  // its synchronisation also completes the copy above
   for (int r = 0; r < h->n_rep; ++r) {
     e[r].pair = rs[r].e_pair;
     e[r].bonded = rs[r].e_bond;
     e[r].sphere = rs[r].e_sphere;
     e[r].kinetic = rs[r].e_kin;
   }
-  return read_error(h);
+  return 0;
 }
 
 int smd_compute_dU(smd_system* h, const double scale[3], double* dU) {
