@@ -72,8 +72,8 @@ ISSUE_PER_SM_CLK = 4  # warp instructions issued per SM and clock (four schedule
 # profiles/step_traffic_bilayer60k.md.  Traffic is a named constant because ncu
 # cannot run inside the timed region.
 STEP_PROFILE = {
-    "bilayer20k": {"dram_bytes_per_bead_step": 61.0, "dram_bytes_per_bead_step_cold": 773.0,
-                   "warp_inst_per_bead_step": 619.0,
+    "bilayer20k": {"dram_bytes_per_bead_step": 54.0, "dram_bytes_per_bead_step_cold": 773.0,
+                   "warp_inst_per_bead_step": 618.0,
                    "source": "profiles/step_traffic_warm_bilayer60k.md (ncu --cache-control none: the bench's "
                              "L2-resident loop; traffic and instructions) and profiles/step_traffic_bilayer60k.md "
                              "(ncu, caches flushed per launch: an upper bound on traffic)"},
@@ -582,7 +582,7 @@ def main():
     kernels = None
     if kernel_launches:
         avg_us = 1e3 * kernel_ms / kernel_launches
-        kernels = {"k_pre + k_force + k_integ": {
+        kernels = {"k_force + k_integ": {
             "avg_us_per_md_step": avg_us, "achieved_gbs": ALG_BYTES_PER_BEAD_STEP * n / (avg_us * 1e3),
             "frac": ALG_BYTES_PER_BEAD_STEP * n / (avg_us * 1e3) / peak, "launch_pairs": kernel_launches,
             "share_of_step": avg_us / us_md_step}}

@@ -320,18 +320,7 @@ int launch_step(smd_system* h, StepEnd se = StepEnd{0, 0, 1, 0, 0}) {
     // (and, in the loop's barostat step, the replicas' trial)
     SMD_LAUNCH(h, k_ref_cells<<<h->grid(), kBlock, 0, h->stream>>>(P, (FL & F_STOP) != 0 ? 1 : 0));
   }
-  if (FL == 0 && h->mixed && !h->has_fields && h->n_sph == 0) {
-    // the loop step in three kernels: k_pre (bonded force + noise), the pair
-    // pass as its programmatic dependent (it runs beside k_pre and completes
-    // after it), and the integrator as the pair pass's dependent
-    SMD_LAUNCH(h, k_pre<<<h->bead_grid(), kBeadBlock, 0, h->stream>>>(P, h->cur));
-    switch (h->tune.lanes) {
-      case 4: SMD_PDL(h, (k_force<true, 0, 4>), h->grid_lanes(4), kBlock, h->stream, P, h->cur); break;
-      case 16: SMD_PDL(h, (k_force<true, 0, 16>), h->grid_lanes(16), kBlock, h->stream, P, h->cur); break;
-      default: SMD_PDL(h, (k_force<true, 0, kLanes>), gl, kBlock, h->stream, P, h->cur);
-    }
-    SMD_PDL_INTEG(h, (k_integ<true, F_PRE>));
-  } else if (h->mixed) {
+  if (h->mixed) {
     if constexpr (FL == 0 || FL == (F_STOP | F_DU)) {  // the loop's pair passes follow the tuner
       switch (h->tune.lanes) {
         case 4:
@@ -877,7 +866,6 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     if ((rc = h->alloc(q, total))) return rc;
   if (h->mixed) {
     if ((rc = h->alloc(&P.fq, 3 * (size_t)total))) return rc;
-    if ((rc = h->alloc(&P.pre, (size_t)total))) return rc;
   } else {
     if ((rc = h->alloc(&P.fp, 3 * (size_t)total))) return rc;
   }

@@ -222,7 +222,6 @@ struct DevPtrs {
   int* occ;          // occupied list cells of the last build (count in Global::n_occ)
   int *nbr, *nnbr;
   long long* fq;     // MIXED pair force, fixed point, 3*n (x | y | z)
-  float4* pre;       // MIXED loop steps: bonded force + Langevin noise per bead (FP32), from k_pre
   double* fp;        // PLAIN pair force, 3*n
   RepParams* rp;
   RepState* rs;

@@ -2,12 +2,8 @@
 //
 // One MD loop iteration (MD.cpp:335-729) in the steady state is
 //   [k_bin, k_scan_*, k_reorder, k_nbr]   only when the Verlet list is stale
-//   k_pre                                  CHAIN + Langevin terms (mixed form,
-//                                          systems without spheres or fields)
-//   k_force<MIXED>                         non-bonded forces, G lanes per bead,
-//                                          beside k_pre
-//   k_integ<MIXED>                         both half-kicks + drift (and the CHAIN
-//                                          + Langevin terms where k_pre does not run)
+//   k_force<MIXED>                         non-bonded forces, G lanes per bead
+//   k_integ<MIXED>                         CHAIN + Langevin + both half-kicks + drift
 // and on barostat steps
 //   k_ref_cells (with the trial), k_force<DU>, k_integ<STOP|DU>, k_mc, k_finish.
 #pragma once
@@ -24,9 +20,8 @@ enum StepFlags {
   F_FORCES = 16,    // conservative forces only, written to P.force_out (file order)
   F_PAIRONLY = 32,  // with F_FORCES: non-bonded part only
   F_ENERGY = 64,    // energies only (pair, bonded, kinetic) into RepState
-  F_FIELDS = 128,   // the system has external-field terms (their out-of-line
+  F_FIELDS = 128    // the system has external-field terms (their out-of-line
                     // evaluation is compiled in only with this flag)
-  F_PRE = 256       // loop step whose bonded force + noise k_pre has summed into P.pre
 };
 
 // ------------------------------------------------------------ last block
@@ -1993,10 +1988,6 @@ __global__ void __launch_bounds__(kBlock) k_force(DevPtrs P, int cur) {
     else warp_atomic_add(dU, &P.rs[r].dU_pair, r);
   }
   if constexpr ((FL & F_ENERGY) != 0) warp_atomic_add(ep, &P.rs[r].e_pair, r);
-  // Launched as k_pre's programmatic dependent the pass runs beside k_pre
-  // (it reads nothing k_pre writes) and completes only after it, so the
-  // integrator's wait for this kernel also covers k_pre.  Otherwise a no-op.
-  if constexpr (FL == 0) pdl_wait();
 }
 
 // Per-bead pass after k_force: CHAIN terms, the total force, the Langevin
@@ -2027,9 +2018,8 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
   const int ci = P.cinfo[i];
   const bool sphere = (ci < 0) && (ci & 0x40000000);  // integrated by k_sphere
   // bonded forces: one function for every step variant, so stopped and
-  // running steps round them alike (k_pre calls it for F_PRE steps)
-  if constexpr ((FL & (F_PAIRONLY | F_ENERGY | F_PRE)) == 0)
-    fb = bonded_force<MIXED, (FL & F_FIELDS) != 0>(P, cur, i, ci, box, rs);
+  // running steps round them alike
+  if constexpr ((FL & (F_PAIRONLY | F_ENERGY)) == 0) fb = bonded_force<MIXED, (FL & F_FIELDS) != 0>(P, cur, i, ci, box, rs);
   if ((FL & F_PAIRONLY) == 0 && (FL & (F_DU | F_ENERGY)) != 0 && ci < 0 && !(ci & 0x40000000)) {
     const int p = ci & 0xfff, len = (ci >> 12) & 0xfff, set = (ci >> 24) & 0x1f;
     // the chain's difference vectors in R (exact from the fractional
@@ -2171,26 +2161,15 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
         // CHAIN force and noise summed in FP32 (both force terms of the
         // mixed form), the pair force exact from its fixed-point sum:
         // a = -gamma v + (q 2^-k + (f_chain + sigma psi))
-        double e[3];
-        if constexpr ((FL & F_PRE) == 0) {
-          float nf[3];
-          langevin_noise_f(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31f, nf);
-          e[0] = (double)__fadd_rn(fb.x, nf[0]);
-          e[1] = (double)__fadd_rn(fb.y, nf[1]);
-          e[2] = (double)__fadd_rn(fb.z, nf[2]);
-          if (P.n_sph > 0) {
-            e[0] += fs.x;
-            e[1] += fs.y;
-            e[2] += fs.z;
-          }
-          pdl_wait();
-        } else {  // summed by k_pre, which the wait for the pair pass covers
-          pdl_wait();
-          const float4 pr = P.pre[i];
-          e[0] = (double)pr.x;
-          e[1] = (double)pr.y;
-          e[2] = (double)pr.z;
+        float nf[3];
+        langevin_noise_f(rp.seed, o - rp.bead_begin, it, (FL & F_INIT) ? 1 : 0, rp.sig31f, nf);
+        double e[3] = {(double)(fb.x + nf[0]), (double)(fb.y + nf[1]), (double)(fb.z + nf[2])};
+        if (P.n_sph > 0) {
+          e[0] += fs.x;
+          e[1] += fs.y;
+          e[2] += fs.z;
         }
+        pdl_wait();
         const long long q[3] = {P.fq[i], P.fq[i + P.n], P.fq[i + 2 * P.n]};
         for (int d = 0; d < 3; ++d)
           a[d] = fma(-rp.gamma, v[d], fma((double)q[d], T.inv_fscale, e[d]));
@@ -2261,27 +2240,6 @@ __device__ __forceinline__ void integ_bead(const DevPtrs& P, int cur, int i, int
       }
     }
   }
-}
-
-// The force-independent part of a mixed loop step's per-bead pass: the
-// bonded force and the Langevin term sigma psi, summed in FP32 as k_integ
-// sums them (no BEAD or NANOCORE spheres, no external-field terms).  The
-// pair pass is launched as this kernel's programmatic dependent and runs
-// beside it; k_integ<F_PRE> reads the sums after its wait for the pair pass.
-__global__ void __launch_bounds__(kBeadBlock) k_pre(DevPtrs P, int cur) {
-  pdl_trigger();  // the pair pass does not read what this kernel writes
-  const int i = blockIdx.x * kBeadBlock + threadIdx.x;
-  if (i >= P.n) return;
-  const long long it = P.g->it;
-  const int r = rep_of(P, i);
-  const RepParams& rp = P.rp[r];
-  const RepState& rs = P.rs[r];
-  const double box[3] = {rs.box[0], rs.box[1], rs.box[2]};
-  const int ci = P.cinfo[i];
-  const Vec3<float> fb = bonded_force<true, false>(P, cur, i, ci, box, rs);
-  float nf[3];
-  langevin_noise_f(rp.seed, P.orig[i] - rp.bead_begin, it, 0, rp.sig31f, nf);
-  P.pre[i] = make_float4(__fadd_rn(fb.x, nf[0]), __fadd_rn(fb.y, nf[1]), __fadd_rn(fb.z, nf[2]), 0.f);
 }
 
 template <bool MIXED, int FL>
