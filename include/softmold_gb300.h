@@ -282,7 +282,8 @@ int smd_set_msd_groups(smd_system* h, int n_groups, const int* offsets, const in
 
 /* Runs the synthetic generators (restating generate/liposome.cpp,
  * generate/bilayer.cpp and generate/continuumSphereAndLiposome.cpp) and
- * writes <path>. */
+ * writes <path>.  An allocation that fails returns 9 (message in
+ * smd_last_error). */
 int smd_synth_vesicle(const char* path, int seed, int n_lipids, double areal_density, double box);
 int smd_synth_bilayer(const char* path, int seed, int n_lipids, double areal_density, double zsize,
                       double delta_lxy, double tension);
@@ -359,7 +360,9 @@ int smd_adjoint(smd_system* h, const smd_adjoint_spec* spec, smd_adjoint_result*
 int smd_hessian_vector(smd_system* h, const double* w, double* kw);
 
 /* Rewrites the .mpd at in_path with new positions, velocities, box and
- * initialTime into out_path (the store of MD.cpp:373-377). */
+ * initialTime into out_path (the store of MD.cpp:373-377).  A file the reader
+ * refuses returns its nonzero status, an allocation that fails 9 (message in
+ * smd_last_error). */
 int smd_mpd_update_state(const char* in_path, const char* out_path, const double* pos, const double* vel,
                          const double box[3], double time);
 
@@ -378,7 +381,9 @@ typedef struct smd_mpd_run {
  * terms, one BEAD or NANOCORE residue, external-field terms); run may be
  * NULL.  The descriptor's arrays belong to *owner until smd_mpd_free(*owner).
  * A residue type the device step does not run is refused (status 11), as is
- * a file without gamma (12). */
+ * a file without gamma (12).  The reader refuses a negative count, or one
+ * whose entries the file does not hold, before allocating for it; an
+ * allocation that fails returns 9.  Messages are in smd_last_error. */
 int smd_mpd_load(const char* path, smd_system_desc* desc, smd_mpd_run* run, void** owner);
 void smd_mpd_free(void* owner);
 

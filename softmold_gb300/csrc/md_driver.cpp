@@ -16,6 +16,7 @@
 // from MTRand(seed).rand53() for each bead's x, y, z in turn
 // (include/algorithms/langevin.h:284-331), through smd_set_noise_once, so
 // that a run can be compared with the reference's output files line by line.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -42,6 +43,15 @@ int die(const std::string& what) {
   std::cout << "Error(MD): " << what << ": " << last_error() << "\n";
   return 1;
 }
+
+// Owns the device system, so that every return releases it (smd_md_main is
+// also exported to callers that stay alive after an error).
+struct SystemGuard {
+  smd_system* h = nullptr;
+  ~SystemGuard() {
+    if (h) smd_destroy(h);
+  }
+};
 
 }  // namespace
 
@@ -70,7 +80,9 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   double tempStep = 0;
   if (S.tempStepInterval > 0) {
     tempStep = S.tempStepInterval * (S.finalTemp - S.initialTemp) / (S.finalTime - S.initialTime);
-    tempStepInt = (endInt - startInt) / int((S.finalTime - S.initialTime) / (S.tempStepInterval));
+    // no ramp step when the interval exceeds the run (the count rounds to 0)
+    const int n_ramp = int((S.finalTime - S.initialTime) / (S.tempStepInterval));
+    tempStepInt = n_ramp > 0 ? (endInt - startInt) / n_ramp : 0;
   }
   if (storeint <= 0 || measureint <= 0) {
     std::cout << "Error(MD): storeInterval and measureInterval must be at least deltaT\n";
@@ -79,8 +91,9 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
 
   smd_system_desc d;
   smd::mpd_descriptor(S, res, d);
-  smd_system* h = nullptr;
-  if (smd_create(&d, precision, &h)) return die("smd_create");
+  SystemGuard guard;
+  if (smd_create(&d, precision, &guard.h)) return die("smd_create");
+  smd_system* const h = guard.h;
 
   smd::Observables obs(name);
   const std::string frames = "frames_" + name + ".xyz";
@@ -195,8 +208,12 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
     const long got = smd_mc_log(h, 0, 0, n, f.data(), a.data());
     for (long t = 0; t < got; ++t) {
       std::vector<double>& hist = a[t] ? acc : rej;
-      hist[(size_t)((f[t] + S.deltaLXY) / interval)] += 0.5;
-      hist[(size_t)((f[t] + S.deltaLXY) / interval)] += 0.5;
+      // a trial in [-deltaLXY, deltaLXY) falls in bins 0..nIntervals-1; the
+      // clamp keeps one whose bin rounds up to the upper edge in the last bin
+      const double q = (f[t] + S.deltaLXY) / interval;
+      const size_t bin = q > 0 ? std::min((size_t)q, (size_t)nIntervals - 1) : 0;
+      hist[bin] += 0.5;
+      hist[bin] += 0.5;
     }
     std::string out;
     for (int i = 0; i < nIntervals; ++i)
@@ -219,6 +236,5 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   if (hist.size() < nb) hist.resize(nb, 0);
   for (size_t k = 0; k < nb; ++k) hist[k] += dev_hist[k];
   obs.finish();
-  smd_destroy(h);
   return 0;
 }

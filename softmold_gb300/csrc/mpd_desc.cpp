@@ -1,5 +1,6 @@
 #include "mpd_desc.h"
 
+#include <exception>
 #include <initializer_list>
 #include <memory>
 
@@ -145,11 +146,8 @@ struct LoadedMpd {
   smd::MpdSystem S;
   smd::MpdResidues r;
 };
-}  // namespace
 
-extern "C" int smd_mpd_load(const char* path, smd_system_desc* desc, smd_mpd_run* run, void** owner) {
-  if (!path || !desc || !owner) return 1;
-  *owner = nullptr;
+int load_mpd(const char* path, smd_system_desc* desc, smd_mpd_run* run, void** owner) {
   std::unique_ptr<LoadedMpd> L(new LoadedMpd);
   std::string err;
   if (int rc = smd::mpd_read_file(path, L->S, err)) {
@@ -175,6 +173,21 @@ extern "C" int smd_mpd_load(const char* path, smd_system_desc* desc, smd_mpd_run
   }
   *owner = L.release();
   return 0;
+}
+
+}  // namespace
+
+extern "C" int smd_mpd_load(const char* path, smd_system_desc* desc, smd_mpd_run* run, void** owner) {
+  if (!path || !desc || !owner) return 1;
+  *owner = nullptr;
+  // the reader refuses counts its file cannot hold; what it allocates for the
+  // rest comes back as error code 9 rather than an exception through the ABI
+  try {
+    return load_mpd(path, desc, run, owner);
+  } catch (const std::exception& e) {
+    smd::set_last_error(std::string("smd_mpd_load: ") + e.what());
+    return 9;
+  }
 }
 
 extern "C" void smd_mpd_free(void* owner) { delete static_cast<LoadedMpd*>(owner); }

@@ -49,7 +49,14 @@ struct Tokens {
     out = t[i++];
     return true;
   }
+  size_t left() const { return t.size() - i; }
 };
+
+// Bounds on counts read from the file that size products below: nTypes keeps
+// kBeadConst * nTypes^2 (a BEAD residue's constants) within an int, and
+// nBondAlloc keeps kBeadConst * nBondAlloc (a NANOCORE residue's) within one.
+constexpr int kMaxTypesRead = 4096;
+constexpr int kMaxBondAllocRead = 1 << 26;
 
 Tokens tokenize(const std::string& text) {
   Tokens tk;
@@ -121,6 +128,20 @@ int mpd_parse(const std::string& text, MpdSystem& s, std::string& err) {
     }
     return true;
   };
+  // The arrays below are sized from counts in the file.  A negative count
+  // fails at once, and one whose entries the rest of the file cannot hold
+  // fails as the missing value would, before anything is allocated for it.
+  auto room = [&](const char* what, double entries) -> bool {
+    if (entries < 0) {
+      err = std::string("Count for ") + what + " is negative!";
+      return false;
+    }
+    if (entries > (double)tk.left()) {
+      err = std::string("Value after ") + what + " is missing (end of file)";
+      return false;
+    }
+    return true;
+  };
   bool haveVel = false;
   while (tk.next(tok)) {
     auto f = lookup.find(tok);
@@ -135,7 +156,13 @@ int mpd_parse(const std::string& text, MpdSystem& s, std::string& err) {
       case CMD_INITIALTEMP: if (!read_d(name, s.initialTemp)) return 2; break;
       case CMD_FINALTEMP: if (!read_d(name, s.finalTemp)) return 2; break;
       case CMD_SEED: if (!read_i(name, s.seed)) return 2; break;
-      case CMD_NTYPES: if (!read_i(name, s.nTypes)) return 2; break;
+      case CMD_NTYPES:
+        if (!read_i(name, s.nTypes)) return 2;
+        if (s.nTypes < 0 || s.nTypes > kMaxTypesRead) {
+          err = "nTypes must be in 0.." + std::to_string(kMaxTypesRead) + "!";
+          return 3;
+        }
+        break;
       case CMD_NMOLECULES: if (!read_i(name, s.nMolecules)) return 2; break;
       case CMD_NPARTICLES: if (!read_i(name, s.nParticles)) return 2; break;
       case CMD_PERIODIC:
@@ -160,6 +187,7 @@ int mpd_parse(const std::string& text, MpdSystem& s, std::string& err) {
         }
         std::vector<double>& dst = (c == CMD_TWOBODYFCONST) ? s.twoBodyFconst : s.twoBodyUconst;
         const int n = kTwoBodyConst * s.nTypes * s.nTypes;
+        if (!room(name, n)) return 2;
         dst.assign(n, 0.0);
         for (int k = 0; k < n; ++k) if (!read_d(name, dst[k])) return 2;
         break;
@@ -169,6 +197,7 @@ int mpd_parse(const std::string& text, MpdSystem& s, std::string& err) {
           err = "nParticles was not present before positions!";
           return 3;
         }
+        if (!room(name, 4.0 * s.nParticles)) return 2;
         s.type.assign(s.nParticles, 0);
         s.pos.assign(3 * (size_t)s.nParticles, 0.0);
         for (int p = 0; p < s.nParticles; ++p) {
@@ -182,6 +211,7 @@ int mpd_parse(const std::string& text, MpdSystem& s, std::string& err) {
           err = "nParticles was not present before velocities!";
           return 3;
         }
+        if (!room(name, 3.0 * s.nParticles)) return 2;
         s.vel.assign(3 * (size_t)s.nParticles, 0.0);
         for (size_t k = 0; k < 3 * (size_t)s.nParticles; ++k) if (!read_d(name, s.vel[k])) return 2;
         haveVel = true;
@@ -208,7 +238,12 @@ int mpd_parse(const std::string& text, MpdSystem& s, std::string& err) {
               return 3;
             }
             if (!read_i(name, mol.nBondAlloc)) return 2;
+            if (mol.nBondAlloc < 0 || mol.nBondAlloc > kMaxBondAllocRead) {
+              err = "Molecule " + std::to_string(m) + ": bond count out of range!";
+              return 3;
+            }
             molecule_layout(mol.type, s.nTypes, mol.nBondAlloc, &nIdx, &nConst);
+            if (!room(name, (double)nConst + (double)nIdx * mol.nBondAlloc)) return 2;
             mol.constants.assign(nConst, 0.0);
             for (int k = 0; k < nConst; ++k) if (!read_d(name, mol.constants[k])) return 2;
             for (int b = 0; b < mol.nBondAlloc; ++b) {
@@ -233,6 +268,7 @@ int mpd_parse(const std::string& text, MpdSystem& s, std::string& err) {
           err = "nTypes was not present before gammaType!";
           return 3;
         }
+        if (!room(name, s.nTypes)) return 2;
         s.gammaType.assign(s.nTypes, 0.0);
         for (int k = 0; k < s.nTypes; ++k) if (!read_d(name, s.gammaType[k])) return 2;
         break;

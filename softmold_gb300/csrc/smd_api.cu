@@ -532,9 +532,13 @@ int validate(const smd_system_desc& d, std::string& why) {
   if (d.n <= 0) return why = "n must be positive", 1;
   if (d.n_types <= 0 || d.n_types > kMaxTypes) return why = "n_types must be in 1..8", 1;
   if (!d.pos || !d.vel || !d.type || !d.fconst || !d.uconst) return why = "null array in descriptor", 1;
-  if (!(d.cutoff > 0)) return why = "cutoff must be positive", 1;
+  if (!(d.cutoff > 0) || !std::isfinite(d.cutoff)) return why = "cutoff must be positive and finite", 1;
+  if (!std::isfinite(d.skin)) return why = "skin not finite", 1;
   for (int k = 0; k < 3; ++k) {
-    if (!(d.box[k] > 0)) return why = "box must be positive", 1;
+    if (!(d.box[k] > 0) || !std::isfinite(d.box[k])) return why = "box must be positive and finite", 1;
+    // bounds the cell grid (and the int conversions below) before any product
+    if (!(d.box[k] / d.cutoff < (double)kMaxGridCells))
+      return why = "box edge above " + std::to_string(kMaxGridCells) + " cutoffs", 1;
     if (int(d.box[k] / d.cutoff) < 3)
       return why = "box edge shorter than 3 cutoffs: the reference cell traversal double-counts there", 1;
   }
@@ -663,6 +667,24 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
       if (d.fconst[k] != d0.fconst[k] || d.uconst[k] != d0.uconst[k])
         return fail(1, "replicas of a batch must share the pair tables");
   }
+  // the list-cell grid of each replica (cells of side cutoff + skin, one
+  // extra per axis: a growing box coarsens the grid in derive_box), sized on
+  // the host before the device.  validate keeps each axis below kMaxGridCells
+  // cells; checked after each product (at most 2^56 + 2^28), the total stays
+  // an int.
+  const double skin = d0.skin > 0 ? d0.skin : 0.5;
+  std::vector<int> cell_caps(n_rep);
+  long long grid_cells = 0;
+  for (int r = 0; r < n_rep; ++r) {
+    long long cap = 1;
+    for (int k = 0; k < 3 && cap <= kMaxGridCells; ++k)
+      cap *= std::max(1LL, (long long)(descs[r].box[k] / (d0.cutoff + skin))) + 1;
+    if (cap > kMaxGridCells - grid_cells)
+      return fail(1, "replica " + std::to_string(r) + ": the cell grid of the handle exceeds " +
+                         std::to_string(kMaxGridCells) + " cells (box edges / (cutoff + skin))");
+    cell_caps[r] = (int)cap;
+    grid_cells += cap;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(2, "no CUDA device: the GB300 step has no CPU fallback");
@@ -670,7 +692,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
   h->mixed = (precision == SMD_MIXED);
   h->n_rep = n_rep;
   h->dt = d0.dt;
-  h->skin = d0.skin > 0 ? d0.skin : 0.5;
+  h->skin = skin;
   h->half_skin = 0.5 * h->skin;
   h->resize_rate = d0.resize_rate > 0 ? d0.resize_rate : 8;
   int total = 0;
@@ -736,8 +758,7 @@ int smd_create_batch(const smd_system_desc* descs, int n_rep, int precision, smd
     p.bead_end = bead + d.n;
     if (d.delta_lxy != 0) h->barostat = true;
     // one extra cell per axis: a growing box coarsens the grid in derive_box
-    int cap = 1;
-    for (int k = 0; k < 3; ++k) cap *= std::max(1, (int)(d.box[k] / T.list_cut)) + 1;
+    const int cap = cell_caps[r];
     p.cell_begin = cells;
     p.cell_cap = cap;
     cells += cap;

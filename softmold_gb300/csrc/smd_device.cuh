@@ -45,6 +45,7 @@ constexpr int kBlock = 256;
 // small CTAs spread a small system over every SM
 constexpr int kBeadBlock = 128;
 constexpr int kScanTile = 2048;  // cells per scan block (256 threads x 8)
+constexpr long long kMaxGridCells = 1LL << 28;  // list cells of one handle, all replicas together
 constexpr int kLanes = 8;        // lanes per bead in the list build and the pair pass
 constexpr int kMaxSpheres = 256; // BEAD or NANOCORE beads of one handle (one k_sphere block)
 constexpr int kBeadBrute = 20;   // BEAD residues up to this size take the brute-force branch

@@ -87,6 +87,10 @@ def _bad(**kw):
     ("inf gamma", "gamma, temperature"),
     ("negative temperature", "gamma, temperature"),
     ("nan bond", "BOND constant not finite"),
+    ("inf box", "box must be positive and finite"),
+    ("long box", "box edge above"),
+    ("sparse grid", "cell grid of the handle exceeds"),
+    ("inf skin", "skin not finite"),
 ])
 def test_invalid_descriptors_are_refused_before_any_device_work(built, change, message):
     """The descriptor checks run on the host before the device is touched,
@@ -133,6 +137,19 @@ def test_invalid_descriptors_are_refused_before_any_device_work(built, change, m
         m = _bad(temperature=-1.0)
     elif change == "nan bond":
         m = _bad(bonds=np.array([[0, 1]], np.int32), bond_consts=np.array([[0.7, np.nan]]))
+    elif change in ("inf box", "long box"):
+        box = np.array(g["box"], np.float64)
+        box[2] = np.inf if change == "inf box" else 1e12
+        m = _bad(box=box)
+    elif change == "sparse grid":
+        # the beads stay where they are in a 10,000^3 box: 4,000 list cells
+        # of cutoff 2 + skin 0.5 per axis, 6.4e10 in all, a count that
+        # overflows an int
+        m = _bad(box=np.full(3, 10000.0))
+    elif change == "inf skin":
+        with pytest.raises(smd.SmdError, match=message):
+            smd.System(_bad(), skin=np.inf)
+        return
     else:
         m = _bad(dt=0.0)
     with pytest.raises(smd.SmdError, match=message):
@@ -194,3 +211,23 @@ def test_reader_refusals(tmp_path):
     (tmp_path / "cut.mpd").write_text(txt[:len(txt) // 2])
     with pytest.raises(smd.SmdError):
         smd.read_mpd(str(tmp_path / "cut.mpd"))
+
+
+@pytest.mark.parametrize("old,new,message", [
+    ("nParticles 600", "nParticles -600", "Count for positions is negative"),
+    ("nParticles 600", "nParticles 2000000000", "Value after positions is missing"),
+    ("nTypes 6", "nTypes 100000", "nTypes must be in 0..4096"),
+    ("8\t 1", "8\t -1", "bond count out of range"),
+    ("8\t 1", "8\t 900000000", "bond count out of range"),
+])
+def test_reader_refuses_counts_before_allocating(tmp_path, old, new, message):
+    """Counts in a damaged file (negative, or more entries than the file
+    holds) are refused with a message before the reader sizes an array from
+    them, so that no allocation error escapes the C ABI."""
+    import softmold_gb300 as smd
+    from conftest import GOLDEN
+    txt = open(os.path.join(GOLDEN, "traj_bil", "bil.mpd")).read()
+    assert txt.count(old) == 1
+    (tmp_path / "bad.mpd").write_text(txt.replace(old, new))
+    with pytest.raises(smd.SmdError, match=message):
+        smd.read_mpd(str(tmp_path / "bad.mpd"))
