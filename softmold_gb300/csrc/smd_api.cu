@@ -1118,7 +1118,7 @@ int smd_set_state(smd_system* h, const double* pos, const double* vel) {
 }
 
 int smd_get_box(smd_system* h, int replica, double box[3]) {
-  if (!h || replica < 0 || replica >= h->n_rep) return fail(1, "bad replica");
+  if (!h || !box || replica < 0 || replica >= h->n_rep) return fail(1, "bad arguments");
   RepState rs;
   SMD_CUDA(cudaMemcpyAsync(&rs, h->P.rs + replica, sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
@@ -1129,7 +1129,8 @@ int smd_get_box(smd_system* h, int replica, double box[3]) {
 int smd_set_box(smd_system* h, int replica, const double box[3]) {
   if (!h || !box || replica < 0 || replica >= h->n_rep) return fail(1, "bad arguments");
   for (int k = 0; k < 3; ++k)
-    if (!(box[k] > 0) || int(box[k] / h->tab.rc) < 3) return fail(1, "box edge shorter than 3 cutoffs");
+    if (!(box[k] > 0) || !std::isfinite(box[k]) || int(box[k] / h->tab.rc) < 3)
+      return fail(1, "box edge not finite or shorter than 3 cutoffs");
   RepState rs;
   SMD_CUDA(cudaMemcpyAsync(&rs, h->P.rs + replica, sizeof(RepState), cudaMemcpyDeviceToHost, h->stream));
   SMD_CUDA(cudaStreamSynchronize(h->stream));
@@ -1233,7 +1234,10 @@ int smd_pair_list(smd_system* h, int* pairs, size_t cap, size_t* count) {
 
 int smd_set_noise_once(smd_system* h, const double* psi) {
   if (!h || !psi) return fail(1, "bad arguments");
-  SMD_CUDA(cudaMemcpy(h->P.ext_noise, psi, 3 * h->n * sizeof(double), cudaMemcpyHostToDevice));
+  // on the handle's stream: a step launched with SMD_ASYNC may still be
+  // reading the previous draws (the stream does not wait for the legacy one)
+  SMD_CUDA(cudaMemcpyAsync(h->P.ext_noise, psi, 3 * h->n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SMD_CUDA(cudaStreamSynchronize(h->stream));
   h->ext_noise_pending = true;
   return 0;
 }
@@ -1581,6 +1585,7 @@ long smd_mc_log(smd_system* h, int replica, long start, long max, double* fluct,
 
 int smd_set_temperature(smd_system* h, int replica, double kT, int update_sigma) {
   if (!h || replica < -1 || replica >= h->n_rep) return fail(1, "bad arguments");
+  if (!std::isfinite(kT) || kT < 0) return fail(1, "temperature must be finite and not negative");
   for (int r = 0; r < h->n_rep; ++r) {
     if (replica >= 0 && r != replica) continue;
     h->rp[r].kT = kT;
