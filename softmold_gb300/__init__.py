@@ -318,6 +318,7 @@ class System:
         self.n = sum(len(m.type) for m in systems)
         self.n_rep = len(systems)
         self.precision = precision
+        self._msd_groups = 0
 
     def close(self):
         if getattr(self, "h", None):
@@ -342,9 +343,17 @@ class System:
         _check(lib().smd_get_state(self.h, p.ctypes.data, v.ctypes.data), "smd_get_state")
         return p, v
 
+    def _sized(self, a, size, what):
+        """`a` as a C-contiguous float64 array of `size` values: the library
+        reads exactly that many from the pointer it gets."""
+        out = np.ascontiguousarray(a, np.float64)
+        if out.size != size:
+            raise ValueError(f"{what} must hold {size} values, got {out.size}")
+        return out
+
     def set_state(self, pos=None, vel=None):
-        pp = None if pos is None else np.ascontiguousarray(pos, np.float64)
-        vv = None if vel is None else np.ascontiguousarray(vel, np.float64)
+        pp = None if pos is None else self._sized(pos, 3 * self.n, "positions")
+        vv = None if vel is None else self._sized(vel, 3 * self.n, "velocities")
         _check(lib().smd_set_state(self.h, None if pp is None else pp.ctypes.data,
                                    None if vv is None else vv.ctypes.data), "smd_set_state")
 
@@ -354,7 +363,7 @@ class System:
         return b
 
     def set_box(self, box, replica=0):
-        b = np.ascontiguousarray(box, np.float64)
+        b = self._sized(box, 3, "box")
         _check(lib().smd_set_box(self.h, replica, b.ctypes.data), "smd_set_box")
 
     def forces(self, pair_only=False):
@@ -369,7 +378,7 @@ class System:
         return [dict(pair=x.pair, bonded=x.bonded, sphere=x.sphere, kinetic=x.kinetic) for x in e]
 
     def dU(self, scale):
-        s = np.ascontiguousarray(scale, np.float64)
+        s = self._sized(scale, 3, "scale")
         out = np.zeros(self.n_rep)
         _check(lib().smd_compute_dU(self.h, s.ctypes.data, out.ctypes.data), "smd_compute_dU")
         return out
@@ -409,7 +418,7 @@ class System:
                     mean_area_per_lipid=res.mean_area_per_lipid, grad_area=np.array(res.grad_area[:]))
 
     def hessian_vector(self, w):
-        ww = np.ascontiguousarray(w, np.float64)
+        ww = self._sized(w, 3 * self.n, "w")
         out = np.zeros((self.n, 3))
         _check(lib().smd_hessian_vector(self.h, ww.ctypes.data, out.ctypes.data), "smd_hessian_vector")
         return out
@@ -439,7 +448,7 @@ class System:
         return ms.value, k.value, n.value
 
     def set_noise_once(self, psi):
-        p = np.ascontiguousarray(psi, np.float64)
+        p = self._sized(psi, 3 * self.n, "psi")
         _check(lib().smd_set_noise_once(self.h, p.ctypes.data), "smd_set_noise_once")
 
     def set_stream(self, stream_handle: int | None):
@@ -456,7 +465,8 @@ class System:
         of the .dat files as a dict (and 'msd_sum' per group while diffusion
         is tracked)."""
         m = Measurement()
-        msd = np.zeros(max(n_groups, 1))
+        # the library writes one sum per group the handle holds
+        msd = np.zeros(max(self._msd_groups, 1))
         _check(lib().smd_measure(self.h, C.byref(m), msd.ctypes.data if n_groups else None), "smd_measure")
         out = dict(kinetic=m.kinetic, lo=np.array(m.lo[:]), hi=np.array(m.hi[:]), bond_length_sum=m.bond_length_sum,
                    n_bond=m.n_bond, bend_cos_sum=m.bend_cos_sum, bend_len0_sum=m.bend_len0_sum,
@@ -476,9 +486,14 @@ class System:
         _check(lib().smd_start_diffusion(self.h), "smd_start_diffusion")
 
     def set_msd_groups(self, offsets, beads):
-        o = np.ascontiguousarray(offsets, np.int32)
-        b = np.ascontiguousarray(beads, np.int32)
-        _check(lib().smd_set_msd_groups(self.h, len(o) - 1, o.ctypes.data, b.ctypes.data), "smd_set_msd_groups")
+        o = np.ascontiguousarray(offsets, np.int32).ravel()
+        b = np.ascontiguousarray(beads, np.int32).ravel()
+        # the library reads offsets[-1] bead indices
+        if len(o) < 1 or int(o[-1]) != len(b):
+            raise ValueError("offsets must end at len(beads)")
+        _check(lib().smd_set_msd_groups(self.h, len(o) - 1, o.ctypes.data, b.ctypes.data if len(b) else None),
+               "smd_set_msd_groups")
+        self._msd_groups = len(o) - 1
 
     def launches(self):
         return self.timing()[2]
@@ -494,9 +509,17 @@ class System:
 
 
 def mpd_update_state(in_path, out_path, pos, vel, box, time):
+    """Rewrites in_path's state into out_path (smd_mpd_update_state); pos and
+    vel hold the file's nParticles x 3 values, which the library reads."""
+    import re
+    with open(in_path) as f:
+        got = re.search(r"(?:^|\s)nParticles\s+(\d+)", f.read())
+    n3 = 3 * int(got.group(1)) if got else -1
     p = np.ascontiguousarray(pos, np.float64)
     v = np.ascontiguousarray(vel, np.float64)
     b = np.ascontiguousarray(box, np.float64)
+    if p.size != n3 or v.size != n3 or b.size != 3:
+        raise ValueError(f"positions and velocities must hold {n3} values (nParticles x 3) and box 3")
     _check(lib().smd_mpd_update_state(in_path.encode(), out_path.encode(), p.ctypes.data, v.ctypes.data,
                                       b.ctypes.data, float(time)), "smd_mpd_update_state")
 

@@ -231,3 +231,21 @@ def test_reader_refuses_counts_before_allocating(tmp_path, old, new, message):
     (tmp_path / "bad.mpd").write_text(txt.replace(old, new))
     with pytest.raises(smd.SmdError, match=message):
         smd.read_mpd(str(tmp_path / "bad.mpd"))
+
+
+def test_state_rewrite_checks_array_sizes(built, tmp_path):
+    """mpd_update_state hands the library pointers it reads nParticles x 3
+    values from: arrays of another size are refused before the call."""
+    import softmold_gb300 as smd
+    from conftest import GOLDEN
+    src = os.path.join(GOLDEN, "traj_bil", "bil.mpd")
+    m = smd.read_mpd(src)
+    n = len(m.type)
+    out = str(tmp_path / "out.mpd")
+    with pytest.raises(ValueError, match="nParticles"):
+        smd.mpd_update_state(src, out, np.zeros((n - 1, 3)), np.zeros((n, 3)), m.box, 1.0)
+    with pytest.raises(ValueError, match="box 3"):
+        smd.mpd_update_state(src, out, m.pos, m.vel, np.zeros(2), 1.0)
+    smd.mpd_update_state(src, out, m.pos, m.vel, m.box, 1.0)
+    back = smd.read_mpd(out)
+    assert np.array_equal(back.pos, m.pos) and back.initial_time == 1.0
