@@ -241,6 +241,13 @@ struct OracleMD {
   }
 };
 
+// A bead's kinetic energy beyond the measurement histogram ends the run.
+int blown_up() {
+  std::cout << "Error(MD): a bead's kinetic energy exceeds the measurement histogram ("
+            << smd::kMaxKeBins / 10000 << " per bead)\n";
+  return 1;
+}
+
 int run(const char* name, int threads, int timeSteps, double* elapsed) {
   OracleMD md;
   md.name = name;
@@ -288,7 +295,7 @@ int run(const char* name, int threads, int timeSteps, double* elapsed) {
       double bp;
       int nb;
       const double pot = md.total_potential(&bp, &nb);
-      obs.compute(S, S.initialTime, md.pos(), md.vel(), md.absPos.data(), pot, bp, nb);
+      if (obs.compute(S, S.initialTime, md.pos(), md.vel(), md.absPos.data(), pot, bp, nb)) return blown_up();
       smd::xyz_append_frame(frames, N, S.type.data(), md.pos(), err);
     } else {
       md.bead_mass_divide();
@@ -346,7 +353,7 @@ int run(const char* name, int threads, int timeSteps, double* elapsed) {
       double bp;
       int nb;
       const double pot = md.total_potential(&bp, &nb);
-      obs.compute(S, S.initialTime, md.pos(), md.vel(), md.absPos.data(), pot, bp, nb);
+      if (obs.compute(S, S.initialTime, md.pos(), md.vel(), md.absPos.data(), pot, bp, nb)) return blown_up();
       current = time(NULL);
     }
     // MC constant-tension box move (MD.cpp:589-721)

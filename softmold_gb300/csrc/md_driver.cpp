@@ -121,8 +121,12 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   if (feed_noise()) return die("smd_set_noise_once");
   if (smd_prepare(h, t0 ? 0 : 1, t0 ? &e0 : nullptr)) return die("smd_prepare");
   if (t0) {
-    obs.compute(S, S.initialTime, S.pos.data(), S.vel.data(), S.pos.data(), e0.pair + e0.bonded + e0.sphere,
-                e0.sphere, n_bead_res);
+    if (obs.compute(S, S.initialTime, S.pos.data(), S.vel.data(), S.pos.data(), e0.pair + e0.bonded + e0.sphere,
+                    e0.sphere, n_bead_res)) {
+      std::cout << "Error(MD): a bead's kinetic energy exceeds the measurement histogram (" << smd::kMaxKeBins / 10000
+                << " per bead)\n";
+      return 1;
+    }
     smd::xyz_append_frame(frames, N, S.type.data(), S.pos.data(), err);
   }
   std::cerr << "starting main loop: \n";

@@ -29,14 +29,15 @@ void msd_groups(const MpdSystem& sys, std::vector<int>& offsets, std::vector<int
   }
 }
 
-void Observables::compute(const MpdSystem& sys, double time, const double* p, const double* v,
-                          const double* ap, double pot, double bead_pot, int n_bead_res) {
+int Observables::compute(const MpdSystem& sys, double time, const double* p, const double* v,
+                         const double* ap, double pot, double bead_pot, int n_bead_res) {
   Measurement m;
-  aggregate(sys, p, v, ap, m);
+  if (int rc = aggregate(sys, p, v, ap, m)) return rc;
   write(sys, time, pot, bead_pot, n_bead_res, m);
+  return 0;
 }
 
-void Observables::aggregate(const MpdSystem& sys, const double* p, const double* v, const double* ap,
+int Observables::aggregate(const MpdSystem& sys, const double* p, const double* v, const double* ap,
                             Measurement& out) {
   const int n = sys.nParticles;
   const double* s = sys.size;
@@ -94,6 +95,11 @@ void Observables::aggregate(const MpdSystem& sys, const double* p, const double*
   if (ap) {
     // per-bead kinetic-energy histogram (dataExtraction.h:1509-1519)
     for (int i = 0; i < n; ++i) {
+      const double q = 0.5 * (v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]) /
+                       0.0001;
+      if (!(q < (double)kMaxKeBins)) return 1;  // converted to an int only in range
+    }
+    for (int i = 0; i < n; ++i) {
       const int part = (int)(0.5 * (v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] +
                                     v[3 * i + 2] * v[3 * i + 2]) /
                              0.0001);
@@ -118,6 +124,7 @@ void Observables::aggregate(const MpdSystem& sys, const double* p, const double*
       out.msd_sum[g] = msd;
     }
   }
+  return 0;
 }
 
 void Observables::write(const MpdSystem& sys, double time, double pot, double bead_pot, int n_bead_res,

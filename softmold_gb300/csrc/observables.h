@@ -38,6 +38,10 @@ struct Measurement {
 // entries.
 void msd_groups(const MpdSystem& sys, std::vector<int>& offsets, std::vector<int>& beads);
 
+// Kinetic-energy bins of 1e-4 the histogram holds at most (energies below
+// 6,710.8864 per bead), as the device measurement does.
+constexpr int kMaxKeBins = 1 << 26;
+
 class Observables {
  public:
   explicit Observables(const std::string& name) : name_(name) {}
@@ -46,13 +50,14 @@ class Observables {
   // unwrapped positions (may be null: no diffusion tracking and no
   // kinetic-energy histogram), time: current time.  pot: total potential
   // (pair + bonded + BEAD); bead_pot: BEAD part; n_bead_res: number of BEAD
-  // residues.
-  void compute(const MpdSystem& sys, double time, const double* pos, const double* vel,
+  // residues.  Returns nonzero, writing nothing, when a bead's kinetic energy
+  // lies beyond the histogram's kMaxKeBins bins (a run that has blown up).
+  int compute(const MpdSystem& sys, double time, const double* pos, const double* vel,
                const double* abs_pos, double pot, double bead_pot, int n_bead_res);
 
   // The aggregates compute() writes from (and the kinetic-energy histogram
-  // update when abs_pos is given).
-  void aggregate(const MpdSystem& sys, const double* pos, const double* vel, const double* abs_pos,
+  // update when abs_pos is given); nonzero as compute().
+  int aggregate(const MpdSystem& sys, const double* pos, const double* vel, const double* abs_pos,
                  Measurement& m);
 
   // Appends the measurement's lines to the .dat files.

@@ -51,3 +51,20 @@ def test_md_oracle_matches_reference_outputs(oracle, tmp_path, where, name):
     for f in want:
         assert got[f] == want[f], f
     assert "Resize acceptance ratio" in r.stderr
+
+
+def test_md_oracle_refuses_a_kinetic_energy_beyond_the_histogram(oracle, tmp_path):
+    """A bead whose kinetic energy lies beyond the measurement histogram's
+    2^26 bins of 1e-4 (a blown-up state) ends the run with a message at the
+    t = 0 measurement, as the device measurement does, before a bin index
+    is formed from it."""
+    from oracle_binding import MD
+    txt = open(os.path.join(TRAJ, "bil.mpd")).read()
+    head, tail = txt.split("velocities", 1)
+    vals = tail.split()
+    vals[0] = "200.0"  # 0.5 v^2 = 2e4 per bead: 2e8 bins
+    (tmp_path / "bil.mpd").write_text(head + "velocities\n" + " ".join(vals) + "\n")
+    r = subprocess.run([MD, "bil", "1"], cwd=tmp_path, env=dict(os.environ, OMP_NUM_THREADS="1"),
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert "exceeds the measurement histogram" in r.stdout
