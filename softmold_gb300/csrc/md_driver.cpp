@@ -72,6 +72,14 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   const int n_bead_res = res.n_bead_res;
   const bool perTypeGamma = res.per_type_gamma;
   const int N = S.nParticles;
+  // the step counts below are ints
+  const double max_steps = 2147483647.0;
+  if (!(S.deltaT > 0) || !(std::fabs(S.finalTime) / S.deltaT < max_steps) ||
+      !(std::fabs(S.initialTime) / S.deltaT < max_steps) || !(std::fabs(S.storeInterval) / S.deltaT < max_steps) ||
+      !(std::fabs(S.measureInterval) / S.deltaT < max_steps)) {
+    std::cout << "Error(MD): deltaT must be positive and every time below 2^31 steps\n";
+    return 1;
+  }
   const int endInt = int(S.finalTime / S.deltaT + 0.0000001);
   const int startInt = int(S.initialTime / S.deltaT + 0.0000001);
   const int storeint = int(S.storeInterval / S.deltaT + 0.0000001);
@@ -80,8 +88,10 @@ extern "C" int smd_md_main(const char* name_c, int precision) {
   double tempStep = 0;
   if (S.tempStepInterval > 0) {
     tempStep = S.tempStepInterval * (S.finalTemp - S.initialTemp) / (S.finalTime - S.initialTime);
-    // no ramp step when the interval exceeds the run (the count rounds to 0)
-    const int n_ramp = int((S.finalTime - S.initialTime) / (S.tempStepInterval));
+    // no ramp step when the interval exceeds the run (the count rounds to 0);
+    // a count of 2^31 or more gives a ramp every 0 steps, i.e. none, too
+    const double ramps = (S.finalTime - S.initialTime) / (S.tempStepInterval);
+    const int n_ramp = std::fabs(ramps) < max_steps ? int(ramps) : 0;
     tempStepInt = n_ramp > 0 ? (endInt - startInt) / n_ramp : 0;
   }
   if (storeint <= 0 || measureint <= 0) {

@@ -1,5 +1,6 @@
 #include "mpd_desc.h"
 
+#include <cmath>
 #include <exception>
 #include <initializer_list>
 #include <memory>
@@ -136,7 +137,9 @@ void mpd_descriptor(const MpdSystem& S, const MpdResidues& r, smd_system_desc& d
   d.tension = S.tension;
   d.delta_lxy = S.deltaLXY;
   d.resize_rate = 8;
-  d.first_step = int(S.initialTime / S.deltaT + 0.0000001);
+  // (a deltaT the library refuses gives step 0 here)
+  const double first = S.initialTime / S.deltaT + 0.0000001;
+  d.first_step = (S.deltaT > 0 && std::fabs(first) < 2147483647.0) ? int(first) : 0;
 }
 
 }  // namespace smd
