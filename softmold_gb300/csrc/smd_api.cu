@@ -28,11 +28,15 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+// A failed call also leaves its error as the runtime's last error, which the
+// next launch check would report as its own: it is read off here.
 #define SMD_CUDA(call)                                                                       \
   do {                                                                                       \
     cudaError_t e_ = (call);                                                                 \
-    if (e_ != cudaSuccess)                                                                   \
+    if (e_ != cudaSuccess) {                                                                 \
+      (void)cudaGetLastError();                                                              \
       return fail(100 + (int)e_, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+    }                                                                                        \
   } while (0)
 
 constexpr int kTrialChunk = 1024;  // barostat trials staged per upload
@@ -129,9 +133,16 @@ struct smd_system {
     void* q = nullptr;
     const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
     cudaError_t e = cudaMalloc(&q, bytes);
-    if (e != cudaSuccess) return fail(100 + (int)e, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();  // not the next launch's error
+      return fail(100 + (int)e, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
     e = cudaMemset(q, 0, bytes);
-    if (e != cudaSuccess) return fail(100 + (int)e, std::string("cudaMemset: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      cudaFree(q);
+      return fail(100 + (int)e, std::string("cudaMemset: ") + cudaGetErrorString(e));
+    }
     allocs.push_back(q);
     *p = (T*)q;
     return 0;
@@ -1849,7 +1860,7 @@ int smd_adjoint(smd_system* h, const smd_adjoint_spec* spec, smd_adjoint_result*
   auto& P = h->P;
   auto& A = h->adj;
   const int T = spec->steps, K = spec->checkpoint_every;
-  const int ncp = (T + K - 1) / K;
+  const int ncp = (int)(((long long)T + K - 1) / K);
   const size_t n3 = 3 * (size_t)h->n;
   const double dt = h->dt, invT = 1.0 / T;
   // derivative rows of Umin(a, b): the tables are linear in Umin
@@ -1881,6 +1892,7 @@ int smd_adjoint(smd_system* h, const smd_adjoint_spec* spec, smd_adjoint_result*
   if (cudaMalloc(&cp, (size_t)ncp * 2 * n3 * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&seg, (size_t)K * n3 * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&fin, 2 * n3 * sizeof(double)) != cudaSuccess) {
+    (void)cudaGetLastError();  // an allocation failure is not the next launch's error
     release();
     return fail(2, "cudaMalloc of the adjoint checkpoints failed");
   }

@@ -79,3 +79,19 @@ def test_refused_state_leaves_the_handle_unchanged(built, bad):
     p, v = s.state()
     assert np.isfinite(p).all() and np.isfinite(v).all()
     s.close()
+
+
+def test_failed_allocation_is_not_the_next_launchs_error(built):
+    """An adjoint whose checkpoints cannot be allocated (2^30 steps with a
+    checkpoint each: tens of terabytes) fails with its own error, and the
+    handle's next steps run: the failed cudaMalloc's error is not left as the
+    runtime's last error for the next launch check to report."""
+    m = mpd_from_golden(load_golden("bil400"))
+    m.delta_lxy = 0.0
+    s = smd.System(m)
+    s.prepare()
+    with pytest.raises(smd.SmdError, match="adjoint checkpoints"):
+        s.adjoint(1 << 30, checkpoint_every=1)
+    s.advance(8)
+    pos, vel = s.state()
+    assert np.isfinite(pos).all() and np.isfinite(vel).all()
