@@ -209,13 +209,18 @@ extern "C" int smd_pair_forces_static(const double* d_pos, const int* d_type, in
   }
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return error(100 + (int)e, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // reported here, not by the caller's next launch check
+    return error(100 + (int)e, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  }
   if (dev < 0 || dev >= kMaxDevices) return error(1, "smd_pair_forces_static: device index out of range");
   int* count = g_scratch_addr[dev].load(std::memory_order_acquire);
   if (!count) {
     e = cudaGetSymbolAddress((void**)&count, g_scratch);
-    if (e != cudaSuccess)
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
       return error(100 + (int)e, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    }
     g_scratch_addr[dev].store(count, std::memory_order_release);
   }
   if (n == 0) return 0;
