@@ -156,6 +156,16 @@ def test_invalid_descriptors_are_refused_before_any_device_work(built, change, m
         smd.System(m)
 
 
+def test_batch_cell_grid_is_bounded_over_all_replicas(built):
+    """Each of 60 replicas in a 427^3 box has 171^3 ≈ 5.0 M list cells (170
+    cells of cutoff 2 + skin 0.5 per axis, one extra), within the bound alone;
+    the 54th brings the handle past 2^28 cells and the batch is refused before
+    any device work."""
+    box = np.full(3, 427.0)
+    with pytest.raises(smd.SmdError, match="replica 53: the cell grid of the handle exceeds"):
+        smd.System([_bad(box=box)] * 60)
+
+
 def test_batch_replicas_must_share_the_pair_tables(built):
     a = _bad()
     f = np.array(a.fconst, np.float64).copy()
