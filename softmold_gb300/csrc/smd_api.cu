@@ -214,7 +214,10 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t
 #define SMD_PDL(h, ...)                                                                          \
   do {                                                                                           \
     const cudaError_t e_ = launch_pdl(__VA_ARGS__);                                              \
-    if (e_ != cudaSuccess) return fail(200 + (int)e_, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    if (e_ != cudaSuccess) {                                                                     \
+      (void)cudaGetLastError();                                                                  \
+      return fail(200 + (int)e_, std::string("kernel launch: ") + cudaGetErrorString(e_));       \
+    }                                                                                            \
     int rc_ = check_launch(h);                                                                   \
     if (rc_) return rc_;                                                                         \
   } while (0)
@@ -223,7 +226,10 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t
 #define SMD_PDL_INTEG(h, kern)                                                                   \
   do {                                                                                           \
     const cudaError_t e_ = launch_pdl_smem(kern, h->bead_grid(), kBeadBlock, h->sph_stage, h->stream, P, h->cur, se); \
-    if (e_ != cudaSuccess) return fail(200 + (int)e_, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    if (e_ != cudaSuccess) {                                                                     \
+      (void)cudaGetLastError();                                                                  \
+      return fail(200 + (int)e_, std::string("kernel launch: ") + cudaGetErrorString(e_));       \
+    }                                                                                            \
     int rc_ = check_launch(h);                                                                   \
     if (rc_) return rc_;                                                                         \
   } while (0)
@@ -1334,11 +1340,17 @@ int capture_period(smd_system* h, int cur0) {
     if (done) cudaGraphDestroy(done);
     return rc;
   }
-  if (e != cudaSuccess) return fail(100 + (int)e, std::string("graph capture: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // reported here, not by the next launch check
+    return fail(100 + (int)e, std::string("graph capture: ") + cudaGetErrorString(e));
+  }
   cudaGraphExec_t exec = nullptr;
   const cudaError_t e2 = cudaGraphInstantiate(&exec, done, 0);
   cudaGraphDestroy(done);
-  if (e2 != cudaSuccess) return fail(100 + (int)e2, std::string("graph instantiate: ") + cudaGetErrorString(e2));
+  if (e2 != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(100 + (int)e2, std::string("graph instantiate: ") + cudaGetErrorString(e2));
+  }
   h->graph[cur0].exec = exec;
   h->graph[cur0].kernels = (int)kernels;
   return 0;
