@@ -58,7 +58,7 @@ METRIC = "bead-steps/s on 1 GB300 (mixed precision)"
 UNIT = "bead-steps/s"
 E2E_INTERVAL = 48  # six barostat periods: one e2e step = upload, 48 MD steps, energies, download
 PERIOD = 8         # MD steps of one barostat period (resizeRate, MD.cpp:67)
-STEP_MD = 10 * PERIOD  # MD steps per bench step (the driver's 20 steps time > 100 ms)
+STEP_MD = 10 * PERIOD  # MD steps per bench step (20 bench steps take over 100 ms)
 SMS = 152          # GB300 streaming multiprocessors
 ISSUE_PER_SM_CLK = 4  # warp instructions issued per SM and clock (four schedulers)
 # DRAM bytes and warp instructions per bead and MD step of the mixed step,
